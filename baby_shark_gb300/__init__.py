@@ -1,0 +1,9 @@
+"""baby_shark_gb300 — GB300 (sm_103a) implementation of baby_shark's
+implicit-modelling path: mesh -> narrow-band SDF with fast-winding-number
+signs, SDF booleans and offset, dual-contouring extraction.
+
+The compute lives in libbs_gb300.so (csrc/, C ABI in include/baby_shark_gb300.h);
+this package is the host-side mirror of the reference's builder API.
+"""
+from .api import Context, DualContouringMesher, MeshToVolume, Volume, default_context  # noqa: F401
+from ._native import BsError  # noqa: F401

@@ -1,0 +1,234 @@
+"""Host-side API mirroring the reference crate's voxel builders.
+
+Names, argument meaning and failure behaviour follow baby_shark v0.3.12:
+
+  MeshToVolume        voxel/mesh_to_volume.rs:17-73
+  Volume              voxel/volume/mod.rs:11-123 (booleans consume both operands)
+  DualContouringMesher voxel/meshing/dual_contouring.rs:12-91
+  VoxelRemesher       remeshing/voxel.rs:44-95
+
+Where the reference returns `None` (empty mesh), these return None; every
+other failure raises BsError with the native status.  All compute runs in
+libbs_gb300.so on the GPU.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+class Context:
+    """A device + CUDA stream + memory pool (bs_ctx)."""
+
+    def __init__(self, device=0, stream=None):
+        self._lib = N.load()
+        h = C.c_void_p()
+        N.check(self._lib.bs_ctx_create(int(device), stream, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self._lib.bs_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        """The cudaStream_t the context runs on (as an int handle)."""
+        return self._lib.bs_ctx_stream(self.h)
+
+    def synchronize(self):
+        N.check(self._lib.bs_ctx_synchronize(self.h), self.h)
+
+    @property
+    def kernel_launches(self):
+        return int(self._lib.bs_ctx_kernel_launches(self.h))
+
+    def set_stage_timing(self, enable=True):
+        N.check(self._lib.bs_ctx_set_stage_timing(self.h, 1 if enable else 0), self.h)
+
+    def stage_times(self, reset=False):
+        """{kernel name: (total ms, launches)} recorded with CUDA events."""
+        n = C.c_int()
+        N.check(self._lib.bs_ctx_stage_count(self.h, C.byref(n)), self.h)
+        out = {}
+        for i in range(n.value):
+            name, ms, cnt = C.c_char_p(), C.c_double(), C.c_uint64()
+            N.check(self._lib.bs_ctx_stage_info(self.h, i, C.byref(name), C.byref(ms), C.byref(cnt)), self.h)
+            out[name.value.decode()] = (ms.value, cnt.value)
+        if reset:
+            N.check(self._lib.bs_ctx_stage_reset(self.h), self.h)
+        return out
+
+    def last_stats(self):
+        """Counters of the last mesh -> volume conversion."""
+        a = (C.c_uint64 * 8)()
+        N.check(self._lib.bs_ctx_last_stats(self.h, a), self.h)
+        keys = ["triangles", "subtris", "brick_pairs", "voxel_pairs", "leaves", "active_voxels"]
+        return dict(zip(keys, [int(x) for x in a]))
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _mesh_arrays(mesh):
+    """Accepts (vertices, faces) or an object with .vertices/.faces, or an (n,3,3) soup."""
+    if isinstance(mesh, tuple) and len(mesh) == 2:
+        v, f = mesh
+    elif hasattr(mesh, "vertices") and hasattr(mesh, "faces"):
+        v, f = mesh.vertices, mesh.faces
+    else:
+        soup = np.asarray(mesh, np.float32).reshape(-1, 3)
+        v, f = soup, np.arange(len(soup), dtype=np.uint32).reshape(-1, 3)
+    v = np.ascontiguousarray(v, np.float32).reshape(-1, 3)
+    f = np.ascontiguousarray(f, np.uint32).reshape(-1, 3)
+    return v, f
+
+
+class Volume:
+    """Narrow-band signed distance volume on the GPU (bs_volume)."""
+
+    def __init__(self, handle, ctx):
+        self.h = handle
+        self.ctx = ctx
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            try:
+                N.load().bs_volume_free(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+    def _take(self):
+        if self.h is None or not self.h.value:
+            raise ValueError("volume was consumed by a boolean operation")
+        h, self.h = self.h, None
+        return h
+
+    def voxel_size(self):
+        out = C.c_float()
+        N.check(N.load().bs_volume_voxel_size(self.h, C.byref(out)))
+        return out.value
+
+    def counts(self):
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        N.check(N.load().bs_volume_counts(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"leaves": a.value, "tiles": b.value, "active_voxels": c.value}
+
+    def clone(self):
+        out = C.c_void_p()
+        N.check(N.load().bs_volume_clone(self.ctx.h, self.h, C.byref(out)), self.ctx.h)
+        return Volume(out, self.ctx)
+
+    def export(self):
+        """(origins int32[n,3], values f32[n,512], masks uint32[n,16]) with leaves sorted by origin."""
+        n = self.counts()["leaves"]
+        o = np.zeros((n, 3), np.int32)
+        v = np.zeros((n, 512), np.float32)
+        m = np.zeros((n, 16), np.uint32)
+        N.check(N.load().bs_volume_export(self.ctx.h, self.h, o.ctypes.data, v.ctypes.data, m.ctypes.data),
+                self.ctx.h)
+        return o, v, m
+
+    def tiles(self):
+        n = self.counts()["tiles"]
+        o = np.zeros((n, 3), np.int32)
+        s = np.zeros(n, np.int32)
+        v = np.zeros(n, np.float32)
+        if n:
+            N.check(N.load().bs_volume_export_tiles(self.ctx.h, self.h, o.ctypes.data, s.ctypes.data,
+                                                    v.ctypes.data), self.ctx.h)
+        return o, s, v
+
+    def _csg(self, other, fn):
+        out = C.c_void_p()
+        a, b = self._take(), other._take()
+        N.check(fn(self.ctx.h, a, b, C.byref(out)), self.ctx.h)
+        return Volume(out, self.ctx)
+
+    def union(self, other):
+        """Volume::union (volume/mod.rs:74-79); consumes self and other."""
+        return self._csg(other, N.load().bs_volume_union)
+
+    def subtract(self, other):
+        """Volume::subtract (volume/mod.rs:88-93); consumes self and other."""
+        return self._csg(other, N.load().bs_volume_subtract)
+
+    def intersect(self, other):
+        """Volume::intersect (volume/mod.rs:81-86); consumes self and other."""
+        return self._csg(other, N.load().bs_volume_intersect)
+
+    def offset(self, distance):
+        """Volume::offset (volume/mod.rs:95-108)."""
+        N.check(N.load().bs_volume_offset(self.ctx.h, self.h, float(distance)), self.ctx.h)
+        return self
+
+
+class MeshToVolume:
+    """MeshToVolume (voxel/mesh_to_volume.rs:17-73)."""
+
+    def __init__(self, ctx=None):
+        self.ctx = ctx or default_context()
+        self.params = N.M2VParams()
+        N.load().bs_m2v_params_default(C.byref(self.params))
+
+    def with_voxel_size(self, size):
+        self.params.voxel_size = float(size)
+        return self
+
+    def with_narrow_band_width(self, width):
+        self.params.band_width = int(width)
+        return self
+
+    def set_voxel_size(self, size):
+        return self.with_voxel_size(size)
+
+    def set_narrow_band_width(self, width):
+        return self.with_narrow_band_width(width)
+
+    def convert(self, mesh):
+        """Returns a Volume, or None for an empty mesh (as the reference)."""
+        v, f = _mesh_arrays(mesh)
+        out = C.c_void_p()
+        st = N.load().bs_mesh_to_volume(self.ctx.h, v.ctypes.data, len(v), f.ctypes.data, len(f),
+                                        C.byref(self.params), C.byref(out))
+        if st == 2:  # BS_ERR_EMPTY
+            return None
+        N.check(st, self.ctx.h)
+        return Volume(out, self.ctx)
+
+
+class DualContouringMesher:
+    """DualContouringMesher (voxel/meshing/dual_contouring.rs:12-91)."""
+
+    def __init__(self):
+        self.voxel_size = 1.0
+
+    def with_voxel_size(self, size):
+        self.voxel_size = float(size)
+        return self
+
+    def mesh(self, volume):
+        """Triangle soup as float32[n, 3, 3] in world units."""
+        L = N.load()
+        n = C.c_uint64()
+        N.check(L.bs_dual_contour(volume.ctx.h, volume.h, self.voxel_size, None, 0, C.byref(n)), volume.ctx.h)
+        out = np.zeros((max(n.value, 1), 3, 3), np.float32)
+        N.check(L.bs_dual_contour(volume.ctx.h, volume.h, self.voxel_size, out.ctypes.data, n.value, C.byref(n)),
+                volume.ctx.h)
+        return out[: n.value]

@@ -1,0 +1,264 @@
+// Internal definitions shared by the CUDA translation units of
+// libbs_gb300.so: the context (device, stream, stream-ordered memory pool,
+// launch counter), the device layout of a volume, and IEEE-exact float
+// helpers used where results must match the reference bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/baby_shark_gb300.h"
+
+// ------------------------------------------------------------- context ----
+struct bs_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaMemPool_t pool = nullptr;
+  uint64_t launches = 0;
+  std::string last_error;
+  void* h_pinned = nullptr;  // small pinned staging area for size read-backs
+  size_t h_pinned_bytes = 0;
+  // optional per-stage timing with CUDA events on the context stream
+  bool timing = false;
+  struct Pending {
+    std::string name;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  struct Stage {
+    double ms = 0.0;
+    uint64_t launches = 0;
+  };
+  std::map<std::string, Stage> stages;
+  // counters of the last mesh -> volume call (see bs_ctx_last_stats)
+  uint64_t last_stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // lifetime: the caller's handle plus one reference per live volume, so a
+  // volume freed after bs_ctx_destroy still finds its stream and pool
+  int refs = 1;
+};
+
+// Drops one reference; the context is torn down with the last one.
+void bs_ctx_release(bs_ctx* ctx);
+
+namespace bs {
+
+struct Error {
+  bs_status status;
+  std::string msg;
+};
+
+// Throws Error on a CUDA failure; the C-ABI wrappers catch and translate.
+#define BS_CUDA(call)                                                                      \
+  do {                                                                                     \
+    cudaError_t e__ = (call);                                                              \
+    if (e__ != cudaSuccess) {                                                              \
+      throw ::bs::Error{e__ == cudaErrorMemoryAllocation ? BS_ERR_OOM : BS_ERR_CUDA,       \
+                        std::string(#call) + ": " + cudaGetErrorString(e__)};              \
+    }                                                                                      \
+  } while (0)
+
+#define BS_CHECK_LAUNCH(ctx)                                                               \
+  do {                                                                                     \
+    (ctx)->launches++;                                                                     \
+    cudaError_t e__ = cudaGetLastError();                                                  \
+    if (e__ != cudaSuccess)                                                                \
+      throw ::bs::Error{BS_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e__)}; \
+  } while (0)
+
+inline void fail(bs_status s, const std::string& m) { throw Error{s, m}; }
+
+// Launches one kernel (the `launch` statement), counts it, checks the launch
+// error and, when stage timing is on, brackets it with CUDA events.
+#define BS_KERNEL(ctx, name, launch)                                   \
+  do {                                                                 \
+    cudaEvent_t e0__ = nullptr;                                        \
+    if ((ctx)->timing) {                                               \
+      BS_CUDA(cudaEventCreate(&e0__));                                 \
+      BS_CUDA(cudaEventRecord(e0__, (ctx)->stream));                   \
+    }                                                                  \
+    launch;                                                            \
+    BS_CHECK_LAUNCH(ctx);                                              \
+    if ((ctx)->timing) {                                               \
+      cudaEvent_t e1__ = nullptr;                                      \
+      BS_CUDA(cudaEventCreate(&e1__));                                 \
+      BS_CUDA(cudaEventRecord(e1__, (ctx)->stream));                   \
+      (ctx)->pending.push_back(bs_ctx::Pending{name, e0__, e1__});     \
+    }                                                                  \
+  } while (0)
+
+// Stream-ordered device allocation from the context's pool.
+template <class T>
+T* dalloc(bs_ctx* ctx, size_t count) {
+  if (count == 0) count = 1;
+  void* p = nullptr;
+  BS_CUDA(cudaMallocFromPoolAsync(&p, count * sizeof(T), ctx->pool, ctx->stream));
+  return static_cast<T*>(p);
+}
+inline void dfree(bs_ctx* ctx, void* p) {
+  if (p) cudaFreeAsync(p, ctx->stream);
+}
+
+// RAII device buffer for temporaries of one call.
+template <class T>
+struct DBuf {
+  bs_ctx* ctx = nullptr;
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() {}
+  DBuf(bs_ctx* c, size_t count) : ctx(c), p(dalloc<T>(c, count)), n(count) {}
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : ctx(o.ctx), p(o.p), n(o.n) { o.p = nullptr; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    reset();
+    ctx = o.ctx; p = o.p; n = o.n; o.p = nullptr;
+    return *this;
+  }
+  ~DBuf() { reset(); }
+  void reset() {
+    if (p) dfree(ctx, p);
+    p = nullptr;
+    n = 0;
+  }
+  T* release() { T* q = p; p = nullptr; n = 0; return q; }
+  T* get() const { return p; }
+};
+
+// Reads `bytes` from device to host through the pinned staging area and
+// waits for the stream.
+void read_back(bs_ctx* ctx, void* host, const void* dev, size_t bytes);
+
+}  // namespace bs
+
+// ------------------------------------------------------------- volume -----
+// Leaves (8^3 bricks) sorted by origin (x, then y, then z).  Tiles are the
+// active constant regions of the reference's internal nodes (128^3 and
+// 4096^3 voxels); they only appear after boolean operations.
+struct bs_volume {
+  explicit bs_volume(bs_ctx* c) : ctx(c) { ctx->refs++; }
+  bs_volume(const bs_volume&) = delete;
+  bs_volume& operator=(const bs_volume&) = delete;
+  bs_ctx* ctx = nullptr;
+  float h = 1.0f;
+  uint64_t n_leaves = 0;
+  int4* d_origins = nullptr;   // [n] (x, y, z, 0)
+  float* d_values = nullptr;   // [n][512]
+  uint32_t* d_masks = nullptr; // [n][16]
+  uint64_t n_active = 0;
+  // active tiles
+  uint64_t n_tiles = 0;
+  int4* d_tiles = nullptr;     // [n] (x, y, z, size)
+  float* d_tile_values = nullptr;
+  // upper tree levels (see volume_ops.cu): kept for boolean semantics
+  struct Upper* upper = nullptr;
+  // cached dual-contouring output (world-unit triangles)
+  float* d_dc_tris = nullptr;
+  uint64_t n_dc_tris = 0;
+  bool dc_valid = false;
+  ~bs_volume();
+};
+
+namespace bs {
+
+// ------------------------------------------------ IEEE-exact float math ---
+// Each helper rounds once (round-to-nearest-even) and is never contracted
+// into a fused multiply-add, matching the reference's Rust f32 arithmetic.
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+
+struct F3 {
+  float x, y, z;
+};
+__device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__device__ __forceinline__ F3 add3(F3 a, F3 b) { return {fadd(a.x, b.x), fadd(a.y, b.y), fadd(a.z, b.z)}; }
+__device__ __forceinline__ F3 sub3(F3 a, F3 b) { return {fsub(a.x, b.x), fsub(a.y, b.y), fsub(a.z, b.z)}; }
+__device__ __forceinline__ F3 scale3(F3 a, float s) { return {fmul(a.x, s), fmul(a.y, s), fmul(a.z, s)}; }
+// (x1*x2 + y1*y2) + z1*z2
+__device__ __forceinline__ float dot3(F3 a, F3 b) {
+  return fadd(fadd(fmul(a.x, b.x), fmul(a.y, b.y)), fmul(a.z, b.z));
+}
+__device__ __forceinline__ F3 min3(F3 a, F3 b) {
+  return {a.x < b.x ? a.x : b.x, a.y < b.y ? a.y : b.y, a.z < b.z ? a.z : b.z};
+}
+__device__ __forceinline__ F3 max3(F3 a, F3 b) {
+  return {a.x > b.x ? a.x : b.x, a.y > b.y ? a.y : b.y, a.z > b.z ? a.z : b.z};
+}
+
+// Closest point on triangle (a, b, c) to p, Voronoi-region method of
+// Ericson, "Real-Time Collision Detection" 5.1.5, with the operation order of
+// triangle3.rs:317-382; returns |closest - p|^2 (before the square root of
+// the reference's norm(), mesh_to_volume.rs:155).  The square root is
+// monotonic and correctly rounded, so sqrt(min |.|^2) == min sqrt(|.|^2)
+// bit for bit and callers take it once per voxel.
+__device__ __forceinline__ float point_triangle_dist2(F3 a, F3 b, F3 c, F3 p) {
+  F3 ab = sub3(b, a), ac = sub3(c, a), ap = sub3(p, a);
+  float d1 = dot3(ab, ap), d2 = dot3(ac, ap);
+  F3 q;
+  if (d1 <= 0.0f && d2 <= 0.0f) {
+    q = a;
+  } else {
+    F3 bp = sub3(p, b);
+    float d3 = dot3(ab, bp), d4 = dot3(ac, bp);
+    if (d3 >= 0.0f && d4 <= d3) {
+      q = b;
+    } else {
+      float vc = fsub(fmul(d1, d4), fmul(d3, d2));
+      if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f) {
+        float v = fdiv(d1, fsub(d1, d3));
+        q = add3(a, scale3(ab, v));
+      } else {
+        F3 cp = sub3(p, c);
+        float d5 = dot3(ab, cp), d6 = dot3(ac, cp);
+        if (d6 >= 0.0f && d5 <= d6) {
+          q = c;
+        } else {
+          float vb = fsub(fmul(d5, d2), fmul(d1, d6));
+          if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f) {
+            float w = fdiv(d2, fsub(d2, d6));
+            q = add3(a, scale3(ac, w));
+          } else {
+            float va = fsub(fmul(d3, d6), fmul(d5, d4));
+            float d43 = fsub(d4, d3), d56 = fsub(d5, d6);
+            if (va <= 0.0f && d43 >= 0.0f && d56 >= 0.0f) {
+              float w = fdiv(d43, fadd(d43, d56));
+              q = add3(b, scale3(sub3(c, b), w));
+            } else {
+              float denom = fdiv(1.0f, fadd(fadd(va, vb), vc));
+              float v = fmul(vb, denom);
+              float w = fmul(vc, denom);
+              q = add3(add3(a, scale3(ab, v)), scale3(ac, w));
+            }
+          }
+        }
+      }
+    }
+  }
+  F3 d = sub3(q, p);
+  return dot3(d, d);
+}
+
+}  // namespace bs
+
+// Releases the upper-level (internal node) tables of a volume (volume_ops.cu).
+void bs_volume_free_upper(bs_volume* v);
+
+// Entry points implemented by the translation units (C++ linkage).
+namespace bs {
+bs_volume* mesh_to_volume_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri,
+                               uint64_t nt, const bs_m2v_params& p);
+void volume_release(bs_volume* v);
+bs_volume* volume_clone_impl(bs_ctx* ctx, const bs_volume* v);
+bs_volume* volume_csg_impl(bs_ctx* ctx, bs_volume* a, bs_volume* b, int op);
+void volume_offset_impl(bs_ctx* ctx, bs_volume* v, float distance);
+void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size);
+}  // namespace bs

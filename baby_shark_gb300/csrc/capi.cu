@@ -1,0 +1,332 @@
+// C ABI of libbs_gb300.so (include/baby_shark_gb300.h): contexts, volume
+// lifetime and export, and the status/exception boundary.  Every entry point
+// catches bs::Error (and std::bad_alloc) and returns a bs_status; nothing
+// throws across the C boundary.
+#include <cstring>
+#include <iterator>
+#include <new>
+
+#include "bs_internal.cuh"
+
+namespace bs {
+
+void read_back(bs_ctx* ctx, void* host, const void* dev, size_t bytes) {
+  if (bytes <= ctx->h_pinned_bytes) {
+    BS_CUDA(cudaMemcpyAsync(ctx->h_pinned, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    BS_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::memcpy(host, ctx->h_pinned, bytes);
+  } else {
+    BS_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    BS_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+}
+
+void volume_release(bs_volume* v) { delete v; }
+
+}  // namespace bs
+
+bs_volume::~bs_volume() {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  bs::dfree(ctx, d_origins);
+  bs::dfree(ctx, d_values);
+  bs::dfree(ctx, d_masks);
+  bs::dfree(ctx, d_tiles);
+  bs::dfree(ctx, d_tile_values);
+  bs::dfree(ctx, d_dc_tris);
+  bs_volume_free_upper(this);
+  bs_ctx_release(ctx);
+}
+
+void bs_ctx_release(bs_ctx* ctx) {
+  if (--ctx->refs > 0) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& p : ctx->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+namespace {
+
+template <class F>
+bs_status guarded(bs_ctx* ctx, F&& f) {
+  try {
+    if (ctx) {
+      BS_CUDA(cudaSetDevice(ctx->device));
+      ctx->last_error.clear();
+    }
+    f();
+    return BS_OK;
+  } catch (const bs::Error& e) {
+    if (ctx) ctx->last_error = e.msg;
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    if (ctx) ctx->last_error = "host allocation failed";
+    return BS_ERR_OOM;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bs_status_string(bs_status s) {
+  switch (s) {
+    case BS_OK: return "ok";
+    case BS_ERR_INVALID_ARG: return "invalid argument";
+    case BS_ERR_EMPTY: return "empty input";
+    case BS_ERR_OOM: return "out of device memory";
+    case BS_ERR_CAPACITY: return "capacity exceeded";
+    case BS_ERR_TIMEOUT: return "device wait timed out";
+    case BS_ERR_CUDA: return "CUDA error";
+    case BS_ERR_UNSUPPORTED: return "unsupported input";
+    case BS_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+bs_status bs_ctx_create(int device, void* stream, bs_ctx** out) {
+  if (!out) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return BS_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return BS_ERR_INVALID_ARG;
+  bs_ctx* ctx = new (std::nothrow) bs_ctx();
+  if (!ctx) return BS_ERR_OOM;
+  ctx->device = device;
+  bs_status st = guarded(nullptr, [&] {
+    BS_CUDA(cudaSetDevice(device));
+    if (stream) {
+      ctx->stream = static_cast<cudaStream_t>(stream);
+    } else {
+      BS_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+      ctx->own_stream = true;
+    }
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    BS_CUDA(cudaMemPoolCreate(&ctx->pool, &props));
+    uint64_t keep = ~uint64_t(0);  // keep freed blocks cached inside this pool
+    BS_CUDA(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    ctx->h_pinned_bytes = 4096;
+    BS_CUDA(cudaMallocHost(&ctx->h_pinned, ctx->h_pinned_bytes));
+  });
+  if (st != BS_OK) {
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return st;
+  }
+  *out = ctx;
+  return BS_OK;
+}
+
+bs_status bs_ctx_destroy(bs_ctx* ctx) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  bs_ctx_release(ctx);  // volumes still alive keep the context until they are freed
+  return BS_OK;
+}
+
+void* bs_ctx_stream(bs_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
+
+bs_status bs_ctx_synchronize(bs_ctx* ctx) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  return guarded(ctx, [&] { BS_CUDA(cudaStreamSynchronize(ctx->stream)); });
+}
+
+uint64_t bs_ctx_kernel_launches(const bs_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+const char* bs_ctx_last_error(const bs_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+bs_status bs_ctx_set_stage_timing(bs_ctx* ctx, int enable) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  ctx->timing = enable != 0;
+  return BS_OK;
+}
+
+static void resolve_stages(bs_ctx* ctx) {
+  for (auto& p : ctx->pending) {
+    float ms = 0.f;
+    BS_CUDA(cudaEventSynchronize(p.b));
+    BS_CUDA(cudaEventElapsedTime(&ms, p.a, p.b));
+    auto& st = ctx->stages[p.name];
+    st.ms += ms;
+    st.launches += 1;
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  ctx->pending.clear();
+}
+
+bs_status bs_ctx_stage_count(bs_ctx* ctx, int* n) {
+  if (!ctx || !n) return BS_ERR_INVALID_ARG;
+  return guarded(ctx, [&] {
+    resolve_stages(ctx);
+    *n = int(ctx->stages.size());
+  });
+}
+
+bs_status bs_ctx_stage_info(bs_ctx* ctx, int i, const char** name, double* total_ms, uint64_t* launches) {
+  if (!ctx || i < 0 || i >= int(ctx->stages.size())) return BS_ERR_INVALID_ARG;
+  auto it = ctx->stages.begin();
+  std::advance(it, i);
+  if (name) *name = it->first.c_str();
+  if (total_ms) *total_ms = it->second.ms;
+  if (launches) *launches = it->second.launches;
+  return BS_OK;
+}
+
+bs_status bs_ctx_stage_reset(bs_ctx* ctx) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  return guarded(ctx, [&] {
+    resolve_stages(ctx);
+    ctx->stages.clear();
+  });
+}
+
+bs_status bs_ctx_last_stats(const bs_ctx* ctx, uint64_t* out8) {
+  if (!ctx || !out8) return BS_ERR_INVALID_ARG;
+  for (int k = 0; k < 8; ++k) out8[k] = ctx->last_stats[k];
+  return BS_OK;
+}
+
+void bs_m2v_params_default(bs_m2v_params* p) {
+  if (!p) return;
+  p->voxel_size = 1.0f;   // MeshToVolume::default (mesh_to_volume.rs:223-236)
+  p->band_width = 0;
+  p->wn_beta = 2.0f;      // mesh_to_volume.rs:264
+  p->wn_threshold = 0.2f; // mesh_to_volume.rs:266
+}
+
+bs_status bs_mesh_to_volume_device(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri,
+                                   uint64_t nt, const bs_m2v_params* params, bs_volume** out) {
+  if (!ctx || !params || !out || (nt && (!d_xyz || !d_tri))) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  return guarded(ctx, [&] { *out = bs::mesh_to_volume_impl(ctx, d_xyz, nv, d_tri, nt, *params); });
+}
+
+bs_status bs_mesh_to_volume(bs_ctx* ctx, const float* h_xyz, uint64_t nv, const uint32_t* h_tri, uint64_t nt,
+                            const bs_m2v_params* params, bs_volume** out) {
+  if (!ctx || !params || !out || (nt && (!h_xyz || !h_tri))) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  return guarded(ctx, [&] {
+    if (nt == 0) bs::fail(BS_ERR_EMPTY, "mesh has no triangles");
+    bs::DBuf<float> xyz(ctx, 3 * nv);
+    bs::DBuf<uint32_t> tri(ctx, 3 * nt);
+    BS_CUDA(cudaMemcpyAsync(xyz.p, h_xyz, 3 * nv * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    BS_CUDA(cudaMemcpyAsync(tri.p, h_tri, 3 * nt * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
+    *out = bs::mesh_to_volume_impl(ctx, xyz.p, nv, tri.p, nt, *params);
+  });
+}
+
+bs_status bs_volume_free(bs_volume* v) {
+  if (!v) return BS_ERR_INVALID_ARG;
+  delete v;
+  return BS_OK;
+}
+
+bs_status bs_volume_voxel_size(const bs_volume* v, float* out) {
+  if (!v || !out) return BS_ERR_INVALID_ARG;
+  *out = v->h;
+  return BS_OK;
+}
+
+bs_status bs_volume_counts(const bs_volume* v, uint64_t* n_leaves, uint64_t* n_tiles, uint64_t* n_active) {
+  if (!v) return BS_ERR_INVALID_ARG;
+  if (n_leaves) *n_leaves = v->n_leaves;
+  if (n_tiles) *n_tiles = v->n_tiles;
+  if (n_active) *n_active = v->n_active;
+  return BS_OK;
+}
+
+bs_status bs_volume_clone(bs_ctx* ctx, const bs_volume* v, bs_volume** out) {
+  if (!ctx || !v || !out || v->ctx != ctx) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  return guarded(ctx, [&] { *out = bs::volume_clone_impl(ctx, v); });
+}
+
+bs_status bs_volume_export(bs_ctx* ctx, const bs_volume* v, int32_t* h_origins, float* h_values,
+                           uint32_t* h_masks) {
+  if (!ctx || !v || v->ctx != ctx) return BS_ERR_INVALID_ARG;
+  return guarded(ctx, [&] {
+    const uint64_t n = v->n_leaves;
+    if (n == 0) return;
+    if (h_origins) {
+      std::vector<int4> o(n);
+      BS_CUDA(cudaMemcpyAsync(o.data(), v->d_origins, n * sizeof(int4), cudaMemcpyDeviceToHost, ctx->stream));
+      BS_CUDA(cudaStreamSynchronize(ctx->stream));
+      for (uint64_t i = 0; i < n; ++i) {
+        h_origins[3 * i] = o[i].x;
+        h_origins[3 * i + 1] = o[i].y;
+        h_origins[3 * i + 2] = o[i].z;
+      }
+    }
+    if (h_values)
+      BS_CUDA(cudaMemcpyAsync(h_values, v->d_values, n * 512 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    if (h_masks)
+      BS_CUDA(cudaMemcpyAsync(h_masks, v->d_masks, n * 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    BS_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+bs_status bs_volume_export_tiles(bs_ctx* ctx, const bs_volume* v, int32_t* h_origins, int32_t* h_sizes,
+                                 float* h_values) {
+  if (!ctx || !v || v->ctx != ctx) return BS_ERR_INVALID_ARG;
+  return guarded(ctx, [&] {
+    const uint64_t n = v->n_tiles;
+    if (n == 0) return;
+    std::vector<int4> t(n);
+    BS_CUDA(cudaMemcpyAsync(t.data(), v->d_tiles, n * sizeof(int4), cudaMemcpyDeviceToHost, ctx->stream));
+    if (h_values)
+      BS_CUDA(cudaMemcpyAsync(h_values, v->d_tile_values, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    BS_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (uint64_t i = 0; i < n; ++i) {
+      if (h_origins) {
+        h_origins[3 * i] = t[i].x;
+        h_origins[3 * i + 1] = t[i].y;
+        h_origins[3 * i + 2] = t[i].z;
+      }
+      if (h_sizes) h_sizes[i] = t[i].w;
+    }
+  });
+}
+
+static bs_status csg(bs_ctx* ctx, bs_volume* a, bs_volume* b, bs_volume** out, int op) {
+  if (!ctx || !a || !b || !out || a == b || a->ctx != ctx || b->ctx != ctx) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  return guarded(ctx, [&] { *out = bs::volume_csg_impl(ctx, a, b, op); });
+}
+bs_status bs_volume_union(bs_ctx* ctx, bs_volume* a, bs_volume* b, bs_volume** out) { return csg(ctx, a, b, out, 0); }
+bs_status bs_volume_subtract(bs_ctx* ctx, bs_volume* a, bs_volume* b, bs_volume** out) { return csg(ctx, a, b, out, 1); }
+bs_status bs_volume_intersect(bs_ctx* ctx, bs_volume* a, bs_volume* b, bs_volume** out) { return csg(ctx, a, b, out, 2); }
+
+bs_status bs_volume_offset(bs_ctx* ctx, bs_volume* v, float distance) {
+  if (!ctx || !v || v->ctx != ctx) return BS_ERR_INVALID_ARG;
+  return guarded(ctx, [&] { bs::volume_offset_impl(ctx, v, distance); });
+}
+
+bs_status bs_dual_contour(bs_ctx* ctx, bs_volume* v, float voxel_size, float* h_tris, uint64_t capacity,
+                          uint64_t* n_tris) {
+  if (!ctx || !v || !n_tris || v->ctx != ctx || (capacity && !h_tris)) return BS_ERR_INVALID_ARG;
+  return guarded(ctx, [&] {
+    bs::dual_contour_impl(ctx, v, voxel_size);
+    *n_tris = v->n_dc_tris;
+    if (capacity >= v->n_dc_tris && v->n_dc_tris) {
+      BS_CUDA(cudaMemcpyAsync(h_tris, v->d_dc_tris, v->n_dc_tris * 9 * sizeof(float), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+      BS_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+  });
+}
+
+}  // extern "C"

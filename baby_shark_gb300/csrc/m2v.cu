@@ -1,0 +1,797 @@
+// Mesh -> narrow-band signed distance volume on the GPU.
+//
+// Replaces MeshToVolume::convert (voxel/mesh_to_volume.rs:52-73):
+//  1. subdivide every triangle until its sides are < 2 voxels
+//     (mesh_to_volume.rs:75-116), one thread per input triangle;
+//  2. bin sub-triangles into the 8^3 bricks their widened integer boxes
+//     overlap (mesh_to_volume.rs:124-143), through a dense brick directory
+//     over the mesh's brick extent: count, scan, fill;
+//  3. per brick, one CTA takes the minimum exact point–triangle distance of
+//     every voxel over the sub-triangles whose box contains it
+//     (mesh_to_volume.rs:147-195) — the active set is the union of the boxes;
+//  4. sign every active voxel with a fast winding number (order-1 + order-2
+//     far field, beta = 2, threshold 0.2; mesh_to_volume.rs:245-280) over an
+//     LBVH of the original triangles (Morton codes, radix sort, Karras
+//     hierarchy, bottom-up coefficient refit).
+// Steps 1-3 use IEEE-exact arithmetic (bs_internal.cuh) so distances and the
+// active set match the reference bit for bit.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <algorithm>
+#include <cmath>
+
+#include "bs_internal.cuh"
+
+namespace bs {
+
+// ------------------------------------------------------------ helpers -----
+template <class T>
+static void exclusive_scan(bs_ctx* ctx, const T* in, T* out, size_t n) {
+  size_t tmp = 0;
+  BS_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, in, out, n, ctx->stream));
+  DBuf<uint8_t> t(ctx, tmp);
+  BS_CUDA(cub::DeviceScan::ExclusiveSum(t.p, tmp, in, out, n, ctx->stream));
+}
+
+__device__ __forceinline__ uint32_t f2ord(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ __forceinline__ float ord2f(uint32_t u) {
+  uint32_t v = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+  float f;
+  memcpy(&f, &v, 4);
+  return f;
+}
+
+struct M2VStats {
+  int vmin[3];        // conservative voxel extent of all widened boxes
+  int vmax[3];
+  uint32_t cmin[3];   // ordered-int bbox of triangle centroids
+  uint32_t cmax[3];
+  int error;          // 1: vertex index out of range, 2: sub-triangle outside directory,
+                      // 3: traversal stack overflow, 4: coordinates out of int range
+  int pad;
+  unsigned long long n_sub;    // 64-bit totals (the scans run in 32 bit)
+  unsigned long long n_pairs;  // (brick, sub-triangle) pairs
+  unsigned long long n_vpairs; // (voxel, sub-triangle) pairs = sum of widened box volumes
+};
+
+struct SubTri {  // 64 B: vertices and the widened inclusive integer box
+  float4 p0;     // a.x a.y a.z b.x
+  float4 p1;     // b.y b.z c.x c.y
+  float4 p2;     // c.z, -, -, -
+  int4 lo;       // box min (x, y, z), -
+  int4 hi;       // box max
+};
+
+// ------------------------------------------- 1. triangles and subdivision --
+__global__ void k_gather(const float* __restrict__ xyz, uint64_t nv, const uint32_t* __restrict__ tri,
+                         uint64_t nt, float h, float inv_h, int band, float4* __restrict__ T,
+                         uint32_t* __restrict__ nsub, M2VStats* st) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= nt) {
+    if (i == nt) nsub[nt] = 0;
+    return;
+  }
+  uint32_t ia = tri[3 * i], ib = tri[3 * i + 1], ic = tri[3 * i + 2];
+  if (ia >= nv || ib >= nv || ic >= nv) {
+    atomicExch(&st->error, 1);
+    nsub[i] = 0;
+    T[3 * i] = T[3 * i + 1] = T[3 * i + 2] = make_float4(0, 0, 0, 0);
+    return;
+  }
+  F3 a = f3(xyz[3 * ia], xyz[3 * ia + 1], xyz[3 * ia + 2]);
+  F3 b = f3(xyz[3 * ib], xyz[3 * ib + 1], xyz[3 * ib + 2]);
+  F3 c = f3(xyz[3 * ic], xyz[3 * ic + 1], xyz[3 * ic + 2]);
+  T[3 * i] = make_float4(a.x, a.y, a.z, 0.f);
+  T[3 * i + 1] = make_float4(b.x, b.y, b.z, 0.f);
+  T[3 * i + 2] = make_float4(c.x, c.y, c.z, 0.f);
+  // triangle3.rs:117-124 and mesh_to_volume.rs:76-88
+  F3 e0 = sub3(b, a), e1 = sub3(c, a), e2 = sub3(c, b);
+  float m = fmaxf(fmaxf(dot3(e0, e0), dot3(e1, e1)), dot3(e2, e2));
+  float ns = floorf(fdiv(fsqrt(m), h));
+  // n^2 sub-triangles in exact integer arithmetic (k_subdivide writes exactly n^2)
+  uint32_t cnt;
+  if (!(ns >= 2.0f)) {
+    cnt = 1;
+  } else if (!(ns < 65536.0f)) {
+    cnt = 0;
+    atomicExch(&st->error, 4);
+  } else {
+    uint32_t n = uint32_t(ns);
+    cnt = n * n;
+  }
+  nsub[i] = cnt;
+  {
+    unsigned long long wsum = cnt;
+    unsigned mask = __activemask();
+    for (int o = 16; o > 0; o >>= 1) wsum += __shfl_down_sync(mask, wsum, o);
+    if ((threadIdx.x & 31) == __ffs(mask) - 1) atomicAdd(&st->n_sub, wsum);
+  }
+  F3 mn = min3(c, min3(a, b)), mx = max3(c, max3(a, b));
+  float lo[3] = {mn.x, mn.y, mn.z}, hi[3] = {mx.x, mx.y, mx.z};
+  for (int k = 0; k < 3; ++k) {
+    float fl = floorf(fmul(lo[k], inv_h)), fh = ceilf(fmul(hi[k], inv_h));
+    if (!(fabsf(fl) < 1.0e9f) || !(fabsf(fh) < 1.0e9f)) {
+      atomicExch(&st->error, 4);
+      continue;
+    }
+    atomicMin(&st->vmin[k], int(fl) - band - 3);
+    atomicMax(&st->vmax[k], int(fh) + band + 3);
+  }
+  F3 cen = f3((a.x + b.x + c.x) * (1.0f / 3.0f), (a.y + b.y + c.y) * (1.0f / 3.0f),
+              (a.z + b.z + c.z) * (1.0f / 3.0f));
+  atomicMin(&st->cmin[0], f2ord(cen.x));
+  atomicMin(&st->cmin[1], f2ord(cen.y));
+  atomicMin(&st->cmin[2], f2ord(cen.z));
+  atomicMax(&st->cmax[0], f2ord(cen.x));
+  atomicMax(&st->cmax[1], f2ord(cen.y));
+  atomicMax(&st->cmax[2], f2ord(cen.z));
+}
+
+__device__ __forceinline__ void widened_box(F3 a, F3 b, F3 c, float inv_h, int band, int lo[3], int hi[3]) {
+  F3 mn = min3(c, min3(a, b)), mx = max3(c, max3(a, b));
+  lo[0] = int(floorf(fmul(mn.x, inv_h))) - band;
+  lo[1] = int(floorf(fmul(mn.y, inv_h))) - band;
+  lo[2] = int(floorf(fmul(mn.z, inv_h))) - band;
+  hi[0] = int(ceilf(fmul(mx.x, inv_h))) + band;
+  hi[1] = int(ceilf(fmul(mx.y, inv_h))) + band;
+  hi[2] = int(ceilf(fmul(mx.z, inv_h))) + band;
+  if (hi[0] == lo[0] || hi[1] == lo[1] || hi[2] == lo[2]) {
+    for (int k = 0; k < 3; ++k) {
+      lo[k] -= 1;
+      hi[k] += 1;
+    }
+  }
+}
+
+__device__ __forceinline__ void put_subtri(SubTri* S, uint64_t idx, F3 a, F3 b, F3 c, float inv_h, int band) {
+  int lo[3], hi[3];
+  widened_box(a, b, c, inv_h, band, lo, hi);
+  SubTri s;
+  s.p0 = make_float4(a.x, a.y, a.z, b.x);
+  s.p1 = make_float4(b.y, b.z, c.x, c.y);
+  s.p2 = make_float4(c.z, 0.f, 0.f, 0.f);
+  s.lo = make_int4(lo[0], lo[1], lo[2], 0);
+  s.hi = make_int4(hi[0], hi[1], hi[2], 0);
+  S[idx] = s;
+}
+
+// mesh_to_volume.rs:75-116, same stepping and accumulation order.
+__global__ void k_subdivide(const float4* __restrict__ T, const uint32_t* __restrict__ nsub,
+                            const uint32_t* __restrict__ off, uint64_t nt, float h, float inv_h, int band,
+                            SubTri* __restrict__ S) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= nt || nsub[i] == 0) return;
+  float4 ta = T[3 * i], tb = T[3 * i + 1], tc = T[3 * i + 2];
+  F3 p1 = f3(ta.x, ta.y, ta.z), p2 = f3(tb.x, tb.y, tb.z), p3 = f3(tc.x, tc.y, tc.z);
+  uint64_t o = off[i];
+  if (nsub[i] == 1) {
+    put_subtri(S, o, p1, p2, p3, inv_h, band);
+    return;
+  }
+  F3 e0 = sub3(p2, p1), e1 = sub3(p3, p1), e2 = sub3(p3, p2);
+  float m = fmaxf(fmaxf(dot3(e0, e0), dot3(e1, e1)), dot3(e2, e2));
+  float ns = floorf(fdiv(fsqrt(m), h));
+  float inv = fdiv(1.0f, ns);
+  F3 s1 = scale3(sub3(p2, p1), inv);
+  F3 s2 = scale3(sub3(p3, p2), inv);
+  F3 a = p1;
+  uint32_t n = uint32_t(ns);
+  for (uint32_t r = 0; r < n; ++r) {
+    F3 b = add3(a, s1);
+    F3 c = add3(b, s2);
+    F3 a_s = add3(a, s2), b_s = add3(b, s2), c_s = add3(c, s2);
+    F3 a_prev = a;
+    for (uint32_t k = 0; k < r; ++k) {
+      put_subtri(S, o++, a_prev, b_s, a_s, inv_h, band);
+      put_subtri(S, o++, a_s, b_s, c_s, inv_h, band);
+      a_prev = a_s;
+      a_s = add3(a_s, s2);
+      b_s = add3(b_s, s2);
+      c_s = add3(c_s, s2);
+    }
+    put_subtri(S, o++, a, b, c, inv_h, band);
+    a = add3(a, s1);
+  }
+}
+
+// ------------------------------------------------- 2. brick directory -----
+struct Dir {
+  int bx0, by0, bz0;  // brick coordinate of entry 0
+  int dx, dy, dz;     // extent in bricks
+};
+
+__device__ __forceinline__ bool brick_range(const SubTri& s, const Dir& d, int lo[3], int hi[3]) {
+  lo[0] = (s.lo.x >> 3) - d.bx0; hi[0] = (s.hi.x >> 3) - d.bx0;
+  lo[1] = (s.lo.y >> 3) - d.by0; hi[1] = (s.hi.y >> 3) - d.by0;
+  lo[2] = (s.lo.z >> 3) - d.bz0; hi[2] = (s.hi.z >> 3) - d.bz0;
+  return lo[0] >= 0 && lo[1] >= 0 && lo[2] >= 0 && hi[0] < d.dx && hi[1] < d.dy && hi[2] < d.dz;
+}
+
+__global__ void k_count_pairs(const SubTri* __restrict__ S, uint64_t ns, Dir d, uint32_t* __restrict__ cnt,
+                              M2VStats* st) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= ns) return;
+  SubTri s = S[i];
+  int lo[3], hi[3];
+  if (!brick_range(s, d, lo, hi)) {
+    atomicExch(&st->error, 2);
+    return;
+  }
+  for (int x = lo[0]; x <= hi[0]; ++x)
+    for (int y = lo[1]; y <= hi[1]; ++y)
+      for (int z = lo[2]; z <= hi[2]; ++z)
+        atomicAdd(&cnt[(uint64_t(x) * d.dy + y) * d.dz + z], 1u);
+  unsigned long long np = uint64_t(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+  unsigned long long vp = uint64_t(s.hi.x - s.lo.x + 1) * (s.hi.y - s.lo.y + 1) * (s.hi.z - s.lo.z + 1);
+  unsigned mask = __activemask();
+  for (int o = 16; o > 0; o >>= 1) {
+    np += __shfl_down_sync(mask, np, o);
+    vp += __shfl_down_sync(mask, vp, o);
+  }
+  if ((threadIdx.x & 31) == __ffs(mask) - 1) {
+    atomicAdd(&st->n_pairs, np);
+    atomicAdd(&st->n_vpairs, vp);
+  }
+}
+
+__global__ void k_dir_flags(const uint32_t* __restrict__ cnt, uint64_t n, uint32_t* __restrict__ flag) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i < n) flag[i] = cnt[i] ? 1u : 0u;
+  if (i == n) flag[n] = 0u;
+}
+
+// Compacts non-empty directory entries into bricks in (x, y, z) order and
+// turns cnt[] into per-entry fill cursors.
+__global__ void k_dir_compact(uint32_t* __restrict__ cnt, const uint32_t* __restrict__ pair_off,
+                              const uint32_t* __restrict__ bidx, uint64_t n, Dir d, int4* __restrict__ origins,
+                              uint32_t* __restrict__ list_off) {
+  uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (e >= n) return;
+  if (cnt[e]) {
+    uint32_t b = bidx[e];
+    int z = int(e % d.dz), y = int((e / d.dz) % d.dy), x = int(e / (uint64_t(d.dz) * d.dy));
+    origins[b] = make_int4((x + d.bx0) * 8, (y + d.by0) * 8, (z + d.bz0) * 8, 0);
+    list_off[b] = pair_off[e];
+  }
+  cnt[e] = pair_off[e];
+}
+
+__global__ void k_fill_pairs(const SubTri* __restrict__ S, uint64_t ns, Dir d, uint32_t* __restrict__ cursor,
+                             uint32_t* __restrict__ list) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= ns) return;
+  SubTri s = S[i];
+  int lo[3], hi[3];
+  if (!brick_range(s, d, lo, hi)) return;
+  for (int x = lo[0]; x <= hi[0]; ++x)
+    for (int y = lo[1]; y <= hi[1]; ++y)
+      for (int z = lo[2]; z <= hi[2]; ++z) {
+        uint32_t p = atomicAdd(&cursor[(uint64_t(x) * d.dy + y) * d.dz + z], 1u);
+        list[p] = uint32_t(i);
+      }
+}
+
+// ----------------------------------------------- 3. per-brick distances ----
+// One CTA of 128 threads per brick.  Each warp takes sub-triangles of the
+// brick's list in turn and its lanes walk only the voxels of (widened box of
+// the sub-triangle) x (brick); the per-voxel minimum is kept in shared memory
+// with atomicMin on the float bits (distances are >= 0, so unsigned order is
+// float order; NaN distances are skipped, as `dist < cur` never holds for NaN
+// in the reference).
+constexpr int DIST_THREADS = 128;
+
+__global__ void __launch_bounds__(DIST_THREADS) k_brick_distance(
+    const int4* __restrict__ origins, const uint32_t* __restrict__ list_off, const uint32_t* __restrict__ list,
+    const SubTri* __restrict__ S, float h, float* __restrict__ values, uint32_t* __restrict__ masks) {
+  __shared__ uint32_t dmin[512];
+  const int b = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int4 org = origins[b];
+  for (int o = t; o < 512; o += DIST_THREADS) dmin[o] = 0x7f800000u;  // +inf
+  __syncthreads();
+  const uint32_t beg = list_off[b], end = list_off[b + 1];
+  for (uint32_t e = beg + warp; e < end; e += DIST_THREADS / 32) {
+    const SubTri& st = S[list[e]];
+    const float4 q0 = st.p0, q1 = st.p1, q2 = st.p2;
+    const int4 lo = st.lo, hi = st.hi;
+    const F3 a = f3(q0.x, q0.y, q0.z), bb = f3(q0.w, q1.x, q1.y), c = f3(q1.z, q1.w, q2.x);
+    const int x0 = max(lo.x, org.x), y0 = max(lo.y, org.y), z0 = max(lo.z, org.z);
+    const int nx = min(hi.x, org.x + 7) - x0 + 1, ny = min(hi.y, org.y + 7) - y0 + 1,
+              nz = min(hi.z, org.z + 7) - z0 + 1;
+    if (nx <= 0 || ny <= 0 || nz <= 0) continue;
+    const int nyz = ny * nz, cnt = nx * nyz;
+    // k -> (ix, iy, iz) by reciprocal multiply: k < 512 and nyz <= 64 keep the
+    // product at least 0.5/64 away from the next integer, far above float error
+    const float rnyz = 1.0f / float(nyz), rnz = 1.0f / float(nz);
+    for (int k = lane; k < cnt; k += 32) {
+      const int ix = int((float(k) + 0.5f) * rnyz), r = k - ix * nyz;
+      const int iy = int((float(r) + 0.5f) * rnz), iz = r - iy * nz;
+      const int x = x0 + ix, y = y0 + iy, z = z0 + iz;
+      const F3 g = f3(fmul(__int2float_rn(x), h), fmul(__int2float_rn(y), h), fmul(__int2float_rn(z), h));
+      const float d2 = point_triangle_dist2(a, bb, c, g);
+      if (d2 < __int_as_float(0x7f800000)) {  // false for NaN and +inf
+        const int o = ((x - org.x) << 6) | ((y - org.y) << 3) | (z - org.z);
+        atomicMin(&dmin[o], __float_as_uint(d2));
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int o = t + DIST_THREADS * k;
+    const uint32_t u = dmin[o];
+    const float dist = fsqrt(__uint_as_float(u));
+    const bool act = dist < __int_as_float(0x7f800000);  // sqrt of a finite square can overflow to inf
+    const uint32_t m = __ballot_sync(0xffffffffu, act);
+    values[uint64_t(b) * 512 + o] = act ? dist : 0.0f;
+    if (lane == 0) masks[uint64_t(b) * 16 + warp + 4 * k] = m;
+  }
+}
+
+// ------------------------------------------------- active voxel list ------
+__global__ void k_brick_popcount(const uint32_t* __restrict__ masks, uint64_t nb, uint32_t* __restrict__ cnt) {
+  uint64_t b = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (b > nb) return;
+  if (b == nb) { cnt[nb] = 0; return; }
+  uint32_t c = 0;
+#pragma unroll
+  for (int w = 0; w < 16; ++w) c += __popc(masks[b * 16 + w]);
+  cnt[b] = c;
+}
+
+// one warp per brick: lane l handles mask words l (l < 16)
+__global__ void k_emit_active(const uint32_t* __restrict__ masks, const uint32_t* __restrict__ off, uint64_t nb,
+                              uint32_t* __restrict__ act) {
+  uint64_t b = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (b >= nb) return;
+  uint32_t m = lane < 16 ? masks[b * 16 + lane] : 0u;
+  uint32_t c = __popc(m);
+  uint32_t pre = c;
+#pragma unroll
+  for (int s = 1; s < 32; s <<= 1) {
+    uint32_t v = __shfl_up_sync(0xffffffffu, pre, s);
+    if (lane >= s) pre += v;
+  }
+  uint32_t pos = off[b] + pre - c;
+  while (m) {
+    int bit = __ffs(m) - 1;
+    m &= m - 1;
+    act[pos++] = uint32_t(b << 9) | uint32_t(lane * 32 + bit);
+  }
+}
+
+// ------------------------------------------------------ 4. LBVH + WN ------
+// Internal node record: 5 float4
+//   [0] dipole centre p (xyz), radius r
+//   [1] order-1 coefficient a (xyz), trace(B)
+//   [2] B00 B01 B02 B10   [3] B11 B12 B20 B21   [4] B22, left, right (int bits), -
+// Leaf record (one triangle, sorted order): 5 float4
+//   [0] centroid (xyz), radius   [1] a = area * normal (xyz), -   [2..4] vertices
+// Child encoding: >= 0 internal node index, < 0 leaf ~index.
+struct Sums {  // area-weighted moments of a subtree
+  float ax, ay, az;           // sum area * n
+  float cx, cy, cz;           // sum area * centroid
+  float s;                    // sum area
+  float m[9];                 // sum centroid * (area n)^T, row-major
+  float lo[3], hi[3];         // bbox
+};
+
+__device__ __forceinline__ uint64_t expand21(uint64_t v) {
+  v &= 0x1fffffull;
+  v = (v | v << 32) & 0x1f00000000ffffull;
+  v = (v | v << 16) & 0x1f0000ff0000ffull;
+  v = (v | v << 8) & 0x100f00f00f00f00full;
+  v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+  v = (v | v << 2) & 0x1249249249249249ull;
+  return v;
+}
+
+__global__ void k_morton(const float4* __restrict__ T, uint64_t nt, const M2VStats* st, uint64_t* __restrict__ keys,
+                         uint32_t* __restrict__ vals) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= nt) return;
+  float4 a = T[3 * i], b = T[3 * i + 1], c = T[3 * i + 2];
+  float cen[3] = {(a.x + b.x + c.x) * (1.0f / 3.0f), (a.y + b.y + c.y) * (1.0f / 3.0f),
+                  (a.z + b.z + c.z) * (1.0f / 3.0f)};
+  uint64_t q[3];
+  for (int k = 0; k < 3; ++k) {
+    float lo = ord2f(st->cmin[k]), hi = ord2f(st->cmax[k]);
+    float ext = hi - lo;
+    float u = ext > 0.f ? (cen[k] - lo) / ext : 0.5f;
+    u = fminf(fmaxf(u, 0.f), 1.f);
+    q[k] = uint64_t(fminf(u * 2097152.0f, 2097151.0f));
+  }
+  keys[i] = (expand21(q[0]) << 2) | (expand21(q[1]) << 1) | expand21(q[2]);
+  vals[i] = uint32_t(i);
+}
+
+__global__ void k_leaves(const float4* __restrict__ T, const uint32_t* __restrict__ order, uint64_t nt,
+                         float4* __restrict__ leaf, Sums* __restrict__ lsum) {
+  uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= nt) return;
+  uint32_t t = order[i];
+  float4 A = T[3 * t], B = T[3 * t + 1], C = T[3 * t + 2];
+  float ex = B.x - A.x, ey = B.y - A.y, ez = B.z - A.z;
+  float fx = C.x - A.x, fy = C.y - A.y, fz = C.z - A.z;
+  float nx = ey * fz - ez * fy, ny = ez * fx - ex * fz, nz = ex * fy - ey * fx;
+  float len = sqrtf(nx * nx + ny * ny + nz * nz);
+  Sums s;
+  float area = 0.5f * len;
+  s.ax = 0.5f * nx; s.ay = 0.5f * ny; s.az = 0.5f * nz;
+  if (!(len > 0.f)) { s.ax = s.ay = s.az = 0.f; area = 0.f; }
+  float cx = (A.x + B.x + C.x) * (1.0f / 3.0f), cy = (A.y + B.y + C.y) * (1.0f / 3.0f),
+        cz = (A.z + B.z + C.z) * (1.0f / 3.0f);
+  s.s = area;
+  s.cx = area * cx; s.cy = area * cy; s.cz = area * cz;
+  float cc[3] = {cx, cy, cz}, aa[3] = {s.ax, s.ay, s.az};
+  for (int r = 0; r < 3; ++r)
+    for (int q = 0; q < 3; ++q) s.m[3 * r + q] = cc[r] * aa[q];
+  s.lo[0] = fminf(A.x, fminf(B.x, C.x)); s.hi[0] = fmaxf(A.x, fmaxf(B.x, C.x));
+  s.lo[1] = fminf(A.y, fminf(B.y, C.y)); s.hi[1] = fmaxf(A.y, fmaxf(B.y, C.y));
+  s.lo[2] = fminf(A.z, fminf(B.z, C.z)); s.hi[2] = fmaxf(A.z, fmaxf(B.z, C.z));
+  lsum[i] = s;
+  // a single triangle's dipole centre is its centroid; order-2 term vanishes
+  float d0 = (s.lo[0] - cx) * (s.lo[0] - cx) + (s.lo[1] - cy) * (s.lo[1] - cy) + (s.lo[2] - cz) * (s.lo[2] - cz);
+  float d1 = (s.hi[0] - cx) * (s.hi[0] - cx) + (s.hi[1] - cy) * (s.hi[1] - cy) + (s.hi[2] - cz) * (s.hi[2] - cz);
+  leaf[5 * i + 0] = make_float4(cx, cy, cz, sqrtf(fmaxf(d0, d1)));
+  leaf[5 * i + 1] = make_float4(s.ax, s.ay, s.az, 0.f);
+  leaf[5 * i + 2] = A;
+  leaf[5 * i + 3] = B;
+  leaf[5 * i + 4] = C;
+}
+
+__device__ __forceinline__ int delta(const uint64_t* __restrict__ k, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  uint64_t a = k[i], b = k[j];
+  if (a == b) return 64 + __clz(uint32_t(i) ^ uint32_t(j));
+  return __clzll(a ^ b);
+}
+
+// Karras, "Maximizing Parallelism in the Construction of BVHs, Octrees, and
+// k-d Trees" (HPG 2012), with index tie-break for equal codes.
+__global__ void k_karras(const uint64_t* __restrict__ k, int n, int2* __restrict__ child, int* __restrict__ parent) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  int d = (delta(k, n, i, i + 1) - delta(k, n, i, i - 1)) >= 0 ? 1 : -1;
+  int dmin = delta(k, n, i, i - d);
+  int lmax = 2;
+  while (delta(k, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t >= 1; t >>= 1)
+    if (delta(k, n, i, i + (l + t) * d) > dmin) l += t;
+  int j = i + l * d;
+  int dnode = delta(k, n, i, j);
+  int s = 0;
+  int t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (delta(k, n, i, i + (s + t) * d) > dnode) s += t;
+  } while (t > 1);
+  int gamma = i + s * d + min(d, 0);
+  int lo = min(i, j), hi = max(i, j);
+  int left = (lo == gamma) ? ~gamma : gamma;
+  int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+  child[i] = make_int2(left, right);
+  // parent[] holds internal parents: [0, n-1) internal nodes, [n-1, 2n-1) leaves
+  parent[left >= 0 ? left : (n - 1) + ~left] = i;
+  parent[right >= 0 ? right : (n - 1) + ~right] = i;
+}
+
+__device__ __forceinline__ void sums_add(Sums& r, const Sums& a, const Sums& b) {
+  r.ax = a.ax + b.ax; r.ay = a.ay + b.ay; r.az = a.az + b.az;
+  r.cx = a.cx + b.cx; r.cy = a.cy + b.cy; r.cz = a.cz + b.cz;
+  r.s = a.s + b.s;
+  for (int q = 0; q < 9; ++q) r.m[q] = a.m[q] + b.m[q];
+  for (int q = 0; q < 3; ++q) { r.lo[q] = fminf(a.lo[q], b.lo[q]); r.hi[q] = fmaxf(a.hi[q], b.hi[q]); }
+}
+
+// Loads a subtree sum written by another SM: bypass L1 (not coherent).
+__device__ __forceinline__ Sums load_sums_cg(const Sums* p) {
+  Sums r;
+  const float* src = reinterpret_cast<const float*>(p);
+  float* dst = reinterpret_cast<float*>(&r);
+#pragma unroll
+  for (int q = 0; q < int(sizeof(Sums) / 4); ++q) dst[q] = __ldcg(src + q);
+  return r;
+}
+
+// Bottom-up: the second thread to reach a node combines both children.
+__global__ void k_refit(int n, const int2* __restrict__ child, const int* __restrict__ parent,
+                        const Sums* __restrict__ lsum, Sums* __restrict__ isum, int* __restrict__ flags,
+                        float4* __restrict__ inode) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int node = parent[(n - 1) + i];
+  for (int guard = 0; node >= 0 && guard < n; ++guard) {
+    __threadfence();
+    if (atomicAdd(&flags[node], 1) == 0) return;  // first arrival stops
+    __threadfence();
+    int2 c = child[node];
+    Sums a = c.x >= 0 ? load_sums_cg(isum + c.x) : lsum[~c.x];
+    Sums b = c.y >= 0 ? load_sums_cg(isum + c.y) : lsum[~c.y];
+    Sums r;
+    sums_add(r, a, b);
+    isum[node] = r;
+    float px = r.cx / r.s, py = r.cy / r.s, pz = r.cz / r.s;
+    float B[9];
+    float p[3] = {px, py, pz}, A[3] = {r.ax, r.ay, r.az};
+    for (int rr = 0; rr < 3; ++rr)
+      for (int q = 0; q < 3; ++q) B[3 * rr + q] = r.m[3 * rr + q] - p[rr] * A[q];
+    float d0 = (r.lo[0] - px) * (r.lo[0] - px) + (r.lo[1] - py) * (r.lo[1] - py) + (r.lo[2] - pz) * (r.lo[2] - pz);
+    float d1 = (r.hi[0] - px) * (r.hi[0] - px) + (r.hi[1] - py) * (r.hi[1] - py) + (r.hi[2] - pz) * (r.hi[2] - pz);
+    inode[5 * node + 0] = make_float4(px, py, pz, sqrtf(fmaxf(d0, d1)));
+    inode[5 * node + 1] = make_float4(r.ax, r.ay, r.az, B[0] + B[4] + B[8]);
+    inode[5 * node + 2] = make_float4(B[0], B[1], B[2], B[3]);
+    inode[5 * node + 3] = make_float4(B[4], B[5], B[6], B[7]);
+    inode[5 * node + 4] = make_float4(B[8], __int_as_float(c.x), __int_as_float(c.y), 0.f);
+    node = parent[node];
+  }
+}
+
+constexpr float FOUR_PI = 12.566370614359172f;
+constexpr int WN_STACK = 96;
+
+// Van Oosterom–Strackee solid angle (aabb_tree.rs:582-615), divided by 4 pi.
+__device__ __forceinline__ float tri_wn(float4 A, float4 B, float4 C, F3 q) {
+  float ax = A.x - q.x, ay = A.y - q.y, az = A.z - q.z;
+  float bx = B.x - q.x, by = B.y - q.y, bz = B.z - q.z;
+  float cx = C.x - q.x, cy = C.y - q.y, cz = C.z - q.z;
+  float la = sqrtf(ax * ax + ay * ay + az * az), lb = sqrtf(bx * bx + by * by + bz * bz),
+        lc = sqrtf(cx * cx + cy * cy + cz * cz);
+  if (la == 0.f || lb == 0.f || lc == 0.f) return 0.f;
+  ax /= la; ay /= la; az /= la;
+  bx /= lb; by /= lb; bz /= lb;
+  cx /= lc; cy /= lc; cz /= lc;
+  float ux = bx - ax, uy = by - ay, uz = bz - az, vx = cx - ax, vy = cy - ay, vz = cz - az;
+  float num = ax * (uy * vz - uz * vy) + ay * (uz * vx - ux * vz) + az * (ux * vy - uy * vx);
+  if (num == 0.f) return 0.f;
+  float den = 1.f + (ax * bx + ay * by + az * bz) + (ax * cx + ay * cy + az * cz) + (bx * cx + by * cy + bz * cz);
+  return atan2f(num, den) * (2.0f / FOUR_PI);
+}
+
+// Warp-coherent traversal: the 32 lanes of a warp hold 32 consecutive active
+// voxels (mostly of one brick, so within a few voxels of each other) and walk
+// the LBVH together.  A node is summed through its far field only when it is
+// far (|q - p| > beta * r, aabb_tree.rs:666) for every lane; otherwise the
+// warp opens it, and at a leaf every lane takes the exact solid angle.  Node
+// loads are warp-uniform, control flow never diverges, and each lane's sum is
+// at least as accurate as its own traversal would be.
+constexpr int WN_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * WN_WARPS) k_wn_sign(const uint32_t* __restrict__ act, uint64_t na,
+                                                           const int4* __restrict__ origins,
+                                                           float* __restrict__ values,
+                                                           const float4* __restrict__ inode,
+                                                           const float4* __restrict__ leaf, int n, float h,
+                                                           float beta, float thresh, M2VStats* st) {
+  __shared__ int stk[WN_WARPS][WN_STACK];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint64_t i = (blockIdx.x * uint64_t(WN_WARPS) + w) * 32 + lane;
+  if ((blockIdx.x * uint64_t(WN_WARPS) + w) * 32 >= na) return;  // whole warp out of range
+  const bool valid = i < na;
+  uint32_t v = valid ? act[i] : act[na - 1];
+  const uint32_t b = v >> 9, o = v & 511;
+  const int4 org = origins[b];
+  const F3 q = f3(fmul(__int2float_rn(org.x + int(o >> 6)), h), fmul(__int2float_rn(org.y + int((o >> 3) & 7)), h),
+                  fmul(__int2float_rn(org.z + int(o & 7)), h));
+  const float beta2 = beta * beta;
+  float sum = 0.f, comp = 0.f;  // Kahan-compensated accumulation
+  int sp = 0;
+  int node = n > 1 ? 0 : ~0;
+  bool overflow = false;
+  for (long long guard = 0; guard < 2ll * n + 2; ++guard) {
+    float wv = 0.f;
+    bool have = true;
+    if (node >= 0) {
+      const float4 P = inode[5 * node];
+      const float rx = P.x - q.x, ry = P.y - q.y, rz = P.z - q.z;
+      const float r2 = rx * rx + ry * ry + rz * rz;
+      const float lim = P.w * P.w * beta2;
+      if (__all_sync(0xffffffffu, r2 > lim)) {
+        const float4 A = inode[5 * node + 1], B0 = inode[5 * node + 2], B1 = inode[5 * node + 3],
+                     B2 = inode[5 * node + 4];
+        const float r1 = sqrtf(r2);
+        const float inv = 1.0f / (FOUR_PI * r2 * r1);
+        const float ar = A.x * rx + A.y * ry + A.z * rz;
+        const float brx = B0.x * rx + B0.y * ry + B0.z * rz;
+        const float bry = B0.w * rx + B1.x * ry + B1.y * rz;
+        const float brz = B1.z * rx + B1.w * ry + B2.x * rz;
+        const float rbr = rx * brx + ry * bry + rz * brz;
+        wv = inv * (ar + A.w) - (3.0f * inv / r2) * rbr;
+      } else {
+        const float4 E = inode[5 * node + 4];
+        if (sp < WN_STACK) {
+          if (lane == 0) stk[w][sp] = __float_as_int(E.z);
+          ++sp;
+        } else {
+          overflow = true;
+        }
+        node = __float_as_int(E.y);
+        have = false;
+      }
+    } else {
+      const int li = ~node;
+      const float4 P = leaf[5 * li];
+      const float rx = P.x - q.x, ry = P.y - q.y, rz = P.z - q.z;
+      const float r2 = rx * rx + ry * ry + rz * rz;
+      if (__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) {
+        const float4 A = leaf[5 * li + 1];
+        wv = (A.x * rx + A.y * ry + A.z * rz) / (FOUR_PI * r2 * sqrtf(r2));
+      } else {
+        wv = tri_wn(leaf[5 * li + 2], leaf[5 * li + 3], leaf[5 * li + 4], q);
+      }
+    }
+    __syncwarp();
+    if (have) {
+      const float y = wv - comp;
+      const float t = sum + y;
+      comp = (t - sum) - y;
+      sum = t;
+      if (sp == 0) break;
+      --sp;
+      node = stk[w][sp];
+    }
+    __syncwarp();
+  }
+  if (overflow && lane == 0) atomicExch(&st->error, 3);
+  if (valid) {
+    const float d = values[uint64_t(b) * 512 + o];
+    values[uint64_t(b) * 512 + o] = (sum < thresh) ? copysignf(d, 1.0f) : copysignf(d, -1.0f);
+  }
+}
+
+// ------------------------------------------------------------ driver ------
+static inline unsigned blocks(uint64_t n, unsigned t) { return unsigned((n + t - 1) / t); }
+
+bs_volume* mesh_to_volume_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
+                               const bs_m2v_params& p) {
+  if (nt == 0) fail(BS_ERR_EMPTY, "mesh has no triangles");
+  if (nt >= (1ull << 31)) fail(BS_ERR_CAPACITY, "more than 2^31 triangles");
+  if (!(p.voxel_size > 0.f) || !std::isfinite(p.voxel_size)) fail(BS_ERR_INVALID_ARG, "voxel_size must be > 0");
+  if (p.band_width < 0 || p.band_width > 1000000) fail(BS_ERR_INVALID_ARG, "band_width out of range");
+  cudaStream_t s = ctx->stream;
+  const float h = p.voxel_size;
+  const float inv_h = 1.0f / h;  // mesh_to_volume.rs:48 (reciprocal, then multiply)
+  const int band = p.band_width;
+
+  DBuf<M2VStats> st(ctx, 1);
+  M2VStats init{};
+  for (int k = 0; k < 3; ++k) {
+    init.vmin[k] = 0x7fffffff;
+    init.vmax[k] = -0x7fffffff;
+    init.cmin[k] = 0xffffffffu;
+    init.cmax[k] = 0u;
+  }
+  BS_CUDA(cudaMemcpyAsync(st.p, &init, sizeof init, cudaMemcpyHostToDevice, s));
+
+  DBuf<float4> T(ctx, 3 * nt);
+  DBuf<uint32_t> nsub(ctx, nt + 1), soff(ctx, nt + 1);
+  BS_KERNEL(ctx, "k_gather", (k_gather<<<blocks(nt + 1, 256), 256, 0, s>>>(d_xyz, nv, d_tri, nt, h, inv_h, band, T.p, nsub.p, st.p)));
+  exclusive_scan(ctx, nsub.p, soff.p, nt + 1);
+
+  struct {
+    M2VStats st;
+    uint32_t total;
+  } hb;
+  read_back(ctx, &hb.st, st.p, sizeof(M2VStats));
+  read_back(ctx, &hb.total, soff.p + nt, sizeof(uint32_t));
+  if (hb.st.error == 1) fail(BS_ERR_INVALID_ARG, "triangle vertex index out of range");
+  if (hb.st.error == 4) fail(BS_ERR_CAPACITY, "coordinates / voxel size exceed the int32 voxel grid");
+  // count of sub-triangles in 64 bit: nsub sums can wrap in uint32
+  if (hb.st.n_sub >= (1ull << 32)) fail(BS_ERR_CAPACITY, "more than 2^32 sub-triangles");
+  const uint64_t ns = hb.total;
+  if (ns == 0) fail(BS_ERR_EMPTY, "no sub-triangles");
+
+  Dir d;
+  d.bx0 = hb.st.vmin[0] >> 3; d.by0 = hb.st.vmin[1] >> 3; d.bz0 = hb.st.vmin[2] >> 3;
+  d.dx = (hb.st.vmax[0] >> 3) - d.bx0 + 1;
+  d.dy = (hb.st.vmax[1] >> 3) - d.by0 + 1;
+  d.dz = (hb.st.vmax[2] >> 3) - d.bz0 + 1;
+  const uint64_t D = uint64_t(d.dx) * d.dy * d.dz;
+  if (D >= (1ull << 32) - 2) fail(BS_ERR_CAPACITY, "brick directory exceeds 2^32 entries");
+
+  DBuf<SubTri> S(ctx, ns);
+  BS_KERNEL(ctx, "k_subdivide", (k_subdivide<<<blocks(nt, 128), 128, 0, s>>>(T.p, nsub.p, soff.p, nt, h, inv_h, band, S.p)));
+  nsub.reset();
+  soff.reset();
+
+  DBuf<uint32_t> cnt(ctx, D + 1), pair_off(ctx, D + 1), flag(ctx, D + 1), bidx(ctx, D + 1);
+  BS_CUDA(cudaMemsetAsync(cnt.p, 0, (D + 1) * sizeof(uint32_t), s));
+  BS_KERNEL(ctx, "k_count_pairs", (k_count_pairs<<<blocks(ns, 256), 256, 0, s>>>(S.p, ns, d, cnt.p, st.p)));
+  exclusive_scan(ctx, cnt.p, pair_off.p, D + 1);
+  BS_KERNEL(ctx, "k_dir_flags", (k_dir_flags<<<blocks(D + 1, 256), 256, 0, s>>>(cnt.p, D, flag.p)));
+  exclusive_scan(ctx, flag.p, bidx.p, D + 1);
+  uint32_t nb_np[2];
+  read_back(ctx, &nb_np[0], bidx.p + D, sizeof(uint32_t));
+  read_back(ctx, &nb_np[1], pair_off.p + D, sizeof(uint32_t));
+  read_back(ctx, &hb.st, st.p, sizeof(M2VStats));
+  if (hb.st.error == 2) fail(BS_ERR_CAPACITY, "sub-triangle outside the brick directory");
+  if (hb.st.n_pairs >= (1ull << 32)) fail(BS_ERR_CAPACITY, "more than 2^32 brick/sub-triangle pairs");
+  const uint64_t nb = nb_np[0], np = nb_np[1];
+  flag.reset();
+
+  bs_volume* vol = new bs_volume(ctx);
+  vol->h = h;
+  try {
+    vol->n_leaves = nb;
+    vol->d_origins = dalloc<int4>(ctx, nb);
+    vol->d_values = dalloc<float>(ctx, nb * 512);
+    vol->d_masks = dalloc<uint32_t>(ctx, nb * 16);
+    DBuf<uint32_t> list_off(ctx, nb + 1), list(ctx, np);
+    BS_KERNEL(ctx, "k_dir_compact", (k_dir_compact<<<blocks(D, 256), 256, 0, s>>>(cnt.p, pair_off.p, bidx.p, D, d, vol->d_origins, list_off.p)));
+    BS_CUDA(cudaMemcpyAsync(list_off.p + nb, pair_off.p + D, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+    pair_off.reset();
+    bidx.reset();
+    BS_KERNEL(ctx, "k_fill_pairs", (k_fill_pairs<<<blocks(ns, 256), 256, 0, s>>>(S.p, ns, d, cnt.p, list.p)));
+    cnt.reset();
+    BS_KERNEL(ctx, "k_brick_distance", (k_brick_distance<<<unsigned(nb), DIST_THREADS, 0, s>>>(vol->d_origins, list_off.p, list.p, S.p, h,
+                                                          vol->d_values, vol->d_masks)));
+    list.reset();
+    list_off.reset();
+    S.reset();
+
+    // active voxels
+    DBuf<uint32_t> vc(ctx, nb + 1), voff(ctx, nb + 1);
+    BS_KERNEL(ctx, "k_brick_popcount", (k_brick_popcount<<<blocks(nb + 1, 256), 256, 0, s>>>(vol->d_masks, nb, vc.p)));
+    exclusive_scan(ctx, vc.p, voff.p, nb + 1);
+    uint32_t na32 = 0;
+    read_back(ctx, &na32, voff.p + nb, sizeof(uint32_t));
+    const uint64_t na = na32;
+    vol->n_active = na;
+    DBuf<uint32_t> act(ctx, na);
+    BS_KERNEL(ctx, "k_emit_active", (k_emit_active<<<blocks(nb * 32, 256), 256, 0, s>>>(vol->d_masks, voff.p, nb, act.p)));
+    vc.reset();
+    voff.reset();
+
+    // LBVH over the original triangles
+    const int n = int(nt);
+    DBuf<uint64_t> keys(ctx, nt), keys2(ctx, nt);
+    DBuf<uint32_t> vals(ctx, nt), order(ctx, nt);
+    BS_KERNEL(ctx, "k_morton", (k_morton<<<blocks(nt, 256), 256, 0, s>>>(T.p, nt, st.p, keys.p, vals.p)));
+    {
+      size_t tmp = 0;
+      BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, keys.p, keys2.p, vals.p, order.p, int(nt), 0, 64, s));
+      DBuf<uint8_t> t(ctx, tmp);
+      BS_CUDA(cub::DeviceRadixSort::SortPairs(t.p, tmp, keys.p, keys2.p, vals.p, order.p, int(nt), 0, 64, s));
+    }
+    keys.reset();
+    vals.reset();
+    DBuf<float4> leaf(ctx, 5 * nt), inode(ctx, 5 * std::max<uint64_t>(nt - 1, 1));
+    DBuf<Sums> lsum(ctx, nt), isum(ctx, std::max<uint64_t>(nt - 1, 1));
+    BS_KERNEL(ctx, "k_leaves", (k_leaves<<<blocks(nt, 256), 256, 0, s>>>(T.p, order.p, nt, leaf.p, lsum.p)));
+    if (n > 1) {
+      DBuf<int2> child(ctx, nt - 1);
+      DBuf<int> parent(ctx, 2 * nt - 1), flags(ctx, nt - 1);
+      BS_CUDA(cudaMemsetAsync(flags.p, 0, (nt - 1) * sizeof(int), s));
+      BS_CUDA(cudaMemsetAsync(parent.p, 0xff, sizeof(int), s));  // root has no parent
+      BS_KERNEL(ctx, "k_karras", (k_karras<<<blocks(nt - 1, 256), 256, 0, s>>>(keys2.p, n, child.p, parent.p)));
+      BS_KERNEL(ctx, "k_refit", (k_refit<<<blocks(nt, 256), 256, 0, s>>>(n, child.p, parent.p, lsum.p, isum.p, flags.p, inode.p)));
+    }
+    keys2.reset();
+    order.reset();
+    lsum.reset();
+    isum.reset();
+    if (na > 0) {
+      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<<<blocks(na, 32 * WN_WARPS), 32 * WN_WARPS, 0, s>>>(act.p, na, vol->d_origins, vol->d_values, inode.p, leaf.p, n, h,
+                                                p.wn_beta, p.wn_threshold, st.p)));
+    }
+    read_back(ctx, &hb.st, st.p, sizeof(M2VStats));
+    if (hb.st.error == 3) fail(BS_ERR_CAPACITY, "winding-number traversal stack overflow");
+    ctx->last_stats[0] = nt;
+    ctx->last_stats[1] = ns;
+    ctx->last_stats[2] = hb.st.n_pairs;
+    ctx->last_stats[3] = hb.st.n_vpairs;
+    ctx->last_stats[4] = nb;
+    ctx->last_stats[5] = na;
+  } catch (...) {
+    volume_release(vol);
+    throw;
+  }
+  return vol;
+}
+
+}  // namespace bs

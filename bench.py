@@ -1,0 +1,338 @@
+"""Benchmark: band voxels/s of mesh -> narrow-band SDF + winding-number sign.
+
+Workload (one step): both displaced tori of the boolean/offset workload —
+R 1, r 0.3, 1024 x 512 parametric grid (1,048,576 triangles each), gradient
+noise 0.02, the second rotated 90 degrees about x and shifted 0.5 in x —
+converted to signed narrow-band volumes at voxel 0.002, band 3 voxels.
+Synthetic, seeded (baby_shark_gb300.synthetic).
+
+  value : band voxels / s with the meshes resident in HBM (bs_mesh_to_volume_device),
+          L2 flushed (256 MiB write) between steps, per-step CUDA events on the
+          library's stream.
+  e2e   : the same through bs_mesh_to_volume with HOST buffers: vertex/index
+          upload and the export of the resulting volumes (origins, values,
+          masks) to host memory inside every timed step.
+  roofline: the dominant kernel, timed live with CUDA events (stage timing),
+          against the FP32 peak measured by bs_diag_fp32_peak when the kernel
+          is FP32-bound, or the measured HBM copy bandwidth when it is
+          memory-bound.
+  cpu_baseline: the oracle (CPU restatement of the reference path, OpenMP,
+          all host cores) on a bounded sample of the same workload.
+
+`--impl reference` times the reference path's CPU implementation (the
+oracle port; the Rust crate cannot be built here) on the same metric.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+H = 0.002
+BAND = 3
+METRIC = "band voxels/s mesh→SDF+sign: learned/batched vs plain GPU, 0 sign flips"
+UNIT = "band_voxels/s"
+WORKLOAD = "two displaced tori, 1,048,576 triangles each, voxel 0.002, band 3: mesh->SDF+sign (plain GPU path)"
+
+
+def rank_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def meshes():
+    from baby_shark_gb300 import synthetic
+    return synthetic.config2()
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_baseline(seconds_target=15.0):
+    """Oracle on a bounded sample: the first 1/16 of torus A's ring (65,536 triangles)."""
+    from oracle import binding as ob
+    (v, f), _ = meshes()
+    nu, nv = 1024, 512
+    take = nu // 16
+    fs = f[np.isin(f[:, 0] // nv, np.arange(take)) & (f.max(axis=1) < (take + 1) * nv)]
+    threads = os.cpu_count() or 1
+    ob.set_threads(threads)
+    t0 = time.perf_counter()
+    vol, stats, _ = ob.mesh_to_volume(v, fs, H, BAND)
+    dt = time.perf_counter() - t0
+    del vol
+    return {"value": stats["band_voxels"] / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "oracle mesh->SDF+sign on %d triangles (1/16 of torus A's ring), %d band voxels, %.2f s"
+                      % (len(fs), stats["band_voxels"], dt)}
+
+
+def run_reference(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    from oracle import binding as ob
+    (v, f), _ = meshes()
+    nu, nv = 1024, 512
+    take = nu // 32
+    fs = f[np.isin(f[:, 0] // nv, np.arange(take)) & (f.max(axis=1) < (take + 1) * nv)]
+    threads = os.cpu_count() or 1
+    ob.set_threads(threads)
+    for _ in range(args.warmup):
+        ob.mesh_to_volume(v, fs, H, BAND)
+    times, band = [], 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        vol, stats, _ = ob.mesh_to_volume(v, fs, H, BAND)
+        times.append(time.perf_counter() - t0)
+        band = stats["band_voxels"]
+        del vol
+    tot = sum(times)
+    value = band * args.steps / tot
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD + "; reference CPU path on a bounded sample"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "oracle (CPU restatement of the reference path; the Rust crate cannot be "
+                                       "built on this machine) on %d triangles (1/32 of torus A's ring), "
+                                       "%d band voxels per step" % (len(fs), band)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import ctypes as C
+
+    import torch
+
+    import baby_shark_gb300 as bs
+    from baby_shark_gb300 import _native as N
+    from baby_shark_gb300 import build as bs_build
+
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    bs_build.build()
+    L = N.load()
+    ctx = bs.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    (va, fa), (vb, fb) = meshes()
+    dev = [(torch.from_numpy(v).cuda(), torch.from_numpy(f.astype(np.int32)).cuda()) for v, f in ((va, fa), (vb, fb))]
+    torch.cuda.synchronize()
+    params = N.M2VParams()
+    L.bs_m2v_params_default(C.byref(params))
+    params.voxel_size = H
+    params.band_width = BAND
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step_device():
+        outs = []
+        band = 0
+        for x, t in dev:
+            out = C.c_void_p()
+            N.check(L.bs_mesh_to_volume_device(ctx.h, x.data_ptr(), x.shape[0], t.data_ptr(), t.shape[0],
+                                               C.byref(params), C.byref(out)), ctx.h)
+            vol = bs.Volume(out, ctx)
+            band += vol.counts()["active_voxels"]
+            outs.append(vol)
+        return band, outs
+
+    def step_e2e():
+        band, h2d, d2h = 0, 0, 0
+        for v, f in ((va, fa), (vb, fb)):
+            vol = bs.MeshToVolume(ctx).with_voxel_size(H).with_narrow_band_width(BAND).convert((v, f))
+            o, val, m = vol.export()
+            band += vol.counts()["active_voxels"]
+            h2d += v.nbytes + f.nbytes
+            d2h += o.nbytes + val.nbytes + m.nbytes
+            del vol
+        return band, h2d, d2h
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step_device()
+    ctx.synchronize()
+    # ---- timed region (device-resident inputs) ----
+    ctx.set_stage_timing(True)
+    ctx.stage_times(reset=True)
+    launches0 = ctx.kernel_launches
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    per_step, band = [], 0
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            band, outs = step_device()
+            e1.record(stream)
+            del outs
+            flush.fill_(1.0)  # L2 flush between steps (outside the event pair)
+            e1.synchronize()
+            per_step.append(e0.elapsed_time(e1))
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    launches = ctx.kernel_launches - launches0
+    stages = ctx.stage_times(reset=True)
+    ctx.set_stage_timing(False)
+    stats = ctx.last_stats()
+    ms = sum(per_step) / len(per_step)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * band / (ms / 1000.0)
+
+    # ---- e2e: host buffers through the C ABI, upload + export inside each step ----
+    for _ in range(max(1, args.warmup // 2)):
+        step_e2e()
+    t_e2e = []
+    for _ in range(args.steps):
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        b_e2e, h2d, d2h = step_e2e()
+        ctx.synchronize()
+        t_e2e.append(time.perf_counter() - t0)
+    e2e_value = world * b_e2e / (sum(t_e2e) / len(t_e2e))
+
+    # ---- roofline of the dominant kernel ----
+    top = max(stages.items(), key=lambda kv: kv[1][0])
+    name, (tot_ms, nl) = top
+    peaks, src = measured_peaks()
+    fp32_peak = fp32_peak_tflops(ctx)
+    # per launch: stats are of the last conversion (torus B); both tori are the same size class
+    if name == "k_brick_distance":
+        flops = 84.0 * stats["voxel_pairs"]
+        achieved = flops / (tot_ms / nl / 1000.0) / 1e12
+        roof = {"kernel": name, "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                "peak_source": "measured by bs_diag_fp32_peak (FFMA loop) on this GPU",
+                "algorithmic": "84 FLOP x (voxel, sub-triangle) pairs = %d per launch" % stats["voxel_pairs"]}
+    else:
+        roof = {"kernel": name, "bound": "hbm", "achieved": None, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                "frac": None, "traffic": None, "peak_source": src}
+    roof["share_of_step"] = tot_ms / sum(v[0] for v in stages.values())
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "triangles_per_step": int(len(fa) + len(fb)),
+                       "band_voxels_per_step": int(band), "l2": "flushed between steps (256 MiB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "roofline": roof,
+            "clocks": clk,
+            "stages_ms_per_step": {k: v[0] / args.steps for k, v in sorted(stages.items(), key=lambda kv: -kv[1][0])},
+            "last_stats": stats}
+    if rank == 0:
+        if world == 1:
+            line["cpu_baseline"] = cpu_baseline()
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def fp32_peak_tflops(ctx):
+    import ctypes as C
+    from baby_shark_gb300 import _native as N
+    L = N.load()
+    if not hasattr(L, "bs_diag_fp32_peak"):
+        return None
+    out = C.c_double()
+    N.check(L.bs_diag_fp32_peak(ctx.h, C.byref(out)), ctx.h)
+    return out.value
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,147 @@
+/*
+ * baby_shark_gb300 — C ABI of the GB300 (sm_103a) implementation of
+ * baby_shark's implicit-modelling path: mesh -> narrow-band signed distance
+ * volume (exact point–triangle distances, fast-winding-number signs),
+ * volume booleans and offset, and dual-contouring extraction.
+ *
+ * The reference (crate baby_shark v0.3.12) is a Rust library with no FFI;
+ * each entry point below replaces one public Rust method, cited as
+ * file:line inside the reference crate.  A Rust wrapper binds these symbols
+ * with `extern "C"` and keeps the crate's builder API on top.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Arrays named h_* are host memory,
+ *    d_* device memory of the context's device.
+ *  - Every call returns a bs_status; results come back through out-params.
+ *  - All work of a context is ordered on its CUDA stream.  Entry points that
+ *    return sizes or host data synchronise that stream before returning.
+ *  - One context per host thread; contexts are independent.
+ *  - A volume belongs to the context that made it.  Boolean operations
+ *    consume both operands, like the reference's `Volume::union(self, other)`.
+ *  - Voxel storage: leaves (bricks) of 8^3 voxels whose origins are
+ *    multiples of 8 in integer grid coordinates (grid point i sits at i*h).
+ *    Inside a leaf, voxel (x,y,z) has index x<<6 | y<<3 | z; its active bit is
+ *    bit (index & 31) of mask word (index >> 5).
+ */
+#ifndef BABY_SHARK_GB300_H
+#define BABY_SHARK_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bs_status {
+  BS_OK = 0,
+  BS_ERR_INVALID_ARG = 1,  /* null pointer, bad size, unknown option */
+  BS_ERR_EMPTY = 2,        /* empty mesh: the reference's convert() returns None */
+  BS_ERR_OOM = 3,          /* device allocation failed */
+  BS_ERR_CAPACITY = 4,     /* a grid or table bound was exceeded */
+  BS_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+  BS_ERR_CUDA = 6,         /* CUDA runtime error (see bs_ctx_last_error) */
+  BS_ERR_UNSUPPORTED = 7,  /* input the reference panics on (e.g. tiles in DC) */
+  BS_ERR_NO_DEVICE = 8     /* no CUDA device / driver */
+} bs_status;
+
+typedef struct bs_ctx bs_ctx;
+typedef struct bs_volume bs_volume;
+
+/* ---------------------------------------------------------------- context */
+/* Creates a context on `device`.  `stream` is a cudaStream_t to run on, or
+ * NULL for a stream the context creates and owns. */
+bs_status bs_ctx_create(int device, void* stream, bs_ctx** out);
+bs_status bs_ctx_destroy(bs_ctx* ctx);
+/* The cudaStream_t all work of the context is ordered on. */
+void* bs_ctx_stream(bs_ctx* ctx);
+bs_status bs_ctx_synchronize(bs_ctx* ctx);
+/* Number of kernels this library launched on the context so far. */
+uint64_t bs_ctx_kernel_launches(const bs_ctx* ctx);
+/* Text of the last error on the context ("" if none). */
+const char* bs_ctx_last_error(const bs_ctx* ctx);
+const char* bs_status_string(bs_status s);
+
+/* ------------------------------------------------------- diagnostics ---- */
+/* These have no counterpart in the reference; they expose measurements of
+ * this implementation.  Stage timing brackets every kernel launch of the
+ * context with CUDA events on its stream (off by default). */
+bs_status bs_ctx_set_stage_timing(bs_ctx* ctx, int enable);
+/* Resolves the recorded events (synchronising them) and returns the number
+ * of distinct kernel names timed so far. */
+bs_status bs_ctx_stage_count(bs_ctx* ctx, int* n_stages);
+/* Name (valid until the next reset), total milliseconds and launch count of stage i. */
+bs_status bs_ctx_stage_info(bs_ctx* ctx, int i, const char** name, double* total_ms, uint64_t* launches);
+bs_status bs_ctx_stage_reset(bs_ctx* ctx);
+/* Counters of the last mesh -> volume call: [0] triangles, [1] sub-triangles,
+ * [2] (brick, sub-triangle) pairs, [3] (voxel, sub-triangle) pairs,
+ * [4] leaves, [5] active voxels, [6..7] reserved. */
+bs_status bs_ctx_last_stats(const bs_ctx* ctx, uint64_t* out8);
+/* Measured FP32 FMA throughput of the context's device in TFLOP/s (a timed
+ * FFMA loop over all SMs); the denominator of FP32-bound roofline fractions. */
+bs_status bs_diag_fp32_peak(bs_ctx* ctx, double* tflops);
+
+/* ----------------------------------------------------- mesh -> volume ---- */
+typedef struct bs_m2v_params {
+  float voxel_size;    /* MeshToVolume::with_voxel_size   (mesh_to_volume.rs:40-50) */
+  int32_t band_width;  /* MeshToVolume::with_narrow_band_width (mesh_to_volume.rs:28-37) */
+  float wn_beta;       /* far-field accuracy scale; the reference uses 2.0 (mesh_to_volume.rs:264) */
+  float wn_threshold;  /* wn < threshold => outside; the reference uses 0.2 (mesh_to_volume.rs:266) */
+} bs_m2v_params;
+
+/* Fills `p` with the reference's defaults (voxel 1, band 0, beta 2, threshold 0.2). */
+void bs_m2v_params_default(bs_m2v_params* p);
+
+/* MeshToVolume::convert (mesh_to_volume.rs:52-73) on an indexed triangle mesh
+ * in HOST memory: h_xyz[3*nv] vertex positions, h_tri[3*nt] vertex indices.
+ * Returns BS_ERR_EMPTY where the reference returns None (no triangles). */
+bs_status bs_mesh_to_volume(bs_ctx* ctx, const float* h_xyz, uint64_t nv, const uint32_t* h_tri,
+                            uint64_t nt, const bs_m2v_params* params, bs_volume** out);
+
+/* Same as bs_mesh_to_volume with the mesh already in device memory. */
+bs_status bs_mesh_to_volume_device(bs_ctx* ctx, const float* d_xyz, uint64_t nv,
+                                   const uint32_t* d_tri, uint64_t nt,
+                                   const bs_m2v_params* params, bs_volume** out);
+
+/* ------------------------------------------------------------- volumes --- */
+bs_status bs_volume_free(bs_volume* v);
+/* Volume::voxel_size (volume/mod.rs:31-34). */
+bs_status bs_volume_voxel_size(const bs_volume* v, float* out);
+/* Volume's Clone impl (volume/mod.rs:114-121). */
+bs_status bs_volume_clone(bs_ctx* ctx, const bs_volume* v, bs_volume** out);
+/* Number of leaves and of active tiles (tiles appear only after booleans). */
+bs_status bs_volume_counts(const bs_volume* v, uint64_t* n_leaves, uint64_t* n_tiles,
+                           uint64_t* n_active_voxels);
+/* Copies the volume to HOST memory: h_origins[3*n_leaves] (int32 leaf origins,
+ * sorted by (x, y, z)), h_values[512*n_leaves], h_masks[16*n_leaves].  Any of
+ * the three may be NULL.  Values of inactive voxels are those the reference
+ * holds there (0 after convert, signed far values after a flood fill). */
+bs_status bs_volume_export(bs_ctx* ctx, const bs_volume* v, int32_t* h_origins, float* h_values,
+                           uint32_t* h_masks);
+/* Active tiles: h_origins[3*n], h_sizes[n] (edge length in voxels), h_values[n]. */
+bs_status bs_volume_export_tiles(bs_ctx* ctx, const bs_volume* v, int32_t* h_origins,
+                                 int32_t* h_sizes, float* h_values);
+
+/* Volume::union / subtract / intersect (volume/mod.rs:74-93): both operands are
+ * flood filled, combined, and consumed; *out receives the result. */
+bs_status bs_volume_union(bs_ctx* ctx, bs_volume* a, bs_volume* b, bs_volume** out);
+bs_status bs_volume_subtract(bs_ctx* ctx, bs_volume* a, bs_volume* b, bs_volume** out);
+bs_status bs_volume_intersect(bs_ctx* ctx, bs_volume* a, bs_volume* b, bs_volume** out);
+/* Volume::offset (volume/mod.rs:95-108), in place. */
+bs_status bs_volume_offset(bs_ctx* ctx, bs_volume* v, float distance);
+
+/* --------------------------------------------------- dual contouring ---- */
+/* DualContouringMesher::with_voxel_size(..).mesh(&volume) (dual_contouring.rs:16-91).
+ * Writes up to `capacity` triangles (9 floats each, world units) to h_tris and
+ * the total count to *n_tris; call with capacity 0 to size the buffer (the
+ * extraction is cached on the volume, so the second call only copies).
+ * Volumes holding active tiles give BS_ERR_UNSUPPORTED, where the reference
+ * stops with todo!() (dual_contouring.rs:139). */
+bs_status bs_dual_contour(bs_ctx* ctx, bs_volume* v, float voxel_size, float* h_tris,
+                          uint64_t capacity, uint64_t* n_tris);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BABY_SHARK_GB300_H */
