@@ -5,6 +5,7 @@ Names, argument meaning and failure behaviour follow baby_shark v0.3.12:
   MeshToVolume        voxel/mesh_to_volume.rs:17-73
   Volume              voxel/volume/mod.rs:11-123 (booleans consume both operands)
   DualContouringMesher voxel/meshing/dual_contouring.rs:12-91
+  CornerTable         mesh/corner_table/builder.rs:292-309 (soup builder)
   VoxelRemesher       remeshing/voxel.rs:44-95
 
 Where the reference returns `None` (empty mesh), these return None; every
@@ -232,3 +233,95 @@ class DualContouringMesher:
         N.check(L.bs_dual_contour(volume.ctx.h, volume.h, self.voxel_size, out.ctypes.data, n.value, C.byref(n)),
                 volume.ctx.h)
         return out[: n.value]
+
+
+class CornerTable:
+    """Corner-table mesh built from a triangle soup (bs_corner_table)."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            try:
+                N.load().bs_corner_table_free(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+    @staticmethod
+    def from_triangles_soup(tris, ctx=None):
+        """CornerTable::from_triangles_soup (builder.rs:97-101)."""
+        ctx = ctx or default_context()
+        t = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+        out = C.c_void_p()
+        N.check(N.load().bs_corner_table_from_soup(ctx.h, t.ctypes.data, len(t), C.byref(out)), ctx.h)
+        return CornerTable(out)
+
+    @staticmethod
+    def from_dual_contouring(volume, voxel_size):
+        out = C.c_void_p()
+        N.check(N.load().bs_corner_table_from_dual_contour(volume.ctx.h, volume.h, float(voxel_size), C.byref(out)),
+                volume.ctx.h)
+        return CornerTable(out)
+
+    def counts(self):
+        a, b, c, d = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
+        N.check(N.load().bs_corner_table_counts(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return {"faces": a.value, "vertices": b.value, "vertex_slots": c.value, "corners": d.value}
+
+    def faces_count(self):
+        return self.counts()["faces"]
+
+    def vertices_count(self):
+        return self.counts()["vertices"]
+
+    def export(self):
+        c = self.counts()
+        pos = np.zeros((c["vertex_slots"], 3), np.float32)
+        dele = np.zeros(c["vertex_slots"], np.uint8)
+        vc = np.zeros(c["vertex_slots"], np.int32)
+        cv = np.zeros(c["corners"], np.int32)
+        co = np.zeros(c["corners"], np.int32)
+        N.check(N.load().bs_corner_table_export(self.h, pos.ctypes.data, dele.ctypes.data, vc.ctypes.data,
+                                                cv.ctypes.data, co.ctypes.data))
+        return {"positions": pos, "deleted": dele.astype(bool), "vertex_corner": vc, "corner_vertex": cv,
+                "corner_opposite": co}
+
+
+class VoxelRemesher:
+    """VoxelRemesher (remeshing/voxel.rs:44-95): mesh -> SDF -> surface -> CornerTable.
+
+    The reference's default meshing method is marching cubes ("Manifold"),
+    which this build does not provide on the GPU; FeaturePreserving (dual
+    contouring) is supported.  The band width defaults to 0 like the
+    reference; with_narrow_band_width is an extension."""
+
+    FEATURE_PRESERVING = "FeaturePreserving"
+    MANIFOLD = "Manifold"
+
+    def __init__(self, ctx=None):
+        self.m2v = MeshToVolume(ctx)
+        self.voxel_size = 1.0
+        self.method = self.MANIFOLD
+
+    def with_voxel_size(self, size):
+        self.m2v.with_voxel_size(size)
+        self.voxel_size = float(size)
+        return self
+
+    def with_narrow_band_width(self, width):
+        self.m2v.with_narrow_band_width(width)
+        return self
+
+    def with_meshing_method(self, method):
+        self.method = method
+        return self
+
+    def remesh(self, mesh):
+        if self.method != self.FEATURE_PRESERVING:
+            raise NotImplementedError("marching cubes is not built on the GPU; use FeaturePreserving")
+        vol = self.m2v.convert(mesh)
+        if vol is None:
+            return None
+        return CornerTable.from_dual_contouring(vol, self.voxel_size)

@@ -137,6 +137,8 @@ void read_back(bs_ctx* ctx, void* host, const void* dev, size_t bytes);
 
 }  // namespace bs
 
+struct Upper;  // internal-node levels, volume_upper.cuh
+
 // ------------------------------------------------------------- volume -----
 // Leaves (8^3 bricks) sorted by origin (x, then y, then z).  Tiles are the
 // active constant regions of the reference's internal nodes (128^3 and
@@ -157,11 +159,12 @@ struct bs_volume {
   int4* d_tiles = nullptr;     // [n] (x, y, z, size)
   float* d_tile_values = nullptr;
   // upper tree levels (see volume_ops.cu): kept for boolean semantics
-  struct Upper* upper = nullptr;
+  Upper* upper = nullptr;
   // cached dual-contouring output (world-unit triangles)
   float* d_dc_tris = nullptr;
   uint64_t n_dc_tris = 0;
   bool dc_valid = false;
+  float dc_h = 0.0f;
   ~bs_volume();
 };
 

@@ -1,0 +1,435 @@
+// Dual contouring on the GPU (voxel/meshing/dual_contouring.rs:16-473).
+//
+// Three passes over the leaves, each counted, scanned and then written into
+// compact arrays indexed through per-leaf bit masks:
+//   1. edge crossings: for every active voxel and axis whose +1 neighbour is
+//      active with the other sign, the crossing point and the normal from
+//      interpolated central / one-sided differences (dual_contouring.rs:249-387);
+//   2. cell vertices: for every cell whose 8 corners are active and not all of
+//      one sign, the particle solver over its crossings (find_feature_point,
+//      dual_contouring.rs:429-458, 50 damped iterations);
+//   3. quads: for every sign-change edge whose 4 surrounding cells have
+//      vertices, two triangles, flipped when the first end is inside, scaled
+//      by the voxel size; exactly degenerate triangles are dropped
+//      (dual_contouring.rs:62-79, 93-174).
+// Every float operation follows the reference's order without fused
+// multiply-adds, so the vertices are bit-identical to the reference's.  The
+// face order is deterministic (leaves in volume order, voxels, axes); the
+// reference's own order depends on thread scheduling.
+#include <cub/device/device_scan.cuh>
+
+#include "bs_internal.cuh"
+#include "leaf_hash.cuh"
+#include "volume_upper.cuh"
+
+namespace bs {
+
+static inline unsigned nbk(uint64_t n, unsigned t) { return unsigned((n + t - 1) / t); }
+
+template <class T>
+static void scan_e(bs_ctx* ctx, const T* in, T* out, size_t n) {
+  size_t tmp = 0;
+  BS_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, in, out, n, ctx->stream));
+  DBuf<uint8_t> t(ctx, tmp);
+  BS_CUDA(cub::DeviceScan::ExclusiveSum(t.p, tmp, in, out, n, ctx->stream));
+}
+
+struct DcVol {
+  const int4* org;
+  const float* val;
+  const uint32_t* msk;
+  LeafHash hash;
+};
+
+// 27 neighbour leaves around a leaf, index (dx+1)*9 + (dy+1)*3 + (dz+1).
+__device__ __forceinline__ void load_neighbours(const DcVol& V, int4 org, int* nb) {
+  for (int k = threadIdx.x; k < 27; k += blockDim.x) {
+    const int dx = k / 9 - 1, dy = (k / 3) % 3 - 1, dz = k % 3 - 1;
+    nb[k] = V.hash.find(org.x + 8 * dx, org.y + 8 * dy, org.z + 8 * dz);
+  }
+}
+
+// Active value at voxel (x, y, z) given relative to the leaf origin, in [-8, 16).
+__device__ __forceinline__ bool at(const DcVol& V, const int* nb, int x, int y, int z, float& v) {
+  const int k = ((x >> 3) + 1) * 9 + ((y >> 3) + 1) * 3 + ((z >> 3) + 1);
+  const int l = nb[k];
+  if (l < 0) return false;
+  const int o = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
+  if (!((V.msk[uint64_t(l) * 16 + (o >> 5)] >> (o & 31)) & 1u)) return false;
+  v = V.val[uint64_t(l) * 512 + o];
+  return true;
+}
+
+// dual_contouring.rs:362-386
+__device__ __forceinline__ bool grad(const DcVol& V, const int* nb, int x, int y, int z, int axis, float& g) {
+  const int lx = axis == 0 ? 1 : 0, ly = axis == 1 ? 1 : 0, lz = axis == 2 ? 1 : 0;
+  float vp, vl, vr;
+  const bool hp = at(V, nb, x, y, z, vp);
+  const bool hl = at(V, nb, x - lx, y - ly, z - lz, vl);
+  const bool hr = at(V, nb, x + lx, y + ly, z + lz, vr);
+  if (hp && hl && hr) { g = fmul(fsub(vr, vl), 0.5f); return true; }
+  if (hp && hr) { g = fsub(vr, vp); return true; }
+  if (hp && hl) { g = fsub(vp, vl); return true; }
+  return false;  // the reference stops with unreachable!() here
+}
+
+struct DcStats {
+  int error;  // 1: gradient with no neighbours, 2: table capacity
+};
+
+// Pass 1a: crossing masks.  cm[l][dir][16]
+__global__ void __launch_bounds__(128) k_dc_edge_mask(DcVol V, uint64_t n, uint32_t* __restrict__ cm,
+                                                      uint32_t* __restrict__ ccount) {
+  __shared__ int nb[27];
+  const uint64_t l = blockIdx.x;
+  if (l >= n) return;
+  const int4 org = V.org[l];
+  load_neighbours(V, org, nb);
+  __syncthreads();
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  uint32_t cnt[3] = {0, 0, 0};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int o = t + 128 * k;
+    const int x = o >> 6, y = (o >> 3) & 7, z = o & 7;
+    float v1;
+    const bool h1 = at(V, nb, x, y, z, v1);
+#pragma unroll
+    for (int dir = 0; dir < 3; ++dir) {
+      float v2;
+      const bool cross = h1 && at(V, nb, x + (dir == 0), y + (dir == 1), z + (dir == 2), v2) &&
+                         (signbit(v1) != signbit(v2));
+      const uint32_t m = __ballot_sync(0xffffffffu, cross);
+      if (lane == 0) {
+        cm[(l * 3 + dir) * 16 + w + 4 * k] = m;
+        cnt[dir] += __popc(m);
+      }
+    }
+  }
+  __shared__ uint32_t sc[3];
+  if (t < 3) sc[t] = 0;
+  __syncthreads();
+  if (lane == 0)
+    for (int dir = 0; dir < 3; ++dir) atomicAdd(&sc[dir], cnt[dir]);
+  __syncthreads();
+  if (t < 3) ccount[l * 3 + t] = sc[t];
+  if (l == n - 1 && t == 3) ccount[n * 3] = 0;
+}
+
+__device__ __forceinline__ uint32_t rank512(const uint32_t* m, int o) {
+  uint32_t r = 0;
+  for (int w = 0; w < (o >> 5); ++w) r += __popc(m[w]);
+  return r + __popc(m[o >> 5] & ((1u << (o & 31)) - 1u));
+}
+
+// Pass 1b: crossing points and normals (dual_contouring.rs:249-313).
+__global__ void __launch_bounds__(128) k_dc_edge_points(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
+                                                        const uint32_t* __restrict__ coff, float* __restrict__ pts,
+                                                        DcStats* st) {
+  __shared__ int nb[27];
+  const uint64_t l = blockIdx.x;
+  if (l >= n) return;
+  const int4 org = V.org[l];
+  load_neighbours(V, org, nb);
+  __syncthreads();
+  for (int k = threadIdx.x; k < 3 * 512; k += blockDim.x) {
+    const int dir = k >> 9, o = k & 511;
+    const uint32_t* m = cm + (l * 3 + dir) * 16;
+    if (!((m[o >> 5] >> (o & 31)) & 1u)) continue;
+    const int x = o >> 6, y = (o >> 3) & 7, z = o & 7;
+    const int x2 = x + (dir == 0), y2 = y + (dir == 1), z2 = z + (dir == 2);
+    float v1, v2;
+    at(V, nb, x, y, z, v1);
+    at(V, nb, x2, y2, z2, v2);
+    const float t = (v1 == v2) ? 0.5f : fdiv(v1, fsub(v1, v2));
+    float p[3] = {__int2float_rn(org.x + x), __int2float_rn(org.y + y), __int2float_rn(org.z + z)};
+    p[dir] = fadd(p[dir], t);
+    float nrm[3];
+    bool ok = true;
+    for (int a = 0; a < 3; ++a) {
+      float g1, g2;
+      ok = ok && grad(V, nb, x, y, z, a, g1) && grad(V, nb, x2, y2, z2, a, g2);
+      if (ok) nrm[a] = fadd(fmul(fsub(1.0f, t), g1), fmul(t, g2));
+    }
+    if (!ok) {
+      atomicExch(&st->error, 1);
+      continue;
+    }
+    const float len = fsqrt(fadd(fadd(fmul(nrm[0], nrm[0]), fmul(nrm[1], nrm[1])), fmul(nrm[2], nrm[2])));
+    const uint64_t idx = coff[l * 3 + dir] + rank512(m, o);
+    float* q = pts + idx * 6;
+    q[0] = p[0];
+    q[1] = p[1];
+    q[2] = p[2];
+    q[3] = fdiv(nrm[0], len);
+    q[4] = fdiv(nrm[1], len);
+    q[5] = fdiv(nrm[2], len);
+  }
+}
+
+// voxel/utils.rs:88-97 and dual_contouring.rs:410-423
+__constant__ int8_t c_cube[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                    {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+__constant__ int8_t c_edges[12][4] = {{0, 0, 0, 0}, {0, 0, 0, 1}, {0, 0, 0, 2}, {1, 0, 0, 1},
+                                      {1, 0, 0, 2}, {0, 0, 1, 0}, {0, 0, 1, 1}, {0, 1, 0, 0},
+                                      {0, 1, 0, 2}, {1, 0, 1, 1}, {0, 1, 1, 0}, {1, 1, 0, 2}};
+__constant__ int8_t c_cells[3][4][3] = {{{0, 0, 0}, {0, 0, -1}, {0, -1, -1}, {0, -1, 0}},
+                                        {{0, 0, 0}, {-1, 0, 0}, {-1, 0, -1}, {0, 0, -1}},
+                                        {{0, -1, 0}, {-1, -1, 0}, {-1, 0, 0}, {0, 0, 0}}};
+
+// Pass 2a: cells with all 8 corners active and a sign change (dual_contouring.rs:193-217).
+__global__ void __launch_bounds__(128) k_dc_cell_mask(DcVol V, uint64_t n, uint32_t* __restrict__ cellm,
+                                                      uint32_t* __restrict__ ccount) {
+  __shared__ int nb[27];
+  __shared__ uint32_t sc;
+  const uint64_t l = blockIdx.x;
+  if (l >= n) return;
+  const int4 org = V.org[l];
+  load_neighbours(V, org, nb);
+  if (threadIdx.x == 0) sc = 0;
+  __syncthreads();
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int o = t + 128 * k;
+    const int x = o >> 6, y = (o >> 3) & 7, z = o & 7;
+    bool ok = true, any_neg = false, any_pos = false;
+    for (int c = 0; c < 8 && ok; ++c) {
+      float v;
+      ok = at(V, nb, x + c_cube[c][0], y + c_cube[c][1], z + c_cube[c][2], v);
+      if (ok) {
+        if (signbit(v)) any_neg = true;
+        else any_pos = true;
+      }
+    }
+    const uint32_t m = __ballot_sync(0xffffffffu, ok && any_neg && any_pos);
+    if (lane == 0) {
+      cellm[l * 16 + w + 4 * k] = m;
+      atomicAdd(&sc, __popc(m));
+    }
+  }
+  __syncthreads();
+  if (t == 0) ccount[l] = sc;
+  if (l == n - 1 && t == 1) ccount[n] = 0;
+}
+
+// Looks up the crossing stored for edge (x, y, z, dir) of the leaf's neighbourhood.
+__device__ __forceinline__ const float* edge_point(const int* nb, const uint32_t* cm, const uint32_t* coff,
+                                                   const float* pts, int x, int y, int z, int dir) {
+  const int k = ((x >> 3) + 1) * 9 + ((y >> 3) + 1) * 3 + ((z >> 3) + 1);
+  const int l = nb[k];
+  if (l < 0) return nullptr;
+  const int o = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
+  const uint32_t* m = cm + (uint64_t(l) * 3 + dir) * 16;
+  if (!((m[o >> 5] >> (o & 31)) & 1u)) return nullptr;
+  return pts + (coff[uint64_t(l) * 3 + dir] + rank512(m, o)) * 6;
+}
+
+// Pass 2b: the particle solver (dual_contouring.rs:429-458).
+__global__ void __launch_bounds__(128) k_dc_cell_points(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
+                                                        const uint32_t* __restrict__ coff, const float* __restrict__ pts,
+                                                        const uint32_t* __restrict__ cellm,
+                                                        const uint32_t* __restrict__ celloff, float* __restrict__ cells) {
+  __shared__ int nb[27];
+  const uint64_t l = blockIdx.x;
+  if (l >= n) return;
+  const int4 org = V.org[l];
+  load_neighbours(V, org, nb);
+  __syncthreads();
+  const uint32_t* m = cellm + l * 16;
+  for (int o = threadIdx.x; o < 512; o += blockDim.x) {
+    if (!((m[o >> 5] >> (o & 31)) & 1u)) continue;
+    const int x = o >> 6, y = (o >> 3) & 7, z = o & 7;
+    const float* ip[12];
+    int np = 0;
+    for (int e = 0; e < 12; ++e) {
+      const float* q = edge_point(nb, cm, coff, pts, x + c_edges[e][0], y + c_edges[e][1], z + c_edges[e][2],
+                                  c_edges[e][3]);
+      if (q) ip[np++] = q;
+    }
+    const float len = __int2float_rn(np);
+    float c0 = 0.f, c1 = 0.f, c2 = 0.f;
+    for (int i = 0; i < np; ++i) {
+      c0 = fadd(c0, ip[i][0]);
+      c1 = fadd(c1, ip[i][1]);
+      c2 = fadd(c2, ip[i][2]);
+    }
+    c0 = fdiv(c0, len);
+    c1 = fdiv(c1, len);
+    c2 = fdiv(c2, len);
+    for (int it = 0; it < 50; ++it) {
+      float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+      for (int i = 0; i < np; ++i) {
+        const float* q = ip[i];
+        const float d = fadd(fadd(fmul(q[3], fsub(c0, q[0])), fmul(q[4], fsub(c1, q[1]))), fmul(q[5], fsub(c2, q[2])));
+        f0 = fadd(f0, fmul(fmul(q[3], -1.0f), d));
+        f1 = fadd(f1, fmul(fmul(q[4], -1.0f), d));
+        f2 = fadd(f2, fmul(fmul(q[5], -1.0f), d));
+      }
+      const float damping = fsub(1.0f, fdiv(__int2float_rn(it), 50.0f));
+      c0 = fadd(c0, fdiv(fmul(f0, damping), len));
+      c1 = fadd(c1, fdiv(fmul(f1, damping), len));
+      c2 = fadd(c2, fdiv(fmul(f2, damping), len));
+      if (fadd(fadd(fmul(f0, f0), fmul(f1, f1)), fmul(f2, f2)) < 1e-6f) break;
+    }
+    float* out = cells + (celloff[l] + rank512(m, o)) * 3;
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+  }
+}
+
+__device__ __forceinline__ const float* cell_point(const int* nb, const uint32_t* cellm, const uint32_t* celloff,
+                                                   const float* cells, int x, int y, int z) {
+  const int k = ((x >> 3) + 1) * 9 + ((y >> 3) + 1) * 3 + ((z >> 3) + 1);
+  const int l = nb[k];
+  if (l < 0) return nullptr;
+  const int o = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
+  const uint32_t* m = cellm + uint64_t(l) * 16;
+  if (!((m[o >> 5] >> (o & 31)) & 1u)) return nullptr;
+  return cells + (celloff[l] + rank512(m, o)) * 3;
+}
+
+__device__ __forceinline__ bool degenerate(const float* a, const float* b, const float* c) {
+  const float e0 = fsub(b[0], a[0]), e1 = fsub(b[1], a[1]), e2 = fsub(b[2], a[2]);
+  const float f0 = fsub(c[0], a[0]), f1 = fsub(c[1], a[1]), f2 = fsub(c[2], a[2]);
+  const float x = fsub(fmul(e1, f2), fmul(e2, f1)), y = fsub(fmul(e2, f0), fmul(e0, f2)),
+              z = fsub(fmul(e0, f1), fmul(e1, f0));
+  return fadd(fadd(fmul(x, x), fmul(y, y)), fmul(z, z)) == 0.0f;
+}
+
+// Pass 3: the two triangles of every quad around a sign-change edge
+// (dual_contouring.rs:93-139), scaled by the voxel size, minus exactly
+// degenerate ones (dual_contouring.rs:62-79).  Writes up to 6 triangles of
+// voxel (x, y, z) to `out` (when not null) and returns how many there are.
+__device__ __forceinline__ int voxel_tris(const DcVol& V, const int* nb, const uint32_t* __restrict__ cm,
+                                          const uint32_t* __restrict__ cellm, const uint32_t* __restrict__ celloff,
+                                          const float* __restrict__ cells, uint64_t l, int x, int y, int z, float h,
+                                          float* out) {
+  const int o = (x << 6) | (y << 3) | z;
+  const uint32_t any = (cm[(l * 3 + 0) * 16 + (o >> 5)] | cm[(l * 3 + 1) * 16 + (o >> 5)] |
+                        cm[(l * 3 + 2) * 16 + (o >> 5)]) >> (o & 31);
+  if (!(any & 1u)) return 0;
+  float v1 = 0.f;
+  at(V, nb, x, y, z, v1);
+  int nt = 0;
+  for (int dir = 0; dir < 3; ++dir) {
+    if (!((cm[(l * 3 + dir) * 16 + (o >> 5)] >> (o & 31)) & 1u)) continue;
+    const float* q[4];
+    bool ok = true;
+    for (int c = 0; c < 4 && ok; ++c) {
+      q[c] = cell_point(nb, cellm, celloff, cells, x + c_cells[dir][c][0], y + c_cells[dir][c][1],
+                        z + c_cells[dir][c][2]);
+      ok = q[c] != nullptr;
+    }
+    if (!ok) continue;
+    // [p0, p1, p2, p2, p3, p0], with (1,2) and (4,5) swapped when v1 < 0
+    const float* f[6] = {q[0], q[1], q[2], q[2], q[3], q[0]};
+    if (signbit(v1)) {
+      const float* t = f[1];
+      f[1] = f[2];
+      f[2] = t;
+      t = f[4];
+      f[4] = f[5];
+      f[5] = t;
+    }
+    for (int tt = 0; tt < 2; ++tt) {
+      float a[3], b[3], c[3];
+      for (int i = 0; i < 3; ++i) {
+        a[i] = fmul(f[3 * tt][i], h);
+        b[i] = fmul(f[3 * tt + 1][i], h);
+        c[i] = fmul(f[3 * tt + 2][i], h);
+      }
+      if (degenerate(a, b, c)) continue;
+      if (out) {
+        float* d = out + nt * 9;
+        for (int i = 0; i < 3; ++i) {
+          d[i] = a[i];
+          d[3 + i] = b[i];
+          d[6 + i] = c[i];
+        }
+      }
+      ++nt;
+    }
+  }
+  return nt;
+}
+
+__global__ void __launch_bounds__(128) k_dc_quads(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
+                                                  const uint32_t* __restrict__ cellm, const uint32_t* __restrict__ celloff,
+                                                  const float* __restrict__ cells, float h, uint32_t* __restrict__ vcount,
+                                                  const uint32_t* __restrict__ voff, float* __restrict__ tris) {
+  __shared__ int nb[27];
+  const uint64_t l = blockIdx.x;
+  if (l >= n) return;
+  const int4 org = V.org[l];
+  load_neighbours(V, org, nb);
+  __syncthreads();
+  for (int o = threadIdx.x; o < 512; o += blockDim.x) {
+    const int x = o >> 6, y = (o >> 3) & 7, z = o & 7;
+    if (tris) {
+      voxel_tris(V, nb, cm, cellm, celloff, cells, l, x, y, z, h, tris + uint64_t(voff[l * 512 + o]) * 9);
+    } else {
+      vcount[l * 512 + o] = uint32_t(voxel_tris(V, nb, cm, cellm, celloff, cells, l, x, y, z, h, nullptr));
+    }
+  }
+  if (!tris && l == n - 1 && threadIdx.x == 0) vcount[n * 512] = 0;
+}
+
+static bool has_active_tiles(const bs_volume* v) { return v->n_tiles != 0; }
+
+void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size) {
+  if (v->dc_valid && v->dc_h == voxel_size) return;
+  if (has_active_tiles(v)) fail(BS_ERR_UNSUPPORTED, "dual contouring of a volume with active tiles (the reference stops with todo!())");
+  cudaStream_t s = ctx->stream;
+  dfree(ctx, v->d_dc_tris);
+  v->d_dc_tris = nullptr;
+  v->n_dc_tris = 0;
+  const uint64_t n = v->n_leaves;
+  if (n == 0) {
+    v->dc_valid = true;
+    v->dc_h = voxel_size;
+    return;
+  }
+  LeafHashBuf hb;
+  hb.build(ctx, v->d_origins, n, n);
+  DcVol V{v->d_origins, v->d_values, v->d_masks, hb.h};
+  DBuf<DcStats> st(ctx, 1);
+  BS_CUDA(cudaMemsetAsync(st.p, 0, sizeof(DcStats), s));
+  // 1. crossings
+  DBuf<uint32_t> cm(ctx, n * 3 * 16), ccnt(ctx, n * 3 + 1), coff(ctx, n * 3 + 1);
+  BS_KERNEL(ctx, "k_dc_edge_mask", (k_dc_edge_mask<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, ccnt.p)));
+  scan_e(ctx, ccnt.p, coff.p, n * 3 + 1);
+  uint32_t ne = 0;
+  read_back(ctx, &ne, coff.p + n * 3, sizeof(uint32_t));
+  DBuf<float> pts(ctx, uint64_t(ne) * 6);
+  BS_KERNEL(ctx, "k_dc_edge_points", (k_dc_edge_points<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, coff.p, pts.p, st.p)));
+  // 2. cells
+  DBuf<uint32_t> cellm(ctx, n * 16), cellc(ctx, n + 1), celloff(ctx, n + 1);
+  BS_KERNEL(ctx, "k_dc_cell_mask", (k_dc_cell_mask<<<unsigned(n), 128, 0, s>>>(V, n, cellm.p, cellc.p)));
+  scan_e(ctx, cellc.p, celloff.p, n + 1);
+  uint32_t nc = 0;
+  read_back(ctx, &nc, celloff.p + n, sizeof(uint32_t));
+  DBuf<float> cells(ctx, uint64_t(nc) * 3);
+  BS_KERNEL(ctx, "k_dc_cell_points", (k_dc_cell_points<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, coff.p, pts.p, cellm.p, celloff.p, cells.p)));
+  // 3. quads
+  DBuf<uint32_t> vcnt(ctx, n * 512 + 1), voff(ctx, n * 512 + 1);
+  BS_KERNEL(ctx, "k_dc_quads", (k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, cellm.p, celloff.p, cells.p, voxel_size, vcnt.p, nullptr, nullptr)));
+  scan_e(ctx, vcnt.p, voff.p, n * 512 + 1);
+  uint32_t nt = 0;
+  read_back(ctx, &nt, voff.p + n * 512, sizeof(uint32_t));
+  DcStats hs;
+  read_back(ctx, &hs, st.p, sizeof hs);
+  if (hs.error == 1)
+    fail(BS_ERR_UNSUPPORTED, "dual contouring: gradient at a voxel with no active neighbour on an axis (the reference stops with unreachable!())");
+  v->d_dc_tris = dalloc<float>(ctx, uint64_t(nt) * 9);
+  if (nt)
+    BS_KERNEL(ctx, "k_dc_quads", (k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, cellm.p, celloff.p, cells.p, voxel_size, nullptr, voff.p, v->d_dc_tris)));
+  v->n_dc_tris = nt;
+  v->dc_valid = true;
+  v->dc_h = voxel_size;
+  ctx->last_stats[6] = ne;
+  ctx->last_stats[7] = nc;
+}
+
+}  // namespace bs

@@ -536,21 +536,25 @@ constexpr float FOUR_PI = 12.566370614359172f;
 constexpr int WN_STACK = 96;
 
 // Van Oosterom–Strackee solid angle (aabb_tree.rs:582-615), divided by 4 pi.
+// Computed with the reference's operation order and no fused multiply-adds:
+// for query points on a triangle's plane the numerator is then the
+// reference's exact value (often exactly 0, which the reference treats as
+// "on the surface"), so such voxels take the reference's sign.
+__device__ __forceinline__ F3 cross3(F3 a, F3 b) {
+  return {fsub(fmul(a.y, b.z), fmul(a.z, b.y)), fsub(fmul(a.z, b.x), fmul(a.x, b.z)),
+          fsub(fmul(a.x, b.y), fmul(a.y, b.x))};
+}
 __device__ __forceinline__ float tri_wn(float4 A, float4 B, float4 C, F3 q) {
-  float ax = A.x - q.x, ay = A.y - q.y, az = A.z - q.z;
-  float bx = B.x - q.x, by = B.y - q.y, bz = B.z - q.z;
-  float cx = C.x - q.x, cy = C.y - q.y, cz = C.z - q.z;
-  float la = sqrtf(ax * ax + ay * ay + az * az), lb = sqrtf(bx * bx + by * by + bz * bz),
-        lc = sqrtf(cx * cx + cy * cy + cz * cz);
+  F3 qa = sub3(f3(A.x, A.y, A.z), q), qb = sub3(f3(B.x, B.y, B.z), q), qc = sub3(f3(C.x, C.y, C.z), q);
+  const float la = fsqrt(dot3(qa, qa)), lb = fsqrt(dot3(qb, qb)), lc = fsqrt(dot3(qc, qc));
   if (la == 0.f || lb == 0.f || lc == 0.f) return 0.f;
-  ax /= la; ay /= la; az /= la;
-  bx /= lb; by /= lb; bz /= lb;
-  cx /= lc; cy /= lc; cz /= lc;
-  float ux = bx - ax, uy = by - ay, uz = bz - az, vx = cx - ax, vy = cy - ay, vz = cz - az;
-  float num = ax * (uy * vz - uz * vy) + ay * (uz * vx - ux * vz) + az * (ux * vy - uy * vx);
+  qa = f3(fdiv(qa.x, la), fdiv(qa.y, la), fdiv(qa.z, la));
+  qb = f3(fdiv(qb.x, lb), fdiv(qb.y, lb), fdiv(qb.z, lb));
+  qc = f3(fdiv(qc.x, lc), fdiv(qc.y, lc), fdiv(qc.z, lc));
+  const float num = dot3(qa, cross3(sub3(qb, qa), sub3(qc, qa)));
   if (num == 0.f) return 0.f;
-  float den = 1.f + (ax * bx + ay * by + az * bz) + (ax * cx + ay * cy + az * cz) + (bx * cx + by * cy + bz * cz);
-  return atan2f(num, den) * (2.0f / FOUR_PI);
+  const float den = fadd(fadd(fadd(1.0f, dot3(qa, qb)), dot3(qa, qc)), dot3(qb, qc));
+  return fdiv(fmul(atan2f(num, den), 2.0f), FOUR_PI);
 }
 
 // Warp-coherent traversal: the 32 lanes of a warp hold 32 consecutive active
@@ -681,6 +685,9 @@ bs_volume* mesh_to_volume_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, con
   read_back(ctx, &hb.total, soff.p + nt, sizeof(uint32_t));
   if (hb.st.error == 1) fail(BS_ERR_INVALID_ARG, "triangle vertex index out of range");
   if (hb.st.error == 4) fail(BS_ERR_CAPACITY, "coordinates / voxel size exceed the int32 voxel grid");
+  for (int k = 0; k < 3; ++k)  // leaf keys pack 21 bits per axis of origin / 8
+    if (hb.st.vmin[k] < -(1 << 23) + 64 || hb.st.vmax[k] > (1 << 23) - 64)
+      fail(BS_ERR_CAPACITY, "mesh extent / voxel size exceeds +-2^23 voxels per axis");
   // count of sub-triangles in 64 bit: nsub sums can wrap in uint32
   if (hb.st.n_sub >= (1ull << 32)) fail(BS_ERR_CAPACITY, "more than 2^32 sub-triangles");
   const uint64_t ns = hb.total;

@@ -140,6 +140,29 @@ bs_status bs_volume_offset(bs_ctx* ctx, bs_volume* v, float distance);
 bs_status bs_dual_contour(bs_ctx* ctx, bs_volume* v, float voxel_size, float* h_tris,
                           uint64_t capacity, uint64_t* n_tris);
 
+/* ------------------------------------------------------- CornerTable ---- */
+typedef struct bs_corner_table bs_corner_table;
+
+/* CornerTable::builder_soup().add_faces(..).finish() (mesh/corner_table/builder.rs:292-309):
+ * exactly equal points merged (algo/merge_points.rs:12-41), faces added in
+ * order with non-manifold faces skipped, isolated vertices deleted and
+ * non-manifold vertices split (builder.rs:168-262).  h_tris: 9 floats per
+ * triangle in HOST memory. */
+bs_status bs_corner_table_from_soup(bs_ctx* ctx, const float* h_tris, uint64_t n_tris, bs_corner_table** out);
+/* The same on the dual-contouring output of a volume, without a host round
+ * trip of the soup (VoxelRemesher with MeshingMethod::FeaturePreserving,
+ * remeshing/voxel.rs:64-85). */
+bs_status bs_corner_table_from_dual_contour(bs_ctx* ctx, bs_volume* v, float voxel_size, bs_corner_table** out);
+/* Faces, live vertices, vertex slots (live + deleted) and corners. */
+bs_status bs_corner_table_counts(const bs_corner_table* t, uint64_t* n_faces, uint64_t* n_vertices,
+                                 uint64_t* n_vertex_slots, uint64_t* n_corners);
+/* Copies the tables to HOST memory (any pointer may be NULL): positions
+ * [3*slots], deleted flags [slots], vertex -> corner [slots] (-1 none),
+ * corner -> vertex [corners], corner -> opposite corner [corners] (-1 none). */
+bs_status bs_corner_table_export(const bs_corner_table* t, float* h_positions, uint8_t* h_deleted,
+                                 int32_t* h_vertex_corner, int32_t* h_corner_vertex, int32_t* h_corner_opposite);
+bs_status bs_corner_table_free(bs_corner_table* t);
+
 #ifdef __cplusplus
 }
 #endif

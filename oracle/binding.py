@@ -46,6 +46,7 @@ def lib():
                 "orc_set_num_threads": (None, [C.c_int]),
                 "orc_mesh_to_volume": (vp, [f32p, i64, u32p, i64, f32, i64, vp, vp]),
                 "orc_volume_free": (None, [vp]),
+                "orc_volume_from_leaves": (vp, [i32p, f32p, u32p, i64, f32]),
                 "orc_volume_clone": (vp, [vp]),
                 "orc_volume_num_leaves": (i64, [vp]),
                 "orc_volume_export": (None, [vp, i32p, vp, vp]),
@@ -173,6 +174,14 @@ def mesh_to_volume(verts, tris, voxel_size, band, with_wn=False):
         lib().orc_volume_free(h2)
     keys = ["subtris", "pairs", "far_evals", "leaf_tri_evals", "band_voxels", "near_threshold"]
     return vol, dict(zip(keys, (int(x) for x in stats))), wn
+
+
+def volume_from_leaves(origins, values, masks, voxel_size):
+    """An oracle volume holding exported leaves (e.g. a GPU result)."""
+    o = np.ascontiguousarray(origins, np.int32)
+    v = np.ascontiguousarray(values, np.float32)
+    m = np.ascontiguousarray(masks, np.uint32)
+    return OracleVolume(lib().orc_volume_from_leaves(o, v, m, len(o), float(voxel_size)), float(voxel_size))
 
 
 def fast_wn(verts, tris, points, beta=2.0):

@@ -106,6 +106,21 @@ void* orc_mesh_to_volume(const float* xyz, int64_t nv, const uint32_t* tri, int6
 }
 
 void orc_volume_free(void* v) { delete static_cast<Volume*>(v); }
+
+// Builds an oracle volume from exported leaves (origins, all 512 values,
+// masks) so that results computed elsewhere can be checked by the oracle.
+void* orc_volume_from_leaves(const int32_t* origins, const float* values, const uint32_t* masks, int64_t n,
+                             float voxel_size) {
+  auto g = std::make_unique<Grid>();
+  for (int64_t i = 0; i < n; ++i) {
+    auto leaf = Leaf3::empty(i3(origins[3 * i], origins[3 * i + 1], origins[3 * i + 2]));
+    std::memcpy(leaf->values, values + 512 * i, 512 * sizeof(float));
+    for (int o = 0; o < 512; ++o)
+      if ((masks[16 * i + (o >> 5)] >> (o & 31)) & 1u) leaf->mask.on(o);
+    g->insert_leaf_at(std::move(leaf));
+  }
+  return new Volume{std::move(g), voxel_size};
+}
 void* orc_volume_clone(void* v) {
   auto* s = static_cast<Volume*>(v);
   return new Volume{s->grid->clone(), s->voxel_size};
