@@ -54,6 +54,7 @@ SIGNATURES = {
     "bs_volume_intersect": (i32, [vp, vp, vp, PP]),
     "bs_volume_offset": (i32, [vp, vp, f32]),
     "bs_dual_contour": (i32, [vp, vp, f32, vp, u64, C.POINTER(u64)]),
+    "bs_dual_contour_noalloc": (i32, [i32, vp, vp, vp, vp, u64, f32, vp, u64, C.POINTER(u64)]),
     "bs_corner_table_from_soup": (i32, [vp, vp, u64, PP]),
     "bs_corner_table_from_dual_contour": (i32, [vp, vp, f32, PP]),
     "bs_corner_table_counts": (i32, [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),

@@ -1,0 +1,199 @@
+// Dual contouring for callers that cannot allocate device memory.
+//
+// Some hosts of this library run where cudaMalloc is off limits at call
+// time: a renderer or simulation that has carved all device memory up front
+// and forbids allocations in its frame loop, a real-time thread that must not
+// block in the driver's allocator, or a plugin sandbox whose host owns every
+// allocation.  bs_dual_contour_noalloc serves them: it takes the volume's
+// leaves and the output buffer as device pointers the caller owns, and keeps
+// all of its working memory in one file-scope static device array of
+// DCNA_SCRATCH_BYTES, which exists on every GPU that loads the library from
+// module load until process exit.  It calls no cudaMalloc, cudaFree or
+// allocating library routine.
+//
+// The array is shared by every call on a device and keeps the previous call's
+// contents; each call clears what must start empty (the leaf hash and the
+// error flag).  Calls whose work overlaps on the GPU (two streams, or two host
+// threads) race on the array and must be serialised by the caller.
+//
+// The first call on a device resolves the array's device address with
+// cudaGetSymbolAddress (with that device current) and caches it; make that
+// first call before any stream capture.
+#include <cub/device/device_scan.cuh>
+
+#include <mutex>
+
+#include "bs_internal.cuh"
+#include "leaf_hash.cuh"
+
+namespace bs {
+
+// Declarations of the dual-contouring kernels defined in dc.cu and of the
+// hash fill kernel in offset.cu (same definitions as there).
+struct DcVol {
+  const int4* org;
+  const float* val;
+  const uint32_t* msk;
+  LeafHash hash;
+};
+struct DcStats {
+  int error;
+};
+__global__ void k_dc_edge_mask(DcVol V, uint64_t n, uint32_t* __restrict__ cm, uint32_t* __restrict__ ccount);
+__global__ void k_dc_edge_points(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
+                                 const uint32_t* __restrict__ coff, float* __restrict__ pts, DcStats* st);
+__global__ void k_dc_cell_mask(DcVol V, uint64_t n, uint32_t* __restrict__ cellm, uint32_t* __restrict__ ccount);
+__global__ void k_dc_cell_points(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
+                                 const uint32_t* __restrict__ coff, const float* __restrict__ pts,
+                                 const uint32_t* __restrict__ cellm, const uint32_t* __restrict__ celloff,
+                                 float* __restrict__ cells);
+__global__ void k_dc_quads(DcVol V, uint64_t n, const uint32_t* __restrict__ cm, const uint32_t* __restrict__ cellm,
+                           const uint32_t* __restrict__ celloff, const float* __restrict__ cells, float h,
+                           uint32_t* __restrict__ vcount, const uint32_t* __restrict__ voff, float* __restrict__ tris);
+__global__ void k_hash_insert(LeafHash h, const int4* __restrict__ org, uint64_t n, int* __restrict__ err);
+
+}  // namespace bs
+
+namespace {
+
+// Limits of the static working memory (about 24 MiB in use of 32 MiB).
+constexpr uint64_t DCNA_MAX_LEAVES = 2048;       // leaves of the input volume
+constexpr uint64_t DCNA_MAX_CROSSINGS = 393216;  // sign-change edges
+constexpr uint64_t DCNA_MAX_CELLS = 393216;      // cells that get a vertex
+constexpr uint64_t DCNA_HASH_CAP = 8192;         // power of two >= 2 * DCNA_MAX_LEAVES
+constexpr uint64_t DCNA_SCRATCH_BYTES = 32ull << 20;
+
+__device__ __align__(256) unsigned char g_dc_scratch[DCNA_SCRATCH_BYTES];
+
+struct Carve {  // bump allocation inside the static array, 256-byte aligned
+  unsigned char* base;
+  uint64_t used = 0;
+  template <class T>
+  T* take(uint64_t count) {
+    used = (used + 255) & ~uint64_t(255);
+    T* p = reinterpret_cast<T*>(base + used);
+    used += count * sizeof(T);
+    if (used > DCNA_SCRATCH_BYTES) throw bs::Error{BS_ERR_CAPACITY, "no-alloc dual contouring: scratch layout exceeds its array"};
+    return p;
+  }
+};
+
+std::mutex g_setup_mutex;
+void* g_scratch_ptr[64] = {nullptr};
+
+// Once per device, with that device current: the device address of the array.
+unsigned char* scratch_for(int device) {
+  if (device < 0 || device >= 64) throw bs::Error{BS_ERR_INVALID_ARG, "device index out of range"};
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (!g_scratch_ptr[device]) {
+    void* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_dc_scratch);
+    if (e != cudaSuccess || !ptr)
+      throw bs::Error{BS_ERR_CUDA, std::string("cudaGetSymbolAddress(g_dc_scratch): ") + cudaGetErrorString(e)};
+    g_scratch_ptr[device] = ptr;
+  }
+  return static_cast<unsigned char*>(g_scratch_ptr[device]);
+}
+
+__global__ void k_origins_to_int4(const int32_t* __restrict__ o3, uint64_t n, int4* __restrict__ o4) {
+  const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i < n) o4[i] = make_int4(o3[3 * i], o3[3 * i + 1], o3[3 * i + 2], 0);
+}
+
+inline unsigned nblocks(uint64_t n, unsigned t) { return unsigned((n + t - 1) / t); }
+
+template <class T>
+void scan_in(cudaStream_t s, void* temp, size_t temp_bytes, const T* in, T* out, uint64_t n) {
+  size_t need = 0;
+  BS_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, need, in, out, n, s));
+  if (need > temp_bytes) throw bs::Error{BS_ERR_CAPACITY, "no-alloc dual contouring: scan workspace too small"};
+  BS_CUDA(cub::DeviceScan::ExclusiveSum(temp, need, in, out, n, s));
+}
+
+template <class T>
+T read1(cudaStream_t s, const T* dev) {
+  T v{};
+  BS_CUDA(cudaMemcpyAsync(&v, dev, sizeof(T), cudaMemcpyDeviceToHost, s));
+  BS_CUDA(cudaStreamSynchronize(s));
+  return v;
+}
+
+}  // namespace
+
+extern "C" bs_status bs_dual_contour_noalloc(int device, void* stream, const int32_t* d_origins, const float* d_values,
+                                             const uint32_t* d_masks, uint64_t n_leaves, float voxel_size,
+                                             float* d_tris, uint64_t capacity, uint64_t* n_tris) {
+  using namespace bs;
+  if (!n_tris || (n_leaves && (!d_origins || !d_values || !d_masks)) || (capacity && !d_tris))
+    return BS_ERR_INVALID_ARG;
+  *n_tris = 0;
+  if (n_leaves > DCNA_MAX_LEAVES) return BS_ERR_CAPACITY;
+  try {
+    BS_CUDA(cudaSetDevice(device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (n_leaves == 0) return BS_OK;
+    Carve c{scratch_for(device)};
+    const uint64_t n = n_leaves;
+    int4* org = c.take<int4>(n);
+    unsigned long long* hkeys = c.take<unsigned long long>(DCNA_HASH_CAP);
+    int* hvals = c.take<int>(DCNA_HASH_CAP);
+    int* herr = c.take<int>(1);
+    DcStats* st = c.take<DcStats>(1);
+    uint32_t* cm = c.take<uint32_t>(n * 3 * 16);
+    uint32_t* ccnt = c.take<uint32_t>(n * 3 + 1);
+    uint32_t* coff = c.take<uint32_t>(n * 3 + 1);
+    float* pts = c.take<float>(DCNA_MAX_CROSSINGS * 6);
+    uint32_t* cellm = c.take<uint32_t>(n * 16);
+    uint32_t* cellc = c.take<uint32_t>(n + 1);
+    uint32_t* celloff = c.take<uint32_t>(n + 1);
+    float* cells = c.take<float>(DCNA_MAX_CELLS * 3);
+    uint32_t* vcnt = c.take<uint32_t>(n * 512 + 1);
+    uint32_t* voff = c.take<uint32_t>(n * 512 + 1);
+    const size_t temp_bytes = 1u << 20;
+    void* temp = c.take<unsigned char>(temp_bytes);
+    // start empty: hash, error flags
+    BS_CUDA(cudaMemsetAsync(hkeys, 0xff, DCNA_HASH_CAP * sizeof(unsigned long long), s));
+    BS_CUDA(cudaMemsetAsync(hvals, 0xff, DCNA_HASH_CAP * sizeof(int), s));
+    BS_CUDA(cudaMemsetAsync(herr, 0, sizeof(int), s));
+    BS_CUDA(cudaMemsetAsync(st, 0, sizeof(DcStats), s));
+    k_origins_to_int4<<<nblocks(n, 256), 256, 0, s>>>(d_origins, n, org);
+    BS_CUDA(cudaGetLastError());
+    LeafHash hash;
+    hash.keys = hkeys;
+    hash.vals = hvals;
+    hash.mask = DCNA_HASH_CAP - 1;
+    k_hash_insert<<<nblocks(n, 256), 256, 0, s>>>(hash, org, n, herr);
+    BS_CUDA(cudaGetLastError());
+    DcVol V{org, d_values, d_masks, hash};
+    k_dc_edge_mask<<<unsigned(n), 128, 0, s>>>(V, n, cm, ccnt);
+    BS_CUDA(cudaGetLastError());
+    scan_in(s, temp, temp_bytes, ccnt, coff, n * 3 + 1);
+    const uint32_t ne = read1(s, coff + n * 3);
+    if (ne > DCNA_MAX_CROSSINGS) return BS_ERR_CAPACITY;
+    k_dc_edge_points<<<unsigned(n), 128, 0, s>>>(V, n, cm, coff, pts, st);
+    BS_CUDA(cudaGetLastError());
+    k_dc_cell_mask<<<unsigned(n), 128, 0, s>>>(V, n, cellm, cellc);
+    BS_CUDA(cudaGetLastError());
+    scan_in(s, temp, temp_bytes, cellc, celloff, n + 1);
+    const uint32_t nc = read1(s, celloff + n);
+    if (nc > DCNA_MAX_CELLS) return BS_ERR_CAPACITY;
+    k_dc_cell_points<<<unsigned(n), 128, 0, s>>>(V, n, cm, coff, pts, cellm, celloff, cells);
+    BS_CUDA(cudaGetLastError());
+    k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm, cellm, celloff, cells, voxel_size, vcnt, nullptr, nullptr);
+    BS_CUDA(cudaGetLastError());
+    scan_in(s, temp, temp_bytes, vcnt, voff, n * 512 + 1);
+    const uint32_t nt = read1(s, voff + n * 512);
+    if (read1(s, herr)) return BS_ERR_CAPACITY;
+    if (read1(s, st).error == 1) return BS_ERR_UNSUPPORTED;
+    *n_tris = nt;
+    if (nt > capacity) return BS_ERR_CAPACITY;  // *n_tris tells the caller the size to provide
+    if (nt) {
+      k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm, cellm, celloff, cells, voxel_size, nullptr, voff, d_tris);
+      BS_CUDA(cudaGetLastError());
+    }
+    BS_CUDA(cudaStreamSynchronize(s));
+    return BS_OK;
+  } catch (const bs::Error& e) {
+    return e.status;
+  }
+}
