@@ -73,7 +73,11 @@ class Context:
         a = (C.c_uint64 * 8)()
         N.check(self._lib.bs_ctx_last_stats(self.h, a), self.h)
         keys = ["triangles", "subtris", "brick_pairs", "voxel_pairs", "leaves", "active_voxels"]
-        return dict(zip(keys, [int(x) for x in a]))
+        out = dict(zip(keys, [int(x) for x in a]))
+        out["wn_warp_visits"] = int(a[6])
+        out["wn_warp_far"] = int(a[7]) & 0xffffffff
+        out["wn_warp_exact"] = int(a[7]) >> 32
+        return out
 
 
 _default_ctx = None

@@ -250,6 +250,55 @@ __device__ __forceinline__ float point_triangle_dist2(F3 a, F3 b, F3 c, F3 p) {
   return dot3(d, d);
 }
 
+// The same with the triangle's edges ab = b - a, ac = c - a, cb = c - b
+// computed once by the caller (the identical roundings).
+__device__ __forceinline__ float point_triangle_dist2_e(F3 a, F3 b, F3 c, F3 ab, F3 ac, F3 cb, F3 p) {
+  F3 ap = sub3(p, a);
+  float d1 = dot3(ab, ap), d2 = dot3(ac, ap);
+  F3 q;
+  if (d1 <= 0.0f && d2 <= 0.0f) {
+    q = a;
+  } else {
+    F3 bp = sub3(p, b);
+    float d3 = dot3(ab, bp), d4 = dot3(ac, bp);
+    if (d3 >= 0.0f && d4 <= d3) {
+      q = b;
+    } else {
+      float vc = fsub(fmul(d1, d4), fmul(d3, d2));
+      if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f) {
+        float v = fdiv(d1, fsub(d1, d3));
+        q = add3(a, scale3(ab, v));
+      } else {
+        F3 cp = sub3(p, c);
+        float d5 = dot3(ab, cp), d6 = dot3(ac, cp);
+        if (d6 >= 0.0f && d5 <= d6) {
+          q = c;
+        } else {
+          float vb = fsub(fmul(d5, d2), fmul(d1, d6));
+          if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f) {
+            float w = fdiv(d2, fsub(d2, d6));
+            q = add3(a, scale3(ac, w));
+          } else {
+            float va = fsub(fmul(d3, d6), fmul(d5, d4));
+            float d43 = fsub(d4, d3), d56 = fsub(d5, d6);
+            if (va <= 0.0f && d43 >= 0.0f && d56 >= 0.0f) {
+              float w = fdiv(d43, fadd(d43, d56));
+              q = add3(b, scale3(cb, w));
+            } else {
+              float denom = fdiv(1.0f, fadd(fadd(va, vb), vc));
+              float v = fmul(vb, denom);
+              float w = fmul(vc, denom);
+              q = add3(add3(a, scale3(ab, v)), scale3(ac, w));
+            }
+          }
+        }
+      }
+    }
+  }
+  F3 d = sub3(q, p);
+  return dot3(d, d);
+}
+
 }  // namespace bs
 
 // Releases the upper-level (internal node) tables of a volume (volume_ops.cu).

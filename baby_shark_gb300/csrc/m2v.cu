@@ -19,6 +19,7 @@
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 
 #include "bs_internal.cuh"
@@ -56,6 +57,9 @@ struct M2VStats {
   unsigned long long n_sub;    // 64-bit totals (the scans run in 32 bit)
   unsigned long long n_pairs;  // (brick, sub-triangle) pairs
   unsigned long long n_vpairs; // (voxel, sub-triangle) pairs = sum of widened box volumes
+  unsigned long long wn_visits;      // warp-level node visits of the winding-number pass
+  unsigned long long wn_far;         // warp-level far-field evaluations (internal + leaf dipoles)
+  unsigned long long wn_exact;       // warp-level exact solid angles
 };
 
 struct SubTri {  // 64 B: vertices and the widened inclusive integer box
@@ -283,40 +287,83 @@ __global__ void k_fill_pairs(const SubTri* __restrict__ S, uint64_t ns, Dir d, u
 // float order; NaN distances are skipped, as `dist < cur` never holds for NaN
 // in the reference).
 constexpr int DIST_THREADS = 128;
+constexpr int DIST_BATCH = 8;  // sub-triangles a warp packs into one stream of (voxel, sub-triangle) pairs
+
+struct BatchTri {
+  float a[3], b[3], c[3], ab[3], ac[3], cb[3];
+  int x0, y0, z0, ny, nz, nyz;
+  float rnyz, rnz;
+};
 
 __global__ void __launch_bounds__(DIST_THREADS) k_brick_distance(
     const int4* __restrict__ origins, const uint32_t* __restrict__ list_off, const uint32_t* __restrict__ list,
     const SubTri* __restrict__ S, float h, float* __restrict__ values, uint32_t* __restrict__ masks) {
   __shared__ uint32_t dmin[512];
+  __shared__ BatchTri bt[DIST_THREADS / 32][DIST_BATCH];
+  __shared__ int pre[DIST_THREADS / 32][DIST_BATCH + 1];
   const int b = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int4 org = origins[b];
   for (int o = t; o < 512; o += DIST_THREADS) dmin[o] = 0x7f800000u;  // +inf
   __syncthreads();
   const uint32_t beg = list_off[b], end = list_off[b + 1];
-  for (uint32_t e = beg + warp; e < end; e += DIST_THREADS / 32) {
-    const SubTri& st = S[list[e]];
-    const float4 q0 = st.p0, q1 = st.p1, q2 = st.p2;
-    const int4 lo = st.lo, hi = st.hi;
-    const F3 a = f3(q0.x, q0.y, q0.z), bb = f3(q0.w, q1.x, q1.y), c = f3(q1.z, q1.w, q2.x);
-    const int x0 = max(lo.x, org.x), y0 = max(lo.y, org.y), z0 = max(lo.z, org.z);
-    const int nx = min(hi.x, org.x + 7) - x0 + 1, ny = min(hi.y, org.y + 7) - y0 + 1,
-              nz = min(hi.z, org.z + 7) - z0 + 1;
-    if (nx <= 0 || ny <= 0 || nz <= 0) continue;
-    const int nyz = ny * nz, cnt = nx * nyz;
-    // k -> (ix, iy, iz) by reciprocal multiply: k < 512 and nyz <= 64 keep the
-    // product at least 0.5/64 away from the next integer, far above float error
-    const float rnyz = 1.0f / float(nyz), rnz = 1.0f / float(nz);
-    for (int k = lane; k < cnt; k += 32) {
-      const int ix = int((float(k) + 0.5f) * rnyz), r = k - ix * nyz;
-      const int iy = int((float(r) + 0.5f) * rnz), iz = r - iy * nz;
-      const int x = x0 + ix, y = y0 + iy, z = z0 + iz;
+  BatchTri* W = bt[warp];
+  int* P = pre[warp];
+  for (uint32_t e0 = beg + warp * DIST_BATCH; e0 < end; e0 += (DIST_THREADS / 32) * DIST_BATCH) {
+    // lanes 0..BATCH-1: stage one sub-triangle each and count its voxels in this brick
+    int cnt = 0;
+    if (lane < DIST_BATCH && e0 + lane < end) {
+      const SubTri st = S[list[e0 + lane]];
+      const F3 a = f3(st.p0.x, st.p0.y, st.p0.z), bb = f3(st.p0.w, st.p1.x, st.p1.y), c = f3(st.p1.z, st.p1.w, st.p2.x);
+      const int x0 = max(st.lo.x, org.x), y0 = max(st.lo.y, org.y), z0 = max(st.lo.z, org.z);
+      const int nx = min(st.hi.x, org.x + 7) - x0 + 1, ny = min(st.hi.y, org.y + 7) - y0 + 1,
+                nz = min(st.hi.z, org.z + 7) - z0 + 1;
+      if (nx > 0 && ny > 0 && nz > 0) {
+        BatchTri& q = W[lane];
+        const F3 ab = sub3(bb, a), ac = sub3(c, a), cb = sub3(c, bb);
+        q.a[0] = a.x; q.a[1] = a.y; q.a[2] = a.z;
+        q.b[0] = bb.x; q.b[1] = bb.y; q.b[2] = bb.z;
+        q.c[0] = c.x; q.c[1] = c.y; q.c[2] = c.z;
+        q.ab[0] = ab.x; q.ab[1] = ab.y; q.ab[2] = ab.z;
+        q.ac[0] = ac.x; q.ac[1] = ac.y; q.ac[2] = ac.z;
+        q.cb[0] = cb.x; q.cb[1] = cb.y; q.cb[2] = cb.z;
+        q.x0 = x0; q.y0 = y0; q.z0 = z0; q.ny = ny; q.nz = nz; q.nyz = ny * nz;
+        q.rnyz = 1.0f / float(ny * nz);
+        q.rnz = 1.0f / float(nz);
+        cnt = nx * ny * nz;
+      }
+    }
+    // inclusive prefix over the batch lanes
+    int inc = cnt;
+#pragma unroll
+    for (int d = 1; d < DIST_BATCH; d <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, inc, d);
+      if (lane >= d) inc += v;
+    }
+    if (lane < DIST_BATCH) P[lane + 1] = inc;
+    if (lane == 0) P[0] = 0;
+    const int total = __shfl_sync(0xffffffffu, inc, DIST_BATCH - 1);
+    __syncwarp();
+    for (int k = lane; k < total; k += 32) {
+      int j = 0;
+#pragma unroll
+      for (int q = 1; q < DIST_BATCH; ++q) j = (k >= P[q]) ? q : j;
+      const BatchTri& q = W[j];
+      const int r0 = k - P[j];
+      // r0 -> (ix, iy, iz) by reciprocal multiply: r0 < 512 and nyz <= 64 keep
+      // the product at least 0.5/64 away from the next integer
+      const int ix = int((float(r0) + 0.5f) * q.rnyz), r = r0 - ix * q.nyz;
+      const int iy = int((float(r) + 0.5f) * q.rnz), iz = r - iy * q.nz;
+      const int x = q.x0 + ix, y = q.y0 + iy, z = q.z0 + iz;
       const F3 g = f3(fmul(__int2float_rn(x), h), fmul(__int2float_rn(y), h), fmul(__int2float_rn(z), h));
-      const float d2 = point_triangle_dist2(a, bb, c, g);
+      const float d2 = point_triangle_dist2_e(f3(q.a[0], q.a[1], q.a[2]), f3(q.b[0], q.b[1], q.b[2]),
+                                              f3(q.c[0], q.c[1], q.c[2]), f3(q.ab[0], q.ab[1], q.ab[2]),
+                                              f3(q.ac[0], q.ac[1], q.ac[2]), f3(q.cb[0], q.cb[1], q.cb[2]), g);
       if (d2 < __int_as_float(0x7f800000)) {  // false for NaN and +inf
         const int o = ((x - org.x) << 6) | ((y - org.y) << 3) | (z - org.z);
         atomicMin(&dmin[o], __float_as_uint(d2));
       }
     }
+    __syncwarp();
   }
   __syncthreads();
 #pragma unroll
@@ -342,14 +389,29 @@ __global__ void k_brick_popcount(const uint32_t* __restrict__ masks, uint64_t nb
   cnt[b] = c;
 }
 
-// one warp per brick: lane l handles mask words l (l < 16)
+// One warp per brick; active voxels are listed in Morton order inside the
+// brick (lane l covers Morton indices 16l .. 16l+15), so 32 consecutive
+// entries form compact blocks for the warp-coherent winding-number pass.
+__device__ __forceinline__ int morton9_to_offset(int m) {
+  // m = z0 y0 x0 z1 y1 x1 z2 y2 x2 (bit 0 = z0): spread back to x<<6 | y<<3 | z
+  const int z = (m & 1) | ((m >> 2) & 2) | ((m >> 4) & 4);
+  const int y = ((m >> 1) & 1) | ((m >> 3) & 2) | ((m >> 5) & 4);
+  const int x = ((m >> 2) & 1) | ((m >> 4) & 2) | ((m >> 6) & 4);
+  return (x << 6) | (y << 3) | z;
+}
+
 __global__ void k_emit_active(const uint32_t* __restrict__ masks, const uint32_t* __restrict__ off, uint64_t nb,
                               uint32_t* __restrict__ act) {
   uint64_t b = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (b >= nb) return;
-  uint32_t m = lane < 16 ? masks[b * 16 + lane] : 0u;
-  uint32_t c = __popc(m);
+  const uint32_t* m = masks + b * 16;
+  uint32_t bits = 0;
+  for (int k = 0; k < 16; ++k) {
+    const int o = morton9_to_offset(lane * 16 + k);
+    if ((m[o >> 5] >> (o & 31)) & 1u) bits |= 1u << k;
+  }
+  const uint32_t c = __popc(bits);
   uint32_t pre = c;
 #pragma unroll
   for (int s = 1; s < 32; s <<= 1) {
@@ -357,10 +419,10 @@ __global__ void k_emit_active(const uint32_t* __restrict__ masks, const uint32_t
     if (lane >= s) pre += v;
   }
   uint32_t pos = off[b] + pre - c;
-  while (m) {
-    int bit = __ffs(m) - 1;
-    m &= m - 1;
-    act[pos++] = uint32_t(b << 9) | uint32_t(lane * 32 + bit);
+  while (bits) {
+    const int k = __ffs(bits) - 1;
+    bits &= bits - 1;
+    act[pos++] = uint32_t(b << 9) | uint32_t(morton9_to_offset(lane * 16 + k));
   }
 }
 
@@ -544,7 +606,7 @@ __device__ __forceinline__ F3 cross3(F3 a, F3 b) {
   return {fsub(fmul(a.y, b.z), fmul(a.z, b.y)), fsub(fmul(a.z, b.x), fmul(a.x, b.z)),
           fsub(fmul(a.x, b.y), fmul(a.y, b.x))};
 }
-__device__ __forceinline__ float tri_wn(float4 A, float4 B, float4 C, F3 q) {
+__device__ __forceinline__ float tri_wn_exact(float4 A, float4 B, float4 C, F3 q) {
   F3 qa = sub3(f3(A.x, A.y, A.z), q), qb = sub3(f3(B.x, B.y, B.z), q), qc = sub3(f3(C.x, C.y, C.z), q);
   const float la = fsqrt(dot3(qa, qa)), lb = fsqrt(dot3(qb, qb)), lc = fsqrt(dot3(qc, qc));
   if (la == 0.f || lb == 0.f || lc == 0.f) return 0.f;
@@ -556,28 +618,54 @@ __device__ __forceinline__ float tri_wn(float4 A, float4 B, float4 C, F3 q) {
   const float den = fadd(fadd(fadd(1.0f, dot3(qa, qb)), dot3(qa, qc)), dot3(qb, qc));
   return fdiv(fmul(atan2f(num, den), 2.0f), FOUR_PI);
 }
+// Fast form (fused arithmetic, rsqrt normalisation).  Its numerator is within
+// ~1e-6 of the exact one, so whenever |num| > 1e-4 both have the same sign and
+// are nonzero; closer to the triangle's plane the exact form decides.
+__device__ __forceinline__ float tri_wn(float4 A, float4 B, float4 C, F3 q) {
+  float ax = A.x - q.x, ay = A.y - q.y, az = A.z - q.z;
+  float bx = B.x - q.x, by = B.y - q.y, bz = B.z - q.z;
+  float cx = C.x - q.x, cy = C.y - q.y, cz = C.z - q.z;
+  const float la2 = ax * ax + ay * ay + az * az, lb2 = bx * bx + by * by + bz * bz, lc2 = cx * cx + cy * cy + cz * cz;
+  if (!(la2 > 1e-30f) || !(lb2 > 1e-30f) || !(lc2 > 1e-30f)) return tri_wn_exact(A, B, C, q);
+  const float ia = rsqrtf(la2), ib = rsqrtf(lb2), ic = rsqrtf(lc2);
+  ax *= ia; ay *= ia; az *= ia;
+  bx *= ib; by *= ib; bz *= ib;
+  cx *= ic; cy *= ic; cz *= ic;
+  const float ux = bx - ax, uy = by - ay, uz = bz - az, vx = cx - ax, vy = cy - ay, vz = cz - az;
+  const float num = ax * (uy * vz - uz * vy) + ay * (uz * vx - ux * vz) + az * (ux * vy - uy * vx);
+  if (fabsf(num) < 1e-4f) return tri_wn_exact(A, B, C, q);
+  const float den = 1.f + (ax * bx + ay * by + az * bz) + (ax * cx + ay * cy + az * cz) + (bx * cx + by * cy + bz * cz);
+  return atan2f(num, den) * (2.0f / FOUR_PI);
+}
 
 // Warp-coherent traversal: the 32 lanes of a warp hold 32 consecutive active
-// voxels (mostly of one brick, so within a few voxels of each other) and walk
+// voxels — Morton order inside a brick, so mostly a 4x4x2 block — and walk
 // the LBVH together.  A node is summed through its far field only when it is
 // far (|q - p| > beta * r, aabb_tree.rs:666) for every lane; otherwise the
 // warp opens it, and at a leaf every lane takes the exact solid angle.  Node
 // loads are warp-uniform, control flow never diverges, and each lane's sum is
 // at least as accurate as its own traversal would be.
 constexpr int WN_WARPS = 4;
+constexpr int WN_THREADS = 32 * WN_WARPS;
 
-__global__ void __launch_bounds__(32 * WN_WARPS) k_wn_sign(const uint32_t* __restrict__ act, uint64_t na,
-                                                           const int4* __restrict__ origins,
-                                                           float* __restrict__ values,
-                                                           const float4* __restrict__ inode,
-                                                           const float4* __restrict__ leaf, int n, float h,
-                                                           float beta, float thresh, M2VStats* st) {
+__device__ __forceinline__ void kahan(float& sum, float& comp, float w) {
+  const float y = w - comp;
+  const float t = sum + y;
+  comp = (t - sum) - y;
+  sum = t;
+}
+
+__global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restrict__ act, uint64_t na,
+                                                        const int4* __restrict__ origins, float* __restrict__ values,
+                                                        const float4* __restrict__ inode,
+                                                        const float4* __restrict__ leaf, int n, float h, float beta,
+                                                        float thresh, M2VStats* st) {
   __shared__ int stk[WN_WARPS][WN_STACK];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint64_t i = (blockIdx.x * uint64_t(WN_WARPS) + w) * 32 + lane;
   if ((blockIdx.x * uint64_t(WN_WARPS) + w) * 32 >= na) return;  // whole warp out of range
   const bool valid = i < na;
-  uint32_t v = valid ? act[i] : act[na - 1];
+  const uint32_t v = valid ? act[i] : act[na - 1];
   const uint32_t b = v >> 9, o = v & 511;
   const int4 org = origins[b];
   const F3 q = f3(fmul(__int2float_rn(org.x + int(o >> 6)), h), fmul(__int2float_rn(org.y + int((o >> 3) & 7)), h),
@@ -587,25 +675,29 @@ __global__ void __launch_bounds__(32 * WN_WARPS) k_wn_sign(const uint32_t* __res
   int sp = 0;
   int node = n > 1 ? 0 : ~0;
   bool overflow = false;
+  uint32_t c_visit = 0, c_far = 0, c_exact = 0;
   for (long long guard = 0; guard < 2ll * n + 2; ++guard) {
     float wv = 0.f;
     bool have = true;
+    ++c_visit;
     if (node >= 0) {
       const float4 P = inode[5 * node];
       const float rx = P.x - q.x, ry = P.y - q.y, rz = P.z - q.z;
       const float r2 = rx * rx + ry * ry + rz * rz;
-      const float lim = P.w * P.w * beta2;
-      if (__all_sync(0xffffffffu, r2 > lim)) {
+      if (__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) {
+        ++c_far;
         const float4 A = inode[5 * node + 1], B0 = inode[5 * node + 2], B1 = inode[5 * node + 3],
                      B2 = inode[5 * node + 4];
-        const float r1 = sqrtf(r2);
-        const float inv = 1.0f / (FOUR_PI * r2 * r1);
+        // a.r / (4 pi r^3) + trace(B) / (4 pi r^3) - 3 r^T B r / (4 pi r^5)
+        const float ri = rsqrtf(r2);
+        const float ri2 = ri * ri;
+        const float inv = ri2 * ri * (1.0f / FOUR_PI);
         const float ar = A.x * rx + A.y * ry + A.z * rz;
         const float brx = B0.x * rx + B0.y * ry + B0.z * rz;
         const float bry = B0.w * rx + B1.x * ry + B1.y * rz;
         const float brz = B1.z * rx + B1.w * ry + B2.x * rz;
         const float rbr = rx * brx + ry * bry + rz * brz;
-        wv = inv * (ar + A.w) - (3.0f * inv / r2) * rbr;
+        wv = inv * ((ar + A.w) - 3.0f * ri2 * rbr);
       } else {
         const float4 E = inode[5 * node + 4];
         if (sp < WN_STACK) {
@@ -623,18 +715,18 @@ __global__ void __launch_bounds__(32 * WN_WARPS) k_wn_sign(const uint32_t* __res
       const float rx = P.x - q.x, ry = P.y - q.y, rz = P.z - q.z;
       const float r2 = rx * rx + ry * ry + rz * rz;
       if (__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) {
+        ++c_far;
         const float4 A = leaf[5 * li + 1];
-        wv = (A.x * rx + A.y * ry + A.z * rz) / (FOUR_PI * r2 * sqrtf(r2));
+        const float ri = rsqrtf(r2);
+        wv = (A.x * rx + A.y * ry + A.z * rz) * (ri * ri * ri * (1.0f / FOUR_PI));
       } else {
+        ++c_exact;
         wv = tri_wn(leaf[5 * li + 2], leaf[5 * li + 3], leaf[5 * li + 4], q);
       }
     }
     __syncwarp();
     if (have) {
-      const float y = wv - comp;
-      const float t = sum + y;
-      comp = (t - sum) - y;
-      sum = t;
+      kahan(sum, comp, wv);
       if (sp == 0) break;
       --sp;
       node = stk[w][sp];
@@ -642,6 +734,11 @@ __global__ void __launch_bounds__(32 * WN_WARPS) k_wn_sign(const uint32_t* __res
     __syncwarp();
   }
   if (overflow && lane == 0) atomicExch(&st->error, 3);
+  if (lane == 0) {
+    atomicAdd(&st->wn_visits, (unsigned long long)c_visit);
+    atomicAdd(&st->wn_far, (unsigned long long)c_far);
+    atomicAdd(&st->wn_exact, (unsigned long long)c_exact);
+  }
   if (valid) {
     const float d = values[uint64_t(b) * 512 + o];
     values[uint64_t(b) * 512 + o] = (sum < thresh) ? copysignf(d, 1.0f) : copysignf(d, -1.0f);
@@ -783,7 +880,7 @@ bs_volume* mesh_to_volume_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, con
     lsum.reset();
     isum.reset();
     if (na > 0) {
-      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<<<blocks(na, 32 * WN_WARPS), 32 * WN_WARPS, 0, s>>>(act.p, na, vol->d_origins, vol->d_values, inode.p, leaf.p, n, h,
+      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<<<blocks(na, WN_THREADS), WN_THREADS, 0, s>>>(act.p, na, vol->d_origins, vol->d_values, inode.p, leaf.p, n, h,
                                                 p.wn_beta, p.wn_threshold, st.p)));
     }
     read_back(ctx, &hb.st, st.p, sizeof(M2VStats));
@@ -794,6 +891,8 @@ bs_volume* mesh_to_volume_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, con
     ctx->last_stats[3] = hb.st.n_vpairs;
     ctx->last_stats[4] = nb;
     ctx->last_stats[5] = na;
+    ctx->last_stats[6] = hb.st.wn_visits;
+    ctx->last_stats[7] = (hb.st.wn_far & 0xffffffffull) | (hb.st.wn_exact << 32);
   } catch (...) {
     volume_release(vol);
     throw;

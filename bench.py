@@ -38,6 +38,16 @@ import numpy as np  # noqa: E402
 
 H = 0.002
 BAND = 3
+# Algorithmic work per unit.
+FLOP_PER_PAIR = 84          # closest point + norm, triangle3.rs:317-382 (face-region path)
+WN_FLOP_FAR = 31            # far test + order-1/2 terms, aabb_tree.rs:662-671, 803-816
+WN_FLOP_EXACT = 70          # Van Oosterom-Strackee solid angle, aabb_tree.rs:582-615 (atan2 as 20)
+WN_FAR_PER_VOXEL = 110.1    # the oracle's traversal of the reference's SAH tree on this workload's
+WN_EXACT_PER_VOXEL = 14.4   # torus (1/8 ring sample, 4.5 M band voxels): counts per band voxel
+WN_FLOP_PER_VOXEL = int(round(WN_FAR_PER_VOXEL * WN_FLOP_FAR + WN_EXACT_PER_VOXEL * WN_FLOP_EXACT))
+# dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture of
+# the half-ring case, scaled to a full torus by the units processed (profiles/)
+TRAFFIC_PER_LAUNCH = {}
 METRIC = "band voxels/s mesh→SDF+sign: learned/batched vs plain GPU, 0 sign flips"
 UNIT = "band_voxels/s"
 WORKLOAD = "two displaced tori, 1,048,576 triangles each, voxel 0.002, band 3: mesh->SDF+sign (plain GPU path)"
@@ -47,9 +57,19 @@ def rank_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
-def meshes():
+def meshes(fraction=1.0):
+    """Both tori; with fraction < 1 only the triangles of the first part of
+    each ring (a smaller case with the same triangle and voxel sizes)."""
     from baby_shark_gb300 import synthetic
-    return synthetic.config2()
+    a, b = synthetic.config2()
+    if fraction >= 1.0:
+        return a, b
+    out = []
+    for v, f in (a, b):
+        nv = 512
+        keep = (f.max(axis=1) // nv) < int(1024 * fraction)
+        out.append((v, np.ascontiguousarray(f[keep])))
+    return out[0], out[1]
 
 
 class ClockSampler:
@@ -183,7 +203,7 @@ def run_ours(args):
     L = N.load()
     ctx = bs.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
-    (va, fa), (vb, fb) = meshes()
+    (va, fa), (vb, fb) = meshes(args.tris_fraction)
     dev = [(torch.from_numpy(v).cuda(), torch.from_numpy(f.astype(np.int32)).cuda()) for v, f in ((va, fa), (vb, fb))]
     torch.cuda.synchronize()
     params = N.M2VParams()
@@ -276,23 +296,41 @@ def run_ours(args):
     name, (tot_ms, nl) = top
     peaks, src = measured_peaks()
     fp32_peak = fp32_peak_tflops(ctx)
-    # per launch: stats are of the last conversion (torus B); both tori are the same size class
+    per_launch_s = tot_ms / nl / 1000.0
+    # stats are of the last conversion (torus B); both tori are the same size class
     if name == "k_brick_distance":
-        flops = 84.0 * stats["voxel_pairs"]
-        achieved = flops / (tot_ms / nl / 1000.0) / 1e12
+        flops = FLOP_PER_PAIR * stats["voxel_pairs"]
+        algo = "%d FLOP x (voxel, sub-triangle) pairs = %d per launch" % (FLOP_PER_PAIR, stats["voxel_pairs"])
+    elif name == "k_wn_sign":
+        flops = WN_FLOP_PER_VOXEL * stats["active_voxels"]
+        algo = ("%d FLOP per band voxel (the reference's own traversal: %.0f far-field nodes x %d FLOP + "
+                "%.0f exact triangles x %d FLOP, counted by the oracle) x %d voxels per launch"
+                % (WN_FLOP_PER_VOXEL, WN_FAR_PER_VOXEL, WN_FLOP_FAR, WN_EXACT_PER_VOXEL, WN_FLOP_EXACT,
+                   stats["active_voxels"]))
+    else:
+        flops = None
+        algo = None
+    if flops is not None:
+        achieved = flops / per_launch_s / 1e12
         roof = {"kernel": name, "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
-                "peak_source": "measured by bs_diag_fp32_peak (FFMA loop) on this GPU",
-                "algorithmic": "84 FLOP x (voxel, sub-triangle) pairs = %d per launch" % stats["voxel_pairs"]}
+                "frac": achieved / fp32_peak if fp32_peak else None, "traffic": TRAFFIC_PER_LAUNCH.get(name),
+                "peak_source": "measured on this GPU by bs_diag_fp32_peak (FFMA loop); MEASURED_PEAKS.json "
+                               "holds no FP32 figure",
+                "algorithmic": algo}
     else:
         roof = {"kernel": name, "bound": "hbm", "achieved": None, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                 "frac": None, "traffic": None, "peak_source": src}
     roof["share_of_step"] = tot_ms / sum(v[0] for v in stages.values())
+    roof["launch_ms"] = tot_ms / nl
+
+    pipe = pipeline_secondary(ctx, params, dev, L, N, bs, C) if args.pipeline else None
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "triangles_per_step": int(len(fa) + len(fb)),
+            "config": {"workload": WORKLOAD if args.tris_fraction >= 1.0 else
+                       WORKLOAD + " (first %.3g of each ring)" % args.tris_fraction,
+                       "triangles_per_step": int(len(fa) + len(fb)),
                        "band_voxels_per_step": int(band), "l2": "flushed between steps (256 MiB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -300,7 +338,8 @@ def run_ours(args):
             "roofline": roof,
             "clocks": clk,
             "stages_ms_per_step": {k: v[0] / args.steps for k, v in sorted(stages.items(), key=lambda kv: -kv[1][0])},
-            "last_stats": stats}
+            "last_stats": stats,
+            "pipeline": pipe}
     if rank == 0:
         if world == 1:
             line["cpu_baseline"] = cpu_baseline()
@@ -308,6 +347,53 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def pipeline_secondary(ctx, params, dev, L, N, bs, C):
+    """The boolean workload's tail, once per boolean: A op B, then offset +0.01
+    and -0.01 (each on its own copy), then dual contouring of each; CUDA events
+    on the library stream around every stage.  Returns ms per stage and the
+    output triangles."""
+    import torch
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def m2v(k):
+        out = C.c_void_p()
+        x, t = dev[k]
+        N.check(L.bs_mesh_to_volume_device(ctx.h, x.data_ptr(), x.shape[0], t.data_ptr(), t.shape[0],
+                                           C.byref(params), C.byref(out)), ctx.h)
+        return bs.Volume(out, ctx)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return r, e0.elapsed_time(e1)
+
+    res = {}
+    tris_total, dc_ms_total = 0, 0.0
+    for op in ("subtract", "union", "intersect"):
+        a, b = m2v(0), m2v(1)
+        c, t_csg = timed(lambda: getattr(a, op)(b))
+        d = {"csg_ms": t_csg, "leaves": c.counts()["leaves"], "tiles": c.counts()["tiles"]}
+        for sign, dist in (("plus", 0.01), ("minus", -0.01)):
+            cc = c.clone()
+            _, t_off = timed(lambda: cc.offset(dist))
+            mesher = bs.DualContouringMesher().with_voxel_size(H)
+            n = C.c_uint64()
+            _, t_dc = timed(lambda: N.check(L.bs_dual_contour(ctx.h, cc.h, H, None, 0, C.byref(n)), ctx.h))
+            d["offset_%s_ms" % sign] = t_off
+            d["dc_%s_ms" % sign] = t_dc
+            d["dc_%s_triangles" % sign] = int(n.value)
+            tris_total += int(n.value)
+            dc_ms_total += t_dc
+            del cc, mesher
+        res[op] = d
+        del a, b, c
+    res["output_triangles_per_s_dc"] = tris_total / (dc_ms_total / 1000.0) if dc_ms_total else None
+    return res
 
 
 def fp32_peak_tflops(ctx):
@@ -327,6 +413,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-pipeline", dest="pipeline", action="store_false",
+                    help="skip the secondary boolean / offset / dual-contouring timings")
+    ap.add_argument("--tris-fraction", type=float, default=1.0,
+                    help="use only the first part of each torus ring (smaller case for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -75,7 +75,10 @@ bs_status bs_ctx_stage_info(bs_ctx* ctx, int i, const char** name, double* total
 bs_status bs_ctx_stage_reset(bs_ctx* ctx);
 /* Counters of the last mesh -> volume call: [0] triangles, [1] sub-triangles,
  * [2] (brick, sub-triangle) pairs, [3] (voxel, sub-triangle) pairs,
- * [4] leaves, [5] active voxels, [6..7] reserved. */
+ * [4] leaves, [5] active voxels, [6] warp-level node visits of the
+ * winding-number pass, [7] warp-level far-field evaluations (low 32 bits) and
+ * exact solid angles (high 32 bits).  A dual contouring call overwrites
+ * [6] and [7] with its crossing and cell counts. */
 bs_status bs_ctx_last_stats(const bs_ctx* ctx, uint64_t* out8);
 /* Measured FP32 FMA throughput of the context's device in TFLOP/s (a timed
  * FFMA loop over all SMs); the denominator of FP32-bound roofline fractions. */
