@@ -69,7 +69,7 @@ class Context:
         return out
 
     def last_stats(self):
-        """Counters of the last mesh -> volume conversion."""
+        """Counters of the last mesh -> volume conversion (see bs_ctx_last_stats)."""
         a = (C.c_uint64 * 8)()
         N.check(self._lib.bs_ctx_last_stats(self.h, a), self.h)
         keys = ["triangles", "subtris", "brick_pairs", "voxel_pairs", "leaves", "active_voxels"]
@@ -77,6 +77,9 @@ class Context:
         out["wn_warp_visits"] = int(a[6])
         out["wn_warp_far"] = int(a[7]) & 0xffffffff
         out["wn_warp_exact"] = int(a[7]) >> 32
+        # after an offset: relaxation passes and leaf sweeps of its 8 sweeps
+        out["offset_passes"] = int(a[6])
+        out["offset_leaf_sweeps"] = int(a[7])
         return out
 
 

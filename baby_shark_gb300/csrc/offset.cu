@@ -6,19 +6,22 @@
 //
 // The reference sweeps leaves popped from a priority queue in lexicographic
 // order of the sweep direction, and each leaf's voxels in the same order.  A
-// leaf reads only its six face neighbours and writes only itself, so the
-// result depends only on the order of face-adjacent pairs.  Processing leaves
-// by diagonal plane p = sx*bx + sy*by + sz*bz (brick coordinates) keeps that
-// order — a neighbour "before" in the sweep is on plane p - 1, one "after" on
-// p + 1 — and all leaves of a plane run in parallel.  Inside a leaf, the same
-// holds for voxels on diagonal planes ux + uy + uz.  Leaves a leaf spawns lie
-// on the next plane, exactly where the reference's queue would pop them.  So
-// the sweeps are bit-identical to the reference's sequential ones.
+// leaf reads only its six face neighbours and writes only itself, so its
+// sweep is a function of its own input, the outputs of the three neighbours
+// before it in the sweep order and the inputs of the three after it; leaves
+// it spawns lie after it.  The reference's result is therefore the unique
+// fixed point of that dependency order.  Here every leaf is swept at once,
+// and a leaf is swept again whenever a face it read from a before-neighbour
+// changes (k_relax), until nothing changes; a final check drops leaves that
+// only an unconverged pass asked for.  Inside a leaf the voxels go by
+// diagonal planes ux + uy + uz, which keeps their order.  So the sweeps are
+// bit-identical to the reference's sequential ones.
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "bs_internal.cuh"
 #include "leaf_hash.cuh"
@@ -100,17 +103,6 @@ __global__ void k_gather_leaves(const uint32_t* __restrict__ keep, const uint32_
 }
 
 // --------------------------------------------------------------- sweeps ----
-struct SweepState {
-  int4* org;
-  float* val;
-  uint32_t* msk;
-  uint32_t* frz;  // active masks at the start of fast_sweep (fast_sweep.rs:31)
-  LeafHash hash;
-  int* n_leaves;  // device counter (spawned leaves are appended)
-  uint64_t cap;
-  int* overflow;
-};
-
 // fast_sweep.rs:509-537, operation for operation.
 __device__ __forceinline__ float compute_distance(float a1, float a2, float a3, float h) {
   float t;
@@ -136,175 +128,354 @@ __device__ __forceinline__ float compute_distance(float a1, float a2, float a3, 
   return fmul(fadd(a1a2a3_sum, fsqrt(r)), 0.333333343f);  // (1.0 / 3.0) as f32
 }
 
-constexpr int SW_WARPS = 4;
-
-struct WarpLeaf {
-  float val[512];
-  uint32_t msk[16];
-  uint32_t frz[16];
-  int nb[6];  // -x, +x, -y, +y, -z, +z
+// Sweep state for one direction.  A leaf's sweep (fast_sweep.rs:125-183 over
+// its voxels) is a function of its own input, the outputs of its three
+// neighbours before it in the sweep order and the inputs of its three
+// neighbours after it.  Each slot keeps its input, its output, its three
+// after-faces as last published (what its after-neighbours read) and its
+// three before-layers of the input (what its before-neighbours read).
+struct Sweep {
+  int4* org;
+  const float* in_val;
+  const uint32_t* in_msk;
+  float* out_val;
+  uint32_t* out_msk;
+  const uint32_t* frz;  // active masks when fast_sweep started (fast_sweep.rs:31)
+  float* pub_val;       // [slot][axis][64] output after-face, 0 where inactive
+  uint32_t* pub_msk;    // [slot][axis][2]
+  float* inf_val;       // [slot][axis][64] input before-layer, 0 where inactive
+  uint32_t* inf_msk;    // [slot][axis][2]
+  int* alive;           // the slot holds a leaf of the volume
+  int* spawned;         // the leaf was created during this sweep
+  int* wanted;          // a before-neighbour's output asks for it
+  int* dirty;           // queued for a sweep
+  LeafHash hash;
+  int* n_slots;
+  uint64_t cap;
+  int* overflow;
+  int* changed;
+  int sx, sy, sz, neg;
+  float lim, h;
 };
 
-// Active value at local (x, y, z) of the stencil: center (shared) or a face neighbour (global).
-__device__ __forceinline__ bool stencil_at(const WarpLeaf& L, const SweepState& S, int x, int y, int z, float& v) {
-  int which = -1;
-  if (z < 0) which = 4;
-  else if (z > 7) which = 5;
-  else if (y < 0) which = 2;
-  else if (y > 7) which = 3;
-  else if (x < 0) which = 0;
-  else if (x > 7) which = 1;
-  const int o = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
-  if (which < 0) {
-    if (!((L.msk[o >> 5] >> (o & 31)) & 1u)) return false;
-    v = L.val[o];
-    return true;
-  }
-  const int nbi = L.nb[which];
-  if (nbi < 0) return false;
-  if (!((S.msk[uint64_t(nbi) * 16 + (o >> 5)] >> (o & 31)) & 1u)) return false;
-  v = S.val[uint64_t(nbi) * 512 + o];
-  return true;
+constexpr int SW_WARPS = 4;
+constexpr int PAD = 10;  // a leaf with a one-voxel halo: 10 x 10 x 10
+
+__device__ __forceinline__ int pad_idx(int x, int y, int z) { return (x + 1) * PAD * PAD + (y + 1) * PAD + (z + 1); }
+
+__device__ __forceinline__ bool bit(const uint32_t* m, int i) { return (m[i >> 5] >> (i & 31)) & 1u; }
+
+// voxel (a, b) of the layer at local coordinate `fl` across axis `ax`
+__device__ __forceinline__ int face_off(int ax, int fl, int i) {
+  const int a = i >> 3, b = i & 7;
+  return ax == 0 ? ((fl << 6) | (a << 3) | b) : (ax == 1 ? ((a << 6) | (fl << 3) | b) : ((a << 6) | (b << 3) | fl));
+}
+__device__ __forceinline__ int face_pad(int ax, int fl, int i) {
+  const int a = i >> 3, b = i & 7;
+  return ax == 0 ? pad_idx(fl, a, b) : (ax == 1 ? pad_idx(a, fl, b) : pad_idx(a, b, fl));
 }
 
-// option_min_by with the |.| comparison of fast_sweep.rs:141-144 (a is the + side).
-__device__ __forceinline__ bool min_by_abs(bool ha, float a, bool hb, float b, float& out) {
-  if (ha && hb) {
-    out = (fabsf(a) > fabsf(b)) ? b : a;
-    return true;
-  }
-  if (ha) { out = a; return true; }
-  if (hb) { out = b; return true; }
-  return false;
-}
+// option_min_by with the |.| comparison of fast_sweep.rs:141-144, a the + side;
+// an inactive neighbour is +inf (active values are finite), so "none" stays +inf.
+__device__ __forceinline__ float min_by_abs(float a, float b) { return (fabsf(a) > fabsf(b)) ? b : a; }
 
-// fast_sweep.rs:125-183 for one voxel of the center leaf.
-__device__ __forceinline__ void sweep_voxel(WarpLeaf& L, const SweepState& S, int x, int y, int z, bool neg_sweep,
-                                            float limit_abs, float h) {
-  const int o = (x << 6) | (y << 3) | z;
-  if ((L.frz[o >> 5] >> (o & 31)) & 1u) return;
-  float xp, xn, yp, yn, zp, zn, dx, dy, dz;
-  const bool hxp = stencil_at(L, S, x + 1, y, z, xp), hxn = stencil_at(L, S, x - 1, y, z, xn);
-  const bool hyp = stencil_at(L, S, x, y + 1, z, yp), hyn = stencil_at(L, S, x, y - 1, z, yn);
-  const bool hzp = stencil_at(L, S, x, y, z + 1, zp), hzn = stencil_at(L, S, x, y, z - 1, zn);
-  const bool hx = min_by_abs(hxp, xp, hxn, xn, dx);
-  const bool hy = min_by_abs(hyp, yp, hyn, yn, dy);
-  const bool hz = min_by_abs(hzp, zp, hzn, zn, dz);
+// fast_sweep.rs:125-183 for the voxel at padded index p of the tile W.
+__device__ __forceinline__ void sweep_voxel(float* W, int p, bool neg_sweep, float limit_abs, float h) {
+  const float dx = min_by_abs(W[p + PAD * PAD], W[p - PAD * PAD]);
+  const float dy = min_by_abs(W[p + PAD], W[p - PAD]);
+  const float dz = min_by_abs(W[p + 1], W[p - 1]);
+  const bool hx = dx != INFINITY, hy = dy != INFINITY, hz = dz != INFINITY;
   if (!hx && !hy && !hz) return;
   const float first = hx ? dx : (hy ? dy : dz);
   if (bool(signbit(first)) != neg_sweep) return;
   const float d1 = hx ? dx : FAR_F, d2 = hy ? dy : FAR_F, d3 = hz ? dz : FAR_F;
   const float dn_abs = compute_distance(fabsf(d1), fabsf(d2), fabsf(d3), h);
   if (dn_abs > limit_abs) return;
-  const bool act = (L.msk[o >> 5] >> (o & 31)) & 1u;
-  const float d_old = act ? L.val[o] : FAR_F;
-  if (dn_abs < fabsf(d_old)) {
-    L.val[o] = neg_sweep ? copysignf(dn_abs, -1.0f) : copysignf(dn_abs, 1.0f);
-    atomicOr(&L.msk[o >> 5], 1u << (o & 31));
-  }
+  // inactive: the reference compares against FAR (f32::MAX); +inf orders the same for dn_abs <= limit
+  if (dn_abs < fabsf(W[p])) W[p] = neg_sweep ? copysignf(dn_abs, -1.0f) : copysignf(dn_abs, 1.0f);
 }
 
-__device__ __forceinline__ void spawn(const SweepState& S, int x, int y, int z, int* dyn_next, int* dyn_next_n) {
+__device__ __forceinline__ int is_alive(const Sweep& S, int l) { return __ldcg(&S.alive[l]); }
+
+__device__ __forceinline__ int find_alive(const Sweep& S, int x, int y, int z) {
+  const int l = S.hash.find(x, y, z);
+  return (l >= 0 && is_alive(S, l)) ? l : -1;
+}
+
+// Queues leaf l for the next pass unless it is queued already.
+__device__ __forceinline__ void mark_dirty(const Sweep& S, int l, int* list, int* cnt) {
+  if (atomicExch(&S.dirty[l], 1) == 0) list[atomicAdd(cnt, 1)] = l;
+}
+
+// The leaf at (x, y, z) is asked for (fast_sweep.rs:185-287): create it, or
+// bring back one dropped earlier, and queue it.
+__device__ void request_leaf(const Sweep& S, int x, int y, int z, int* list, int* cnt) {
   bool ins;
   const int slot = S.hash.insert_key(x, y, z, ins);
   if (slot < 0) {
     atomicExch(S.overflow, 1);
     return;
   }
-  if (!ins) return;
-  const int idx = atomicAdd(S.n_leaves, 1);
-  if (uint64_t(idx) >= S.cap) {
-    atomicExch(S.overflow, 1);
-    return;
+  int idx;
+  if (ins) {
+    idx = atomicAdd(S.n_slots, 1);
+    if (uint64_t(idx) >= S.cap) {
+      atomicExch(S.overflow, 1);
+      return;
+    }
+    S.org[idx] = make_int4(x, y, z, 0);  // spare slots hold empty inputs, outputs and faces
+    __threadfence();
+    atomicExch(&S.hash.vals[slot], idx);
+  } else {
+    // the slot may be claimed by another warp right now: wait (bounded) for its index
+    idx = -1;
+    for (int it = 0; it < (1 << 20) && idx < 0; ++it) idx = atomicAdd(&S.hash.vals[slot], 0);
+    if (idx < 0) {
+      atomicExch(S.overflow, 1);
+      return;
+    }
   }
-  S.org[idx] = make_int4(x, y, z, 0);  // values, masks and frozen bits of spare leaves are zero
-  S.hash.vals[slot] = idx;
-  dyn_next[atomicAdd(dyn_next_n, 1)] = idx;
+  S.wanted[idx] = 1;
+  if (is_alive(S, idx)) return;
+  S.spawned[idx] = 1;
+  if (atomicExch(&S.alive[idx], 1) == 0) {
+    __threadfence();
+    atomicExch(S.changed, 1);
+    mark_dirty(S, idx, list, cnt);
+  }
 }
 
-// One launch per leaf plane: static leaves [plane_off[p], plane_off[p+1]) of
-// the sorted list plus the leaves spawned into this plane by the previous one.
-__global__ void __launch_bounds__(32 * SW_WARPS) k_sweep_plane(SweepState S, const int* __restrict__ sorted,
-                                                               const uint32_t* __restrict__ plane_off, int p, int n_planes,
-                                                               const int* __restrict__ dyn_cur, const int* __restrict__ dyn_cur_n,
-                                                               int* __restrict__ dyn_next, int* __restrict__ dyn_next_n,
-                                                               int sx, int sy, int sz, int neg_sweep_i, float limit_abs,
-                                                               float h) {
-  __shared__ WarpLeaf sm[SW_WARPS];
+// The spawn test of fast_sweep.rs:185-287 for one value of an after-face.
+__device__ __forceinline__ bool spawns(const Sweep& S, bool on, float v) {
+  return on && (bool(signbit(v)) == (S.neg != 0)) && (fabsf(v) < S.lim);
+}
+
+// Per block: for the k-th voxel in diagonal-plane order of this sweep
+// direction, its padded tile index (low 16 bits) and voxel index (high 16).
+__device__ __forceinline__ void fill_order(const Sweep& S, uint32_t* order) {
+  for (int k = threadIdx.x; k < 512; k += blockDim.x) {
+    const int u = c_plane_vox[k];
+    const int x = S.sx > 0 ? (u >> 6) : 7 - (u >> 6);
+    const int y = S.sy > 0 ? ((u >> 3) & 7) : 7 - ((u >> 3) & 7);
+    const int z = S.sz > 0 ? (u & 7) : 7 - (u & 7);
+    order[k] = uint32_t(pad_idx(x, y, z)) | (uint32_t((x << 6) | (y << 3) | z) << 16);
+  }
+}
+
+// One relaxation pass over the listed leaves.  Each is swept from its input
+// with its neighbours' current faces; an after-face that changed queues the
+// neighbour behind it, and a face that asks for a missing neighbour creates
+// it.  Repeated until nothing is queued, the outputs reach the unique fixed
+// point of the before/after dependency order — the result of the reference's
+// sequential sweep, whose queue pops every before-neighbour first.
+__global__ void __launch_bounds__(32 * SW_WARPS, 8) k_relax(Sweep S, const int* __restrict__ list, const int* __restrict__ n_list,
+                                                            int* __restrict__ next, int* __restrict__ n_next,
+                                                            int* __restrict__ n_clear) {
+  __shared__ float tile[SW_WARPS][PAD * PAD * PAD];
+  __shared__ uint32_t frz[SW_WARPS][16];
+  __shared__ uint32_t order[512];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *n_clear = 0;  // the counter the pass after next fills
+  fill_order(S, order);
+  __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  WarpLeaf& L = sm[w];
-  const uint32_t sb = p < n_planes ? plane_off[p] : 0u, se = p < n_planes ? plane_off[p + 1] : 0u;
-  const int n_static = int(se - sb), n_dyn = *dyn_cur_n;
-  const int total = n_static + n_dyn;
-  const bool neg_sweep = neg_sweep_i != 0;
-  const float lim = limit_abs;
+  float* W = tile[w];
+  uint32_t* F = frz[w];
+  const int sdir[3] = {S.sx, S.sy, S.sz};
+  const int total = *n_list;
   for (int item = blockIdx.x * SW_WARPS + w; item < total; item += gridDim.x * SW_WARPS) {
-    const int leaf = item < n_static ? sorted[sb + item] : dyn_cur[item - n_static];
-    const int4 org = S.org[leaf];
-    for (int k = lane; k < 512; k += 32) L.val[k] = S.val[uint64_t(leaf) * 512 + k];
-    if (lane < 16) {
-      L.msk[lane] = S.msk[uint64_t(leaf) * 16 + lane];
-      L.frz[lane] = S.frz[uint64_t(leaf) * 16 + lane];
+    const int leaf = list[item];
+    int live = 0;
+    if (lane == 0) {
+      atomicExch(&S.dirty[leaf], 0);
+      __threadfence();
+      live = is_alive(S, leaf);
     }
+    if (!__shfl_sync(0xffffffffu, live, 0)) continue;
+    const int4 org = S.org[leaf];
+    const float* iv = S.in_val + uint64_t(leaf) * 512;
+    const uint32_t* im = S.in_msk + uint64_t(leaf) * 16;
+    for (int k = lane; k < 512; k += 32) {
+      const uint32_t m = im[k >> 5];
+      const float v = iv[k];
+      W[pad_idx(k >> 6, (k >> 3) & 7, k & 7)] = ((m >> lane) & 1u) ? v : INFINITY;
+    }
+    if (lane < 16) F[lane] = S.frz[uint64_t(leaf) * 16 + lane];
+    int nb = -1;
     if (lane < 6) {
-      const int ax = lane >> 1, dir = (lane & 1) ? 8 : -8;
-      L.nb[lane] = S.hash.find(org.x + (ax == 0 ? dir : 0), org.y + (ax == 1 ? dir : 0), org.z + (ax == 2 ? dir : 0));
+      const int ax = lane >> 1, step = (lane & 1) ? 8 : -8;
+      nb = find_alive(S, org.x + (ax == 0 ? step : 0), org.y + (ax == 1 ? step : 0), org.z + (ax == 2 ? step : 0));
+    }
+    // halo: all twelve loads of this lane first, then the tile writes
+    float hv[12];
+    uint32_t hm[12];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const int n = __shfl_sync(0xffffffffu, nb, k);
+      const int ax = k >> 1, side = k & 1;
+      // the neighbour on the - side is before the leaf when the sweep goes +
+      const bool before = (side == 0) == (sdir[ax] > 0);
+      const float* fv = before ? S.pub_val : S.inf_val;
+      const uint32_t* fm = before ? S.pub_msk : S.inf_msk;
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        hv[2 * k + r] = INFINITY;
+        hm[2 * k + r] = 0u;
+        if (n >= 0) {
+          hv[2 * k + r] = __ldcg(&fv[(uint64_t(n) * 3 + ax) * 64 + lane + 32 * r]);
+          hm[2 * k + r] = __ldcg(&fm[(uint64_t(n) * 3 + ax) * 2 + r]);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const int ax = k >> 1, side = k & 1;
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        const int i = lane + 32 * r;
+        W[face_pad(ax, side ? 8 : -1, i)] = ((hm[2 * k + r] >> lane) & 1u) ? hv[2 * k + r] : INFINITY;
+      }
     }
     __syncwarp();
     for (int q = 0; q < 22; ++q) {
       const int beg = c_plane_off[q], end = c_plane_off[q + 1];
       for (int k = beg + lane; k < end; k += 32) {
-        const int u = c_plane_vox[k];
-        const int ux = u >> 6, uy = (u >> 3) & 7, uz = u & 7;
-        sweep_voxel(L, S, sx > 0 ? ux : 7 - ux, sy > 0 ? uy : 7 - uy, sz > 0 ? uz : 7 - uz, neg_sweep, lim, h);
+        const uint32_t e = order[k];
+        const int o = int(e >> 16);
+        if (!bit(F, o)) sweep_voxel(W, int(e & 0xffffu), S.neg != 0, S.lim, S.h);
       }
       __syncwarp();
     }
-    for (int k = lane; k < 512; k += 32) S.val[uint64_t(leaf) * 512 + k] = L.val[k];
-    if (lane < 16) S.msk[uint64_t(leaf) * 16 + lane] = L.msk[lane];
-    // fast_sweep.rs:185-287: spawn the next leaf along each axis whose
-    // "after" face holds a value of the sweep's sign below the limit
-    const int fx = sx > 0 ? 7 : 0, fy = sy > 0 ? 7 : 0, fz = sz > 0 ? 7 : 0;
-    bool hit[3];
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-      bool any = false;
-      for (int k = lane; k < 64; k += 32) {
-        const int a = k >> 3, b = k & 7;
-        const int o = ax == 0 ? ((fx << 6) | (a << 3) | b) : (ax == 1 ? ((a << 6) | (fy << 3) | b) : ((a << 6) | (b << 3) | fz));
-        const bool act = (L.msk[o >> 5] >> (o & 31)) & 1u;
-        const float v = L.val[o];
-        any |= act && (bool(signbit(v)) == neg_sweep) && (fabsf(v) < lim);
-      }
-      hit[ax] = __any_sync(0xffffffffu, any);
+    float* ov = S.out_val + uint64_t(leaf) * 512;
+    for (int k = lane; k < 512; k += 32) {
+      const float t = W[pad_idx(k >> 6, (k >> 3) & 7, k & 7)];
+      const bool on = t != INFINITY;
+      ov[k] = on ? t : iv[k];
+      const uint32_t mw = __ballot_sync(0xffffffffu, on);
+      if (lane == 0) S.out_msk[uint64_t(leaf) * 16 + (k >> 5)] = mw;
     }
-    if (lane == 0) {
-      if (hit[0]) spawn(S, org.x + 8 * sx, org.y, org.z, dyn_next, dyn_next_n);
-      if (hit[1]) spawn(S, org.x, org.y + 8 * sy, org.z, dyn_next, dyn_next_n);
-      if (hit[2]) spawn(S, org.x, org.y, org.z + 8 * sz, dyn_next, dyn_next_n);
+    for (int ax = 0; ax < 3; ++ax) {
+      const int fl = sdir[ax] > 0 ? 7 : 0;
+      const uint64_t fb = uint64_t(leaf) * 3 + ax;
+      bool diff = false, any = false;
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        const int i = lane + 32 * r;
+        const float t = W[face_pad(ax, fl, i)];
+        const bool on = t != INFINITY;
+        const float v = on ? t : 0.f;
+        any |= spawns(S, on, v);
+        const uint32_t mw = __ballot_sync(0xffffffffu, on);
+        const uint32_t old_m = __ldcg(&S.pub_msk[fb * 2 + r]);
+        const float old_v = __ldcg(&S.pub_val[fb * 64 + i]);
+        diff |= (mw != old_m) || (__float_as_uint(old_v) != __float_as_uint(v));
+        S.pub_val[fb * 64 + i] = v;
+        if (lane == 0) S.pub_msk[fb * 2 + r] = mw;
+      }
+      const bool changed = __any_sync(0xffffffffu, diff);
+      const bool spawn = __any_sync(0xffffffffu, any);
+      const int after = __shfl_sync(0xffffffffu, nb, 2 * ax + (sdir[ax] > 0 ? 1 : 0));
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) {
+        if (changed && after >= 0) mark_dirty(S, after, next, n_next);
+        if (spawn && after < 0)
+          request_leaf(S, org.x + (ax == 0 ? 8 * sdir[0] : 0), org.y + (ax == 1 ? 8 * sdir[1] : 0),
+                       org.z + (ax == 2 ? 8 * sdir[2] : 0), next, n_next);
+      }
     }
     __syncwarp();
   }
 }
 
-__global__ void k_plane_keys(const int4* __restrict__ org, const int* __restrict__ n_dev, int sx, int sy, int sz,
-                             int pmin, uint32_t* __restrict__ keys, int* __restrict__ idx, uint32_t* __restrict__ hist) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= *n_dev) return;
-  const int4 o = org[i];
-  const int p = sx * (o.x >> 3) + sy * (o.y >> 3) + sz * (o.z >> 3) - pmin;
-  keys[i] = uint32_t(p);
-  idx[i] = i;
-  atomicAdd(&hist[p], 1u);
+// Start of a sweep: out = in, after-faces published from the input, the
+// input's before-layers stored, every live leaf queued.
+__global__ void __launch_bounds__(128) k_sweep_init(Sweep S, int n, int* list, int* n_list) {
+  const int lane = threadIdx.x & 31;
+  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (l >= n) return;
+  const float* iv = S.in_val + uint64_t(l) * 512;
+  const uint32_t* im = S.in_msk + uint64_t(l) * 16;
+  for (int k = lane; k < 512; k += 32) S.out_val[uint64_t(l) * 512 + k] = iv[k];
+  if (lane < 16) S.out_msk[uint64_t(l) * 16 + lane] = im[lane];
+  const int sdir[3] = {S.sx, S.sy, S.sz};
+  for (int ax = 0; ax < 3; ++ax) {
+    for (int side = 0; side < 2; ++side) {
+      // side 0: the after-face (published output), side 1: the before-layer
+      const int fl = (sdir[ax] > 0) == (side == 0) ? 7 : 0;
+      float* fv = side == 0 ? S.pub_val : S.inf_val;
+      uint32_t* fm = side == 0 ? S.pub_msk : S.inf_msk;
+      for (int r = 0; r < 2; ++r) {
+        const int i = lane + 32 * r;
+        const int o = face_off(ax, fl, i);
+        const bool on = bit(im, o);
+        fv[(uint64_t(l) * 3 + ax) * 64 + i] = on ? iv[o] : 0.f;
+        const uint32_t mw = __ballot_sync(0xffffffffu, on);
+        if (lane == 0) fm[(uint64_t(l) * 3 + ax) * 2 + r] = mw;
+      }
+    }
+  }
+  if (lane == 0) {
+    S.spawned[l] = 0;
+    S.dirty[l] = 0;
+    if (S.alive[l]) {
+      S.dirty[l] = 1;
+      list[atomicAdd(n_list, 1)] = l;
+    }
+  }
 }
 
-__global__ void k_brick_bounds(const int4* __restrict__ org, const int* __restrict__ n_dev, int* __restrict__ bb) {
+// Check after the passes converged, step 1: forget who asked for whom.
+__global__ void k_spawn_clear(Sweep S, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= *n_dev) return;
-  const int4 o = org[i];
-  atomicMin(&bb[0], o.x >> 3); atomicMax(&bb[3], o.x >> 3);
-  atomicMin(&bb[1], o.y >> 3); atomicMax(&bb[4], o.y >> 3);
-  atomicMin(&bb[2], o.z >> 3); atomicMax(&bb[5], o.z >> 3);
+  if (i < n) S.wanted[i] = 0;
+}
+
+// Step 2: every live leaf asks for the leaves its final output calls for.
+__global__ void __launch_bounds__(128) k_spawn_mark(Sweep S, int n, int* list, int* n_list) {
+  const int lane = threadIdx.x & 31;
+  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (l >= n || !S.alive[l]) return;
+  const int sdir[3] = {S.sx, S.sy, S.sz};
+  const int4 org = S.org[l];
+  const float* ov = S.out_val + uint64_t(l) * 512;
+  const uint32_t* om = S.out_msk + uint64_t(l) * 16;
+  for (int ax = 0; ax < 3; ++ax) {
+    const int fl = sdir[ax] > 0 ? 7 : 0;
+    bool any = false;
+    for (int r = 0; r < 2; ++r) {
+      const int o = face_off(ax, fl, lane + 32 * r);
+      any |= spawns(S, bit(om, o), ov[o]);
+    }
+    if (__any_sync(0xffffffffu, any) && lane == 0)
+      request_leaf(S, org.x + (ax == 0 ? 8 * sdir[0] : 0), org.y + (ax == 1 ? 8 * sdir[1] : 0),
+                   org.z + (ax == 2 ? 8 * sdir[2] : 0), list, n_list);
+  }
+}
+
+// Step 3: a leaf created in this sweep that nobody asks for any more is
+// dropped (a request that an earlier, unconverged pass made); the leaves
+// behind its after-faces are queued again.
+__global__ void __launch_bounds__(128) k_spawn_drop(Sweep S, int n, int* list, int* n_list) {
+  const int lane = threadIdx.x & 31;
+  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (l >= n || !S.spawned[l] || !S.alive[l] || S.wanted[l]) return;
+  for (int k = lane; k < 512; k += 32) S.out_val[uint64_t(l) * 512 + k] = 0.f;
+  if (lane < 16) S.out_msk[uint64_t(l) * 16 + lane] = 0u;
+  for (int k = lane; k < 3 * 64; k += 32) S.pub_val[uint64_t(l) * 192 + k] = 0.f;
+  if (lane < 6) S.pub_msk[uint64_t(l) * 6 + lane] = 0u;
+  __threadfence();
+  __syncwarp();
+  if (lane == 0) {
+    atomicExch(&S.alive[l], 0);
+    atomicExch(S.changed, 1);
+    const int4 org = S.org[l];
+    const int sdir[3] = {S.sx, S.sy, S.sz};
+    for (int ax = 0; ax < 3; ++ax) {
+      const int a = find_alive(S, org.x + (ax == 0 ? 8 * sdir[0] : 0), org.y + (ax == 1 ? 8 * sdir[1] : 0),
+                               org.z + (ax == 2 ? 8 * sdir[2] : 0));
+      if (a >= 0) mark_dirty(S, a, list, n_list);
+    }
+  }
 }
 
 __global__ void k_sub_active(float* __restrict__ val, const uint32_t* __restrict__ msk, uint64_t n, float d) {
@@ -372,105 +543,119 @@ static uint64_t compact_nonempty(bs_ctx* ctx, bs_volume* v, float remove_above) 
 static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float limit) {
   cudaStream_t s = ctx->stream;
   const uint64_t n0 = v->n_leaves;
-  SweepState S;
   DBuf<int4> org(ctx, cap);
-  DBuf<float> val(ctx, cap * 512);
-  DBuf<uint32_t> msk(ctx, cap * 16), frz(ctx, cap * 16);
-  DBuf<int> n_dev(ctx, 1), overflow(ctx, 1);
-  BS_CUDA(cudaMemsetAsync(val.p, 0, cap * 512 * sizeof(float), s));
-  BS_CUDA(cudaMemsetAsync(msk.p, 0, cap * 16 * sizeof(uint32_t), s));
+  DBuf<float> val_a(ctx, cap * 512), val_b(ctx, cap * 512), pub_val(ctx, cap * 192), inf_val(ctx, cap * 192);
+  DBuf<uint32_t> msk_a(ctx, cap * 16), msk_b(ctx, cap * 16), frz(ctx, cap * 16), pub_msk(ctx, cap * 6),
+      inf_msk(ctx, cap * 6);
+  DBuf<int> flags(ctx, cap * 4), list_a(ctx, cap), list_b(ctx, cap), ctl(ctx, 8);
+  // every spare slot is an empty leaf: zero inputs, outputs, faces and flags
+  BS_CUDA(cudaMemsetAsync(val_a.p, 0, cap * 512 * sizeof(float), s));
+  BS_CUDA(cudaMemsetAsync(val_b.p, 0, cap * 512 * sizeof(float), s));
+  BS_CUDA(cudaMemsetAsync(msk_a.p, 0, cap * 16 * sizeof(uint32_t), s));
+  BS_CUDA(cudaMemsetAsync(msk_b.p, 0, cap * 16 * sizeof(uint32_t), s));
   BS_CUDA(cudaMemsetAsync(frz.p, 0, cap * 16 * sizeof(uint32_t), s));
-  if (n0) {
-    BS_CUDA(cudaMemcpyAsync(org.p, v->d_origins, n0 * sizeof(int4), cudaMemcpyDeviceToDevice, s));
-    BS_CUDA(cudaMemcpyAsync(val.p, v->d_values, n0 * 512 * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    BS_CUDA(cudaMemcpyAsync(msk.p, v->d_masks, n0 * 16 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
-    BS_CUDA(cudaMemcpyAsync(frz.p, v->d_masks, n0 * 16 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+  BS_CUDA(cudaMemsetAsync(pub_val.p, 0, cap * 192 * sizeof(float), s));
+  BS_CUDA(cudaMemsetAsync(pub_msk.p, 0, cap * 6 * sizeof(uint32_t), s));
+  BS_CUDA(cudaMemsetAsync(inf_val.p, 0, cap * 192 * sizeof(float), s));
+  BS_CUDA(cudaMemsetAsync(inf_msk.p, 0, cap * 6 * sizeof(uint32_t), s));
+  BS_CUDA(cudaMemsetAsync(flags.p, 0, cap * 4 * sizeof(int), s));
+  BS_CUDA(cudaMemsetAsync(ctl.p, 0, 8 * sizeof(int), s));
+  int* alive = flags.p;
+  BS_CUDA(cudaMemcpyAsync(org.p, v->d_origins, n0 * sizeof(int4), cudaMemcpyDeviceToDevice, s));
+  BS_CUDA(cudaMemcpyAsync(val_a.p, v->d_values, n0 * 512 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  BS_CUDA(cudaMemcpyAsync(msk_a.p, v->d_masks, n0 * 16 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+  BS_CUDA(cudaMemcpyAsync(frz.p, v->d_masks, n0 * 16 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+  {
+    std::vector<int> ones(n0, 1);
+    BS_CUDA(cudaMemcpyAsync(alive, ones.data(), n0 * sizeof(int), cudaMemcpyHostToDevice, s));
+    const int n0i = int(n0);
+    BS_CUDA(cudaMemcpyAsync(ctl.p + 3, &n0i, sizeof(int), cudaMemcpyHostToDevice, s));
+    BS_CUDA(cudaStreamSynchronize(s));  // `ones` leaves scope
   }
-  const int n0i = int(n0);
-  BS_CUDA(cudaMemcpyAsync(n_dev.p, &n0i, sizeof(int), cudaMemcpyHostToDevice, s));
-  BS_CUDA(cudaMemsetAsync(overflow.p, 0, sizeof(int), s));
   LeafHashBuf hb;
   hb.build(ctx, org.p, n0, cap);
+  // ctl: [0..2] rotating list counters, [3] used slots, [4] overflow, [5] changed
+  int* cnt = ctl.p;
+  Sweep S;
   S.org = org.p;
-  S.val = val.p;
-  S.msk = msk.p;
   S.frz = frz.p;
+  S.pub_val = pub_val.p;
+  S.pub_msk = pub_msk.p;
+  S.inf_val = inf_val.p;
+  S.inf_msk = inf_msk.p;
+  S.alive = alive;
+  S.spawned = flags.p + cap;
+  S.wanted = flags.p + 2 * cap;
+  S.dirty = flags.p + 3 * cap;
   S.hash = hb.h;
-  S.n_leaves = n_dev.p;
+  S.n_slots = ctl.p + 3;
   S.cap = cap;
-  S.overflow = overflow.p;
-  const bool neg_sweep = signbit(limit);
-  const float limit_abs = fabsf(limit);
-  DBuf<int> dyn_a(ctx, cap), dyn_b(ctx, cap), cnt_a(ctx, 1), cnt_b(ctx, 1);
-  DBuf<uint32_t> keys(ctx, cap), keys2(ctx, cap);
-  DBuf<int> idx(ctx, cap), sorted(ctx, cap);
-  DBuf<int> bb(ctx, 6);
+  S.overflow = ctl.p + 4;
+  S.changed = ctl.p + 5;
+  S.neg = signbit(limit) ? 1 : 0;
+  S.lim = fabsf(limit);
+  S.h = h;
+  int* lists[2] = {list_a.p, list_b.p};
+  float* vals[2] = {val_a.p, val_b.p};
+  uint32_t* msks[2] = {msk_a.p, msk_b.p};
+  int cur = 0;
+  uint64_t total_passes = 0, total_sweeps = 0;
   static const int DIRS[8][3] = {{1, 1, 1},  {-1, 1, 1},  {1, -1, 1},  {-1, -1, 1},
                                  {1, 1, -1}, {-1, 1, -1}, {1, -1, -1}, {-1, -1, -1}};
-  // spawn chains reach at most the limit from the last existing plane
-  const int extra_planes = int(std::ceil(limit_abs * 1.7320508f / (8.0f * h))) + 3;
   for (int d = 0; d < 8; ++d) {
-    const int sx = DIRS[d][0], sy = DIRS[d][1], sz = DIRS[d][2];
+    S.sx = DIRS[d][0];
+    S.sy = DIRS[d][1];
+    S.sz = DIRS[d][2];
+    S.in_val = vals[cur];
+    S.in_msk = msks[cur];
+    S.out_val = vals[cur ^ 1];
+    S.out_msk = msks[cur ^ 1];
     int n = 0;
-    read_back(ctx, &n, n_dev.p, sizeof(int));
-    if (n == 0) break;
-    int init_bb[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, -0x7fffffff, -0x7fffffff, -0x7fffffff};
-    BS_CUDA(cudaMemcpyAsync(bb.p, init_bb, sizeof init_bb, cudaMemcpyHostToDevice, s));
-    BS_KERNEL(ctx, "k_brick_bounds", (k_brick_bounds<<<nb_(n, 256), 256, 0, s>>>(org.p, n_dev.p, bb.p)));
-    int hbb[6];
-    read_back(ctx, hbb, bb.p, sizeof hbb);
-    const int pmin = (sx > 0 ? hbb[0] : -hbb[3]) + (sy > 0 ? hbb[1] : -hbb[4]) + (sz > 0 ? hbb[2] : -hbb[5]);
-    const int pmax = (sx > 0 ? hbb[3] : -hbb[0]) + (sy > 0 ? hbb[4] : -hbb[1]) + (sz > 0 ? hbb[5] : -hbb[2]);
-    const int P = pmax - pmin + 1;
-    DBuf<uint32_t> hist(ctx, uint64_t(P) + 1), off(ctx, uint64_t(P) + 1);
-    BS_CUDA(cudaMemsetAsync(hist.p, 0, (uint64_t(P) + 1) * sizeof(uint32_t), s));
-    BS_KERNEL(ctx, "k_plane_keys", (k_plane_keys<<<nb_(n, 256), 256, 0, s>>>(org.p, n_dev.p, sx, sy, sz, pmin, keys.p, idx.p, hist.p)));
-    {
-      size_t tmp = 0;
-      int bits = 1;
-      while ((1 << bits) < P + 1 && bits < 31) ++bits;
-      BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, keys.p, keys2.p, idx.p, sorted.p, n, 0, bits, s));
-      DBuf<uint8_t> t(ctx, tmp);
-      BS_CUDA(cub::DeviceRadixSort::SortPairs(t.p, tmp, keys.p, keys2.p, idx.p, sorted.p, n, 0, bits, s));
+    BS_CUDA(cudaMemsetAsync(cnt, 0, 3 * sizeof(int), s));
+    read_back(ctx, &n, S.n_slots, sizeof(int));
+    BS_KERNEL(ctx, "k_sweep_init", (k_sweep_init<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, lists[0], cnt)));
+    int pass = 0;
+    for (;;) {
+      for (;;) {
+        int queued = 0;
+        read_back(ctx, &queued, cnt + pass % 3, sizeof(int));
+        if (queued == 0) break;
+        if (pass >= (1 << 16)) fail(BS_ERR_TIMEOUT, "offset: sweep relaxation did not converge");
+        total_sweeps += uint64_t(queued);
+        const unsigned grid = nb_(uint64_t(queued), SW_WARPS);
+        BS_KERNEL(ctx, "k_relax", (k_relax<<<grid, 32 * SW_WARPS, 0, s>>>(S, lists[pass & 1], cnt + pass % 3, lists[(pass + 1) & 1],
+                                                                           cnt + (pass + 1) % 3, cnt + (pass + 2) % 3)));
+        ++pass;
+      }
+      // the passes converged: check that the set of spawned leaves is the one
+      // the final outputs ask for
+      read_back(ctx, &n, S.n_slots, sizeof(int));
+      if (uint64_t(n) > cap) return false;
+      BS_CUDA(cudaMemsetAsync(S.changed, 0, sizeof(int), s));
+      BS_KERNEL(ctx, "k_spawn_clear", (k_spawn_clear<<<nb_(uint64_t(n), 256), 256, 0, s>>>(S, n)));
+      BS_KERNEL(ctx, "k_spawn_mark", (k_spawn_mark<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, lists[pass & 1], cnt + pass % 3)));
+      BS_KERNEL(ctx, "k_spawn_drop", (k_spawn_drop<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, lists[pass & 1], cnt + pass % 3)));
+      int ch = 0;
+      read_back(ctx, &ch, S.changed, sizeof(int));
+      if (!ch) break;
     }
-    scan_ex(ctx, hist.p, off.p, uint64_t(P) + 1);
-    BS_CUDA(cudaMemsetAsync(cnt_a.p, 0, sizeof(int), s));
-    BS_CUDA(cudaMemsetAsync(cnt_b.p, 0, sizeof(int), s));
-    int *dc = dyn_a.p, *dn = dyn_b.p, *cc = cnt_a.p, *cn = cnt_b.p;
-    const unsigned grid = unsigned(std::max<uint64_t>(64, std::min<uint64_t>(4096, (uint64_t(n) / std::max(P, 1)) / SW_WARPS + 64)));
-    for (int p = 0; p < P + extra_planes; ++p) {
-      BS_KERNEL(ctx, "k_sweep_plane", (k_sweep_plane<<<grid, 32 * SW_WARPS, 0, s>>>(S, sorted.p, off.p, p, P, dc, cc, dn, cn, sx, sy, sz,
-                                                                       neg_sweep ? 1 : 0, limit_abs, h)));
-      BS_CUDA(cudaMemsetAsync(cc, 0, sizeof(int), s));
-      std::swap(dc, dn);
-      std::swap(cc, cn);
-    }
-    // any spawns left past the last planned plane: keep sweeping until none
-    for (int p = P + extra_planes, guard = 0; guard < 1 << 16; ++p, ++guard) {
-      int left = 0;
-      read_back(ctx, &left, cc, sizeof(int));
-      if (left == 0) break;
-      BS_KERNEL(ctx, "k_sweep_plane", (k_sweep_plane<<<grid, 32 * SW_WARPS, 0, s>>>(S, sorted.p, off.p, p, P, dc, cc, dn, cn, sx, sy, sz,
-                                                                       neg_sweep ? 1 : 0, limit_abs, h)));
-      BS_CUDA(cudaMemsetAsync(cc, 0, sizeof(int), s));
-      std::swap(dc, dn);
-      std::swap(cc, cn);
-    }
+    total_passes += uint64_t(pass);
     int of = 0;
-    read_back(ctx, &of, overflow.p, sizeof(int));
+    read_back(ctx, &of, S.overflow, sizeof(int));
     if (of) return false;
+    cur ^= 1;
   }
-  int n = 0, of = 0;
-  read_back(ctx, &n, n_dev.p, sizeof(int));
-  read_back(ctx, &of, overflow.p, sizeof(int));
-  if (of) return false;
-  // adopt the swept arrays
+  int n = 0;
+  read_back(ctx, &n, S.n_slots, sizeof(int));
+  ctx->last_stats[6] = total_passes;
+  ctx->last_stats[7] = total_sweeps;
+  // adopt the swept arrays (dead and empty slots go with the next compaction)
   dfree(ctx, v->d_origins);
   dfree(ctx, v->d_values);
   dfree(ctx, v->d_masks);
   v->d_origins = org.release();
-  v->d_values = val.release();
-  v->d_masks = msk.release();
+  v->d_values = cur == 0 ? val_a.release() : val_b.release();
+  v->d_masks = cur == 0 ? msk_a.release() : msk_b.release();
   v->n_leaves = uint64_t(n);
   return true;
 }

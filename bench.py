@@ -38,7 +38,7 @@ import numpy as np  # noqa: E402
 
 H = 0.002
 BAND = 3
-# Algorithmic work per unit.
+# Algorithmic work per unit, counted from the reference's operations.
 FLOP_PER_PAIR = 84          # closest point + norm, triangle3.rs:317-382 (face-region path)
 WN_FLOP_FAR = 31            # far test + order-1/2 terms, aabb_tree.rs:662-671, 803-816
 WN_FLOP_EXACT = 70          # Van Oosterom-Strackee solid angle, aabb_tree.rs:582-615 (atan2 as 20)
@@ -46,7 +46,7 @@ WN_FAR_PER_VOXEL = 110.1    # the oracle's traversal of the reference's SAH tree
 WN_EXACT_PER_VOXEL = 14.4   # torus (1/8 ring sample, 4.5 M band voxels): counts per band voxel
 WN_FLOP_PER_VOXEL = int(round(WN_FAR_PER_VOXEL * WN_FLOP_FAR + WN_EXACT_PER_VOXEL * WN_FLOP_EXACT))
 # dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture of
-# the half-ring case, scaled to a full torus by the units processed (profiles/)
+# the half-ring case, scaled to a full torus by the units processed
 TRAFFIC_PER_LAUNCH = {}
 METRIC = "band voxels/s mesh→SDF+sign: learned/batched vs plain GPU, 0 sign flips"
 UNIT = "band_voxels/s"
@@ -381,6 +381,9 @@ def pipeline_secondary(ctx, params, dev, L, N, bs, C):
         for sign, dist in (("plus", 0.01), ("minus", -0.01)):
             cc = c.clone()
             _, t_off = timed(lambda: cc.offset(dist))
+            st = ctx.last_stats()
+            d["offset_%s_relax_passes" % sign] = st["offset_passes"]
+            d["offset_%s_leaf_sweeps" % sign] = st["offset_leaf_sweeps"]
             mesher = bs.DualContouringMesher().with_voxel_size(H)
             n = C.c_uint64()
             _, t_dc = timed(lambda: N.check(L.bs_dual_contour(ctx.h, cc.h, H, None, 0, C.byref(n)), ctx.h))

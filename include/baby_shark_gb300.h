@@ -78,7 +78,8 @@ bs_status bs_ctx_stage_reset(bs_ctx* ctx);
  * [4] leaves, [5] active voxels, [6] warp-level node visits of the
  * winding-number pass, [7] warp-level far-field evaluations (low 32 bits) and
  * exact solid angles (high 32 bits).  A dual contouring call overwrites
- * [6] and [7] with its crossing and cell counts. */
+ * [6] and [7] with its crossing and cell counts, an offset call with its
+ * relaxation passes and leaf sweeps over the 8 sweep directions. */
 bs_status bs_ctx_last_stats(const bs_ctx* ctx, uint64_t* out8);
 /* Measured FP32 FMA throughput of the context's device in TFLOP/s (a timed
  * FFMA loop over all SMs); the denominator of FP32-bound roofline fractions. */
