@@ -69,24 +69,25 @@ void LeafHashBuf::build(bs_ctx* ctx, const int4* origins, uint64_t n, uint64_t m
 }
 
 // -------------------------------------------------------------- remove_if ---
-// tree_node.rs remove_if(|v| v.abs() > 2h): clears the active bits, counts what remains.
+// tree_node.rs remove_if(|v| v.abs() > 2h): clears the active bits, counts
+// what remains.  One warp per leaf, coalesced: mask word j covers voxels
+// 32j .. 32j + 31, one per lane.
 __global__ void k_remove_far(const float* __restrict__ values, uint32_t* __restrict__ masks, uint64_t n, float lim,
                              uint32_t* __restrict__ keep) {
   const uint64_t b = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (b >= n) return;
-  uint32_t m = 0;
-  if (lane < 16) {
-    m = masks[b * 16 + lane];
-    uint32_t mm = m;
-    while (mm) {
-      const int bit = __ffs(mm) - 1;
-      mm &= mm - 1;
-      if (fabsf(values[b * 512 + lane * 32 + bit]) > lim) m &= ~(1u << bit);
-    }
-    masks[b * 16 + lane] = m;
+  const uint32_t mine = lane < 16 ? masks[b * 16 + lane] : 0u;
+  uint32_t kept = 0, any = 0;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const uint32_t m = __shfl_sync(0xffffffffu, mine, j);
+    const bool on = ((m >> lane) & 1u) && !(fabsf(values[b * 512 + j * 32 + lane]) > lim);
+    const uint32_t word = __ballot_sync(0xffffffffu, on);
+    if (lane == j) kept = word;
+    any |= word;
   }
-  const uint32_t any = __ballot_sync(0xffffffffu, m != 0);
+  if (lane < 16 && kept != mine) masks[b * 16 + lane] = kept;
   if (lane == 0) keep[b] = any ? 1u : 0u;
   if (b == n - 1 && lane == 0) keep[n] = 0u;
 }
@@ -97,7 +98,8 @@ __global__ void k_gather_leaves(const uint32_t* __restrict__ keep, const uint32_
   const uint64_t b = blockIdx.x;
   if (b >= n || !keep[b]) return;
   const uint64_t d = pos[b];
-  for (int t = threadIdx.x; t < 512; t += blockDim.x) vo[d * 512 + t] = vi[b * 512 + t];
+  for (int t = threadIdx.x; t < 128; t += blockDim.x)
+    reinterpret_cast<float4*>(vo + d * 512)[t] = reinterpret_cast<const float4*>(vi + b * 512)[t];
   if (threadIdx.x < 16) mo[d * 16 + threadIdx.x] = mi[b * 16 + threadIdx.x];
   if (threadIdx.x == 0) oo[d] = oi[b];
 }
@@ -149,6 +151,8 @@ struct Sweep {
   int* spawned;         // the leaf was created during this sweep
   int* wanted;          // a before-neighbour's output asks for it
   int* dirty;           // queued for a sweep
+  int* nbr;             // [slot][6] slot of the face neighbour (-x, +x, -y, +y, -z, +z) or -1
+  int* linked;          // nbr of the slot is filled in
   LeafHash hash;
   int* n_slots;
   uint64_t cap;
@@ -207,8 +211,21 @@ __device__ __forceinline__ void mark_dirty(const Sweep& S, int l, int* list, int
   if (atomicExch(&S.dirty[l], 1) == 0) list[atomicAdd(cnt, 1)] = l;
 }
 
+// Brings back a leaf dropped earlier in the offset and queues it.
+__device__ __forceinline__ void revive_leaf(const Sweep& S, int idx, int* list, int* cnt) {
+  S.wanted[idx] = 1;
+  if (is_alive(S, idx)) return;
+  S.spawned[idx] = 1;
+  if (atomicExch(&S.alive[idx], 1) == 0) {
+    __threadfence();
+    atomicExch(S.changed, 1);
+    mark_dirty(S, idx, list, cnt);
+  }
+}
+
 // The leaf at (x, y, z) is asked for (fast_sweep.rs:185-287): create it, or
-// bring back one dropped earlier, and queue it.
+// bring back one dropped earlier, and queue it.  A created slot fills in its
+// neighbour cache on its first sweep.
 __device__ void request_leaf(const Sweep& S, int x, int y, int z, int* list, int* cnt) {
   bool ins;
   const int slot = S.hash.insert_key(x, y, z, ins);
@@ -235,14 +252,7 @@ __device__ void request_leaf(const Sweep& S, int x, int y, int z, int* list, int
       return;
     }
   }
-  S.wanted[idx] = 1;
-  if (is_alive(S, idx)) return;
-  S.spawned[idx] = 1;
-  if (atomicExch(&S.alive[idx], 1) == 0) {
-    __threadfence();
-    atomicExch(S.changed, 1);
-    mark_dirty(S, idx, list, cnt);
-  }
+  revive_leaf(S, idx, list, cnt);
 }
 
 // The spawn test of fast_sweep.rs:185-287 for one value of an after-face.
@@ -268,10 +278,18 @@ __device__ __forceinline__ void fill_order(const Sweep& S, uint32_t* order) {
 // it.  Repeated until nothing is queued, the outputs reach the unique fixed
 // point of the before/after dependency order — the result of the reference's
 // sequential sweep, whose queue pops every before-neighbour first.
+//
+// Neighbours come from the slot's cached `nbr`.  A dropped neighbour reads as
+// empty (its faces are zero).  A neighbour created after the cache was filled
+// is missing from it until that neighbour's first sweep links both ways; it
+// only matters as the target of a changed after-face, which falls back to the
+// hash.
 __global__ void __launch_bounds__(32 * SW_WARPS, 8) k_relax(Sweep S, const int* __restrict__ list, const int* __restrict__ n_list,
                                                             int* __restrict__ next, int* __restrict__ n_next,
                                                             int* __restrict__ n_clear) {
   __shared__ float tile[SW_WARPS][PAD * PAD * PAD];
+  __shared__ float oldf[SW_WARPS][3 * 64];
+  __shared__ uint32_t oldm[SW_WARPS][6];
   __shared__ uint32_t frz[SW_WARPS][16];
   __shared__ uint32_t order[512];
   if (blockIdx.x == 0 && threadIdx.x == 0) *n_clear = 0;  // the counter the pass after next fills
@@ -292,6 +310,17 @@ __global__ void __launch_bounds__(32 * SW_WARPS, 8) k_relax(Sweep S, const int* 
     }
     if (!__shfl_sync(0xffffffffu, live, 0)) continue;
     const int4 org = S.org[leaf];
+    int nb = -1;
+    if (lane < 6) {
+      if (__ldcg(&S.linked[leaf])) {
+        nb = __ldcg(&S.nbr[uint64_t(leaf) * 6 + lane]);
+      } else {  // first sweep of a created slot: link both ways
+        const int ax = lane >> 1, step = (lane & 1) ? 8 : -8;
+        nb = S.hash.find(org.x + (ax == 0 ? step : 0), org.y + (ax == 1 ? step : 0), org.z + (ax == 2 ? step : 0));
+        S.nbr[uint64_t(leaf) * 6 + lane] = nb;
+        if (nb >= 0) S.nbr[uint64_t(nb) * 6 + (lane ^ 1)] = leaf;
+      }
+    }
     const float* iv = S.in_val + uint64_t(leaf) * 512;
     const uint32_t* im = S.in_msk + uint64_t(leaf) * 16;
     for (int k = lane; k < 512; k += 32) {
@@ -300,11 +329,9 @@ __global__ void __launch_bounds__(32 * SW_WARPS, 8) k_relax(Sweep S, const int* 
       W[pad_idx(k >> 6, (k >> 3) & 7, k & 7)] = ((m >> lane) & 1u) ? v : INFINITY;
     }
     if (lane < 16) F[lane] = S.frz[uint64_t(leaf) * 16 + lane];
-    int nb = -1;
-    if (lane < 6) {
-      const int ax = lane >> 1, step = (lane & 1) ? 8 : -8;
-      nb = find_alive(S, org.x + (ax == 0 ? step : 0), org.y + (ax == 1 ? step : 0), org.z + (ax == 2 ? step : 0));
-    }
+    // this leaf's faces as published before: only this warp writes them in this pass
+    for (int k = lane; k < 3 * 64; k += 32) oldf[w][k] = __ldcg(&S.pub_val[uint64_t(leaf) * 192 + k]);
+    if (lane < 6) oldm[w][lane] = __ldcg(&S.pub_msk[uint64_t(leaf) * 6 + lane]);
     // halo: all twelve loads of this lane first, then the tile writes
     float hv[12];
     uint32_t hm[12];
@@ -353,6 +380,8 @@ __global__ void __launch_bounds__(32 * SW_WARPS, 8) k_relax(Sweep S, const int* 
       const uint32_t mw = __ballot_sync(0xffffffffu, on);
       if (lane == 0) S.out_msk[uint64_t(leaf) * 16 + (k >> 5)] = mw;
     }
+    uint32_t flags = 0;  // bit ax: face changed, bit 3 + ax: face asks for the next leaf
+#pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
       const int fl = sdir[ax] > 0 ? 7 : 0;
       const uint64_t fb = uint64_t(leaf) * 3 + ax;
@@ -365,26 +394,47 @@ __global__ void __launch_bounds__(32 * SW_WARPS, 8) k_relax(Sweep S, const int* 
         const float v = on ? t : 0.f;
         any |= spawns(S, on, v);
         const uint32_t mw = __ballot_sync(0xffffffffu, on);
-        const uint32_t old_m = __ldcg(&S.pub_msk[fb * 2 + r]);
-        const float old_v = __ldcg(&S.pub_val[fb * 64 + i]);
-        diff |= (mw != old_m) || (__float_as_uint(old_v) != __float_as_uint(v));
+        diff |= (mw != oldm[w][2 * ax + r]) || (__float_as_uint(oldf[w][ax * 64 + i]) != __float_as_uint(v));
         S.pub_val[fb * 64 + i] = v;
         if (lane == 0) S.pub_msk[fb * 2 + r] = mw;
       }
-      const bool changed = __any_sync(0xffffffffu, diff);
-      const bool spawn = __any_sync(0xffffffffu, any);
-      const int after = __shfl_sync(0xffffffffu, nb, 2 * ax + (sdir[ax] > 0 ? 1 : 0));
-      __threadfence();
-      __syncwarp();
-      if (lane == 0) {
-        if (changed && after >= 0) mark_dirty(S, after, next, n_next);
-        if (spawn && after < 0)
-          request_leaf(S, org.x + (ax == 0 ? 8 * sdir[0] : 0), org.y + (ax == 1 ? 8 * sdir[1] : 0),
-                       org.z + (ax == 2 ? 8 * sdir[2] : 0), next, n_next);
+      if (__any_sync(0xffffffffu, diff)) flags |= 1u << ax;
+      if (__any_sync(0xffffffffu, any)) flags |= 8u << ax;
+    }
+    int after3[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) after3[ax] = __shfl_sync(0xffffffffu, nb, 2 * ax + (sdir[ax] > 0 ? 1 : 0));
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) {
+      S.linked[leaf] = 1;
+      for (int ax = 0; ax < 3; ++ax) {
+        const bool chg = (flags >> ax) & 1u, spw = (flags >> (3 + ax)) & 1u;
+        if (!chg && !spw) continue;
+        const int x = org.x + (ax == 0 ? 8 * sdir[0] : 0), y = org.y + (ax == 1 ? 8 * sdir[1] : 0),
+                  z = org.z + (ax == 2 ? 8 * sdir[2] : 0);
+        int after = after3[ax];
+        if (after < 0) after = S.hash.find(x, y, z);  // created after the cache was filled
+        if (chg && after >= 0) mark_dirty(S, after, next, n_next);
+        if (spw) {
+          if (after < 0) request_leaf(S, x, y, z, next, n_next);
+          else revive_leaf(S, after, next, n_next);
+        }
       }
     }
     __syncwarp();
   }
+}
+
+// Neighbour cache of the leaves present when the offset starts.
+__global__ void k_link(Sweep S, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * 6) return;
+  const int l = i / 6, k = i - 6 * l;
+  const int4 o = S.org[l];
+  const int ax = k >> 1, step = (k & 1) ? 8 : -8;
+  S.nbr[i] = S.hash.find(o.x + (ax == 0 ? step : 0), o.y + (ax == 1 ? step : 0), o.z + (ax == 2 ? step : 0));
+  if (k == 0) S.linked[l] = 1;
 }
 
 // Start of a sweep: out = in, after-faces published from the input, the
@@ -501,7 +551,8 @@ __global__ void k_permute_leaves(const uint32_t* __restrict__ perm, uint64_t n, 
   const uint64_t d = blockIdx.x;
   if (d >= n) return;
   const uint64_t s = perm[d];
-  for (int t = threadIdx.x; t < 512; t += blockDim.x) vo[d * 512 + t] = vi[s * 512 + t];
+  for (int t = threadIdx.x; t < 128; t += blockDim.x)
+    reinterpret_cast<float4*>(vo + d * 512)[t] = reinterpret_cast<const float4*>(vi + s * 512)[t];
   if (threadIdx.x < 16) mo[d * 16 + threadIdx.x] = mi[s * 16 + threadIdx.x];
   if (threadIdx.x == 0) oo[d] = oi[s];
 }
@@ -547,7 +598,7 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   DBuf<float> val_a(ctx, cap * 512), val_b(ctx, cap * 512), pub_val(ctx, cap * 192), inf_val(ctx, cap * 192);
   DBuf<uint32_t> msk_a(ctx, cap * 16), msk_b(ctx, cap * 16), frz(ctx, cap * 16), pub_msk(ctx, cap * 6),
       inf_msk(ctx, cap * 6);
-  DBuf<int> flags(ctx, cap * 4), list_a(ctx, cap), list_b(ctx, cap), ctl(ctx, 8);
+  DBuf<int> flags(ctx, cap * 5), list_a(ctx, cap), list_b(ctx, cap), ctl(ctx, 8), nbr(ctx, cap * 6);
   // every spare slot is an empty leaf: zero inputs, outputs, faces and flags
   BS_CUDA(cudaMemsetAsync(val_a.p, 0, cap * 512 * sizeof(float), s));
   BS_CUDA(cudaMemsetAsync(val_b.p, 0, cap * 512 * sizeof(float), s));
@@ -558,7 +609,7 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   BS_CUDA(cudaMemsetAsync(pub_msk.p, 0, cap * 6 * sizeof(uint32_t), s));
   BS_CUDA(cudaMemsetAsync(inf_val.p, 0, cap * 192 * sizeof(float), s));
   BS_CUDA(cudaMemsetAsync(inf_msk.p, 0, cap * 6 * sizeof(uint32_t), s));
-  BS_CUDA(cudaMemsetAsync(flags.p, 0, cap * 4 * sizeof(int), s));
+  BS_CUDA(cudaMemsetAsync(flags.p, 0, cap * 5 * sizeof(int), s));
   BS_CUDA(cudaMemsetAsync(ctl.p, 0, 8 * sizeof(int), s));
   int* alive = flags.p;
   BS_CUDA(cudaMemcpyAsync(org.p, v->d_origins, n0 * sizeof(int4), cudaMemcpyDeviceToDevice, s));
@@ -587,6 +638,8 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   S.spawned = flags.p + cap;
   S.wanted = flags.p + 2 * cap;
   S.dirty = flags.p + 3 * cap;
+  S.linked = flags.p + 4 * cap;
+  S.nbr = nbr.p;
   S.hash = hb.h;
   S.n_slots = ctl.p + 3;
   S.cap = cap;
@@ -595,6 +648,7 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   S.neg = signbit(limit) ? 1 : 0;
   S.lim = fabsf(limit);
   S.h = h;
+  BS_KERNEL(ctx, "k_link", (k_link<<<nb_(n0 * 6, 256), 256, 0, s>>>(S, int(n0))));
   int* lists[2] = {list_a.p, list_b.p};
   float* vals[2] = {val_a.p, val_b.p};
   uint32_t* msks[2] = {msk_a.p, msk_b.p};

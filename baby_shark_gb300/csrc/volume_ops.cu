@@ -173,46 +173,60 @@ namespace bs {
 __device__ __forceinline__ bool mask_on(const uint32_t* m, int i) { return (m[i >> 5] >> (i & 31)) & 1u; }
 __device__ __forceinline__ float signed_far(bool neg) { return neg ? -FAR_F : FAR_F; }
 
-// leaf_node/flood_fill.rs:12-50.  One warp per leaf; lane l scans the z-lines
-// (x, y) = (l >> 3, l & 7) and (4 + (l >> 3), l & 7).
-__global__ void k_ff_leaf(float* __restrict__ values, const uint32_t* __restrict__ masks, uint64_t n,
-                          uint8_t* __restrict__ first_neg, uint8_t* __restrict__ last_neg) {
-  const uint64_t b = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+// leaf_node/flood_fill.rs:12-50.  One warp per leaf: the leaf is staged in
+// shared memory with coalesced float4 loads, lane l scans the z-lines
+// (x, y) = (l >> 3, l & 7) and (4 + (l >> 3), l & 7), and the leaf is written
+// back whole.  Full and empty leaves are left as they are.
+constexpr int FF_WARPS = 8;
+__global__ void __launch_bounds__(32 * FF_WARPS) k_ff_leaf(float* __restrict__ values, const uint32_t* __restrict__ masks,
+                                                           uint64_t n, uint8_t* __restrict__ first_neg,
+                                                           uint8_t* __restrict__ last_neg) {
+  __shared__ float4 sv4[FF_WARPS][128];
+  __shared__ uint32_t smk[FF_WARPS][16];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint64_t b = blockIdx.x * uint64_t(FF_WARPS) + w;
   if (b >= n) return;
-  const uint32_t* m = masks + b * 16;
-  float* v = values + b * 512;
-  uint32_t full = 0xffffffffu, any = 0;
-  int first = -1;
-#pragma unroll
-  for (int w = 0; w < 16; ++w) {
-    uint32_t mw = m[w];
-    full &= mw;
-    any |= mw;
-    if (first < 0 && mw) first = w * 32 + __ffs(mw) - 1;
+  float* V = reinterpret_cast<float*>(sv4[w]);
+  uint32_t* M = smk[w];
+  const uint32_t mw = lane < 16 ? masks[b * 16 + lane] : 0u;
+  if (lane < 16) M[lane] = mw;
+  const bool full = __all_sync(0xffffffffu, lane >= 16 || mw == 0xffffffffu);
+  const uint32_t nonzero = __ballot_sync(0xffffffffu, mw != 0u);
+  float4* g4 = reinterpret_cast<float4*>(values + b * 512);
+  if (full || nonzero == 0u) {
+    if (lane == 0) {
+      first_neg[b] = signbit(values[b * 512]) ? 1 : 0;
+      last_neg[b] = signbit(values[b * 512 + 511]) ? 1 : 0;
+    }
+    return;
   }
-  if (full != 0xffffffffu && any) {
-    const bool s0 = signbit(v[first]);
-    for (int line = lane; line < 64; line += 32) {
-      const int x = line >> 3, y = line & 7;
-      bool c = s0;
-      for (int xx = 0; xx <= x; ++xx)
-        if (mask_on(m, xx << 6)) c = signbit(v[xx << 6]);
-      for (int yy = 0; yy <= y; ++yy)
-        if (mask_on(m, (x << 6) | (yy << 3))) c = signbit(v[(x << 6) | (yy << 3)]);
-      for (int z = 0; z < 8; ++z) {
-        const int o = (x << 6) | (y << 3) | z;
-        if (mask_on(m, o))
-          c = signbit(v[o]);
-        else
-          v[o] = signed_far(c);
-      }
+  const int fw = __ffs(nonzero) - 1;
+  const int first = fw * 32 + __ffs(__shfl_sync(0xffffffffu, mw, fw)) - 1;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) sv4[w][lane + 32 * j] = g4[lane + 32 * j];
+  __syncwarp();
+  const bool s0 = signbit(V[first]);
+  for (int line = lane; line < 64; line += 32) {
+    const int x = line >> 3, y = line & 7;
+    bool c = s0;
+    for (int xx = 0; xx <= x; ++xx)
+      if (mask_on(M, xx << 6)) c = signbit(V[xx << 6]);
+    for (int yy = 0; yy <= y; ++yy)
+      if (mask_on(M, (x << 6) | (yy << 3))) c = signbit(V[(x << 6) | (yy << 3)]);
+    for (int z = 0; z < 8; ++z) {
+      const int o = (x << 6) | (y << 3) | z;
+      if (mask_on(M, o))
+        c = signbit(V[o]);
+      else
+        V[o] = signed_far(c);
     }
   }
   __syncwarp();
+#pragma unroll
+  for (int j = 0; j < 4; ++j) g4[lane + 32 * j] = sv4[w][lane + 32 * j];
   if (lane == 0) {
-    first_neg[b] = signbit(v[0]) ? 1 : 0;
-    last_neg[b] = signbit(v[511]) ? 1 : 0;
+    first_neg[b] = signbit(V[0]) ? 1 : 0;
+    last_neg[b] = signbit(V[511]) ? 1 : 0;
   }
 }
 
@@ -331,7 +345,7 @@ void flood_fill(bs_ctx* ctx, bs_volume* v) {
   cudaStream_t s = ctx->stream;
   DBuf<uint8_t> lf(ctx, v->n_leaves), ll(ctx, v->n_leaves);
   if (v->n_leaves)
-    BS_KERNEL(ctx, "k_ff_leaf", (k_ff_leaf<<<nblk(v->n_leaves * 32, 256), 256, 0, s>>>(v->d_values, v->d_masks, v->n_leaves, lf.p, ll.p)));
+    BS_KERNEL(ctx, "k_ff_leaf", (k_ff_leaf<<<nblk(v->n_leaves, FF_WARPS), 32 * FF_WARPS, 0, s>>>(v->d_values, v->d_masks, v->n_leaves, lf.p, ll.p)));
   if (u->l1.n)
     BS_KERNEL(ctx, "k_ff_internal_l1", (k_ff_internal<L1_LOG2><<<unsigned(u->l1.n), 256, 0, s>>>(u->l1.d_state, u->l1.d_tile, u->l1.n, lf.p, ll.p,
                                                                                     u->l1.d_first_neg, u->l1.d_last_neg)));
@@ -482,6 +496,13 @@ __global__ void k_req_keys(const Req* __restrict__ req, uint64_t n, const int4* 
   out[i] = r.type == 1 ? kb[r.b] : ka[r.a];
 }
 
+// partial_min / partial_max of voxel/utils.rs:38-62 (ties and NaN take b)
+__device__ __forceinline__ float csg_value(int op, float a, float b) {
+  if (op == OP_UNION) return (a < b) ? a : b;
+  if (op == OP_SUBTRACT) return (a > -b) ? a : -b;
+  return (a > b) ? a : b;
+}
+
 // Output leaves: copy, copy with flipped signs, or combine (leaf_node/csg.rs:17-45).
 __global__ void __launch_bounds__(128) k_csg_leaves(int op, const Req* __restrict__ req, uint64_t n,
                                                     const int4* __restrict__ oa, const float* __restrict__ va,
@@ -501,22 +522,19 @@ __global__ void __launch_bounds__(128) k_csg_leaves(int op, const Req* __restric
     else m = ma[uint64_t(r.a) * 16 + t] | mb[uint64_t(r.b) * 16 + t];
     mo[l * 16 + t] = m;
   }
-  for (int o = t; o < 512; o += 128) {
-    float x;
-    if (r.type == 0) {
-      x = va[uint64_t(r.a) * 512 + o];
-    } else if (r.type == 1) {
-      x = vb[uint64_t(r.b) * 512 + o];
-      if (r.flip) x = -x;
-    } else {
-      const float a = va[uint64_t(r.a) * 512 + o], b = vb[uint64_t(r.b) * 512 + o];
-      // partial_min / partial_max of voxel/utils.rs:38-62 (ties and NaN take b)
-      if (op == OP_UNION) x = (a < b) ? a : b;
-      else if (op == OP_SUBTRACT) x = (a > -b) ? a : -b;
-      else x = (a > b) ? a : b;
-    }
-    vo[l * 512 + o] = x;
+  // one float4 of the leaf per thread
+  float4 x;
+  if (r.type == 0) {
+    x = reinterpret_cast<const float4*>(va + uint64_t(r.a) * 512)[t];
+  } else if (r.type == 1) {
+    x = reinterpret_cast<const float4*>(vb + uint64_t(r.b) * 512)[t];
+    if (r.flip) x = make_float4(-x.x, -x.y, -x.z, -x.w);
+  } else {
+    const float4 a = reinterpret_cast<const float4*>(va + uint64_t(r.a) * 512)[t];
+    const float4 b = reinterpret_cast<const float4*>(vb + uint64_t(r.b) * 512)[t];
+    x = make_float4(csg_value(op, a.x, b.x), csg_value(op, a.y, b.y), csg_value(op, a.z, b.z), csg_value(op, a.w, b.w));
   }
+  reinterpret_cast<float4*>(vo + l * 512)[t] = x;
 }
 
 __global__ void k_count_active(const uint32_t* __restrict__ m, uint64_t n, unsigned long long* out) {

@@ -210,6 +210,12 @@ def run_ours(args):
     L.bs_m2v_params_default(C.byref(params))
     params.voxel_size = H
     params.band_width = BAND
+    if args.pipeline_only:
+        params.voxel_size = args.voxel_size
+        # the boolean / offset / dual-contouring tail alone, once (a profiling case)
+        print(json.dumps({"pipeline": pipeline_secondary(ctx, params, dev, L, N, bs, C),
+                          "tris_fraction": args.tris_fraction, "voxel_size": args.voxel_size}))
+        return
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def step_device():
@@ -384,15 +390,15 @@ def pipeline_secondary(ctx, params, dev, L, N, bs, C):
             st = ctx.last_stats()
             d["offset_%s_relax_passes" % sign] = st["offset_passes"]
             d["offset_%s_leaf_sweeps" % sign] = st["offset_leaf_sweeps"]
-            mesher = bs.DualContouringMesher().with_voxel_size(H)
             n = C.c_uint64()
-            _, t_dc = timed(lambda: N.check(L.bs_dual_contour(ctx.h, cc.h, H, None, 0, C.byref(n)), ctx.h))
+            _, t_dc = timed(lambda: N.check(L.bs_dual_contour(ctx.h, cc.h, params.voxel_size, None, 0, C.byref(n)),
+                                            ctx.h))
             d["offset_%s_ms" % sign] = t_off
             d["dc_%s_ms" % sign] = t_dc
             d["dc_%s_triangles" % sign] = int(n.value)
             tris_total += int(n.value)
             dc_ms_total += t_dc
-            del cc, mesher
+            del cc
         res[op] = d
         del a, b, c
     res["output_triangles_per_s_dc"] = tris_total / (dc_ms_total / 1000.0) if dc_ms_total else None
@@ -420,6 +426,10 @@ def main():
                     help="skip the secondary boolean / offset / dual-contouring timings")
     ap.add_argument("--tris-fraction", type=float, default=1.0,
                     help="use only the first part of each torus ring (smaller case for profiling)")
+    ap.add_argument("--pipeline-only", action="store_true",
+                    help="run only the boolean / offset / dual-contouring tail once and print its stage times")
+    ap.add_argument("--voxel-size", type=float, default=H,
+                    help="voxel size of the --pipeline-only case (the workload's is 0.002)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
