@@ -53,6 +53,11 @@ SIGNATURES = {
     "bs_volume_subtract": (i32, [vp, vp, vp, PP]),
     "bs_volume_intersect": (i32, [vp, vp, vp, PP]),
     "bs_volume_offset": (i32, [vp, vp, f32]),
+    "bs_volume_from_samples": (i32, [vp, f32, C.c_int64, vp, vp, vp, PP]),
+    "bs_volume_from_samples_device": (i32, [vp, f32, C.c_int64, vp, vp, vp, PP]),
+    "bs_volume_sphere": (i32, [vp, f32, f32, vp, PP]),
+    "bs_volume_cuboid": (i32, [vp, f32, vp, vp, PP]),
+    "bs_volume_iwp": (i32, [vp, f32, vp, vp, f32, PP]),
     "bs_dual_contour": (i32, [vp, vp, f32, vp, u64, C.POINTER(u64)]),
     "bs_dual_contour_noalloc": (i32, [i32, vp, vp, vp, vp, u64, f32, vp, u64, C.POINTER(u64)]),
     "bs_corner_table_from_soup": (i32, [vp, vp, u64, PP]),

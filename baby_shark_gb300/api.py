@@ -83,6 +83,40 @@ class Context:
         return out
 
 
+class VolumeBuilder:
+    """VolumeBuilder (volume/builder.rs:5-84): sphere, cuboid and the IWP
+    surface, evaluated and built on the GPU."""
+
+    def __init__(self, ctx=None):
+        self.ctx = ctx or default_context()
+        self.voxel_size = 1.0
+
+    def with_voxel_size(self, voxel_size):
+        self.voxel_size = float(voxel_size)
+        return self
+
+    def set_voxel_size(self, voxel_size):
+        self.voxel_size = float(voxel_size)
+
+    def _make(self, fn, *args):
+        out = C.c_void_p()
+        N.check(fn(self.ctx.h, C.c_float(self.voxel_size), *args, C.byref(out)), self.ctx.h)
+        return Volume(out, self.ctx)
+
+    @staticmethod
+    def _v3(a):
+        return (C.c_float * 3)(*[float(x) for x in a])
+
+    def sphere(self, radius, origin):
+        return self._make(N.load().bs_volume_sphere, C.c_float(radius), self._v3(origin))
+
+    def cuboid(self, vmin, vmax):
+        return self._make(N.load().bs_volume_cuboid, self._v3(vmin), self._v3(vmax))
+
+    def iwp(self, vmin, vmax, cell_size):
+        return self._make(N.load().bs_volume_iwp, self._v3(vmin), self._v3(vmax), C.c_float(cell_size))
+
+
 _default_ctx = None
 
 
@@ -132,6 +166,37 @@ class Volume:
         out = C.c_float()
         N.check(N.load().bs_volume_voxel_size(self.h, C.byref(out)))
         return out.value
+
+    @staticmethod
+    def from_fn(voxel_size, vmin, vmax, narrow_band_width, func, ctx=None):
+        """Volume::from_fn (volume/mod.rs:40-72): `func` maps an (N, 3) float32
+        array of grid points (numpy, or a torch tensor on the context's GPU) to
+        N signed values, inside negative; the sparse volume is built on the GPU.
+        Grid points are idx * voxel_size for idx from floor(min / voxel_size)
+        to ceil(max / voxel_size), as the reference."""
+        ctx = ctx or default_context()
+        h = np.float32(voxel_size)
+        lo = np.floor(np.asarray(vmin, np.float32) / h).astype(np.int64)
+        hi = np.ceil(np.asarray(vmax, np.float32) / h).astype(np.int64)
+        dims = (hi - lo + 1).astype(np.uint64)
+        if np.any(hi < lo):
+            raise ValueError("from_fn: max below min")
+        axes = [np.arange(lo[i], hi[i] + 1).astype(np.float32) * h for i in range(3)]
+        X, Y, Z = np.meshgrid(*axes, indexing="ij")
+        pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+        out = C.c_void_p()
+        vals = func(pts)
+        if hasattr(vals, "is_cuda") and vals.is_cuda:
+            import torch
+            v = vals.to(torch.float32).contiguous()
+            N.check(N.load().bs_volume_from_samples_device(ctx.h, float(h), int(narrow_band_width),
+                                                           lo.ctypes.data, dims.ctypes.data, v.data_ptr(),
+                                                           C.byref(out)), ctx.h)
+        else:
+            v = np.ascontiguousarray(np.asarray(vals, np.float32).reshape(-1))
+            N.check(N.load().bs_volume_from_samples(ctx.h, float(h), int(narrow_band_width), lo.ctypes.data,
+                                                    dims.ctypes.data, v.ctypes.data, C.byref(out)), ctx.h)
+        return Volume(out, ctx)
 
     def counts(self):
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()

@@ -310,6 +310,11 @@ bs_volume* mesh_to_volume_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, con
                                uint64_t nt, const bs_m2v_params& p);
 void volume_release(bs_volume* v);
 bs_volume* volume_clone_impl(bs_ctx* ctx, const bs_volume* v);
+bs_volume* volume_sphere_impl(bs_ctx* ctx, float h, float radius, const float origin[3]);
+bs_volume* volume_cuboid_impl(bs_ctx* ctx, float h, const float mn[3], const float mx[3]);
+bs_volume* volume_iwp_impl(bs_ctx* ctx, float h, const float mn[3], const float mx[3], float cell);
+bs_volume* volume_from_samples_impl(bs_ctx* ctx, float h, long long band_width, const long long idx_min[3],
+                                    const unsigned long long dims[3], const float* d_values);
 bs_volume* volume_csg_impl(bs_ctx* ctx, bs_volume* a, bs_volume* b, int op);
 void volume_offset_impl(bs_ctx* ctx, bs_volume* v, float distance);
 void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size);

@@ -255,6 +255,53 @@ bs_status bs_volume_clone(bs_ctx* ctx, const bs_volume* v, bs_volume** out) {
   return guarded(ctx, [&] { *out = bs::volume_clone_impl(ctx, v); });
 }
 
+bs_status bs_volume_from_samples_device(bs_ctx* ctx, float voxel_size, int64_t band_width, const int64_t* idx_min,
+                                        const uint64_t* dims, const float* d_values, bs_volume** out) {
+  if (!ctx || !idx_min || !dims || !d_values || !out) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  return guarded(ctx, [&] {
+    const long long lo[3] = {idx_min[0], idx_min[1], idx_min[2]};
+    const unsigned long long d[3] = {dims[0], dims[1], dims[2]};
+    *out = bs::volume_from_samples_impl(ctx, voxel_size, band_width, lo, d, d_values);
+  });
+}
+
+bs_status bs_volume_from_samples(bs_ctx* ctx, float voxel_size, int64_t band_width, const int64_t* idx_min,
+                                 const uint64_t* dims, const float* h_values, bs_volume** out) {
+  if (!ctx || !idx_min || !dims || !h_values || !out) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  return guarded(ctx, [&] {
+    const double n = double(dims[0]) * double(dims[1]) * double(dims[2]);
+    if (!(n > 0.0)) bs::fail(BS_ERR_EMPTY, "from_fn: empty sample grid");
+    if (n > double(1ull << 36)) bs::fail(BS_ERR_CAPACITY, "from_fn: more than 2^36 samples");
+    const uint64_t cnt = dims[0] * dims[1] * dims[2];
+    bs::DBuf<float> vals(ctx, cnt);
+    BS_CUDA(cudaMemcpyAsync(vals.p, h_values, cnt * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    const long long lo[3] = {idx_min[0], idx_min[1], idx_min[2]};
+    const unsigned long long d[3] = {dims[0], dims[1], dims[2]};
+    *out = bs::volume_from_samples_impl(ctx, voxel_size, band_width, lo, d, vals.p);
+  });
+}
+
+bs_status bs_volume_sphere(bs_ctx* ctx, float voxel_size, float radius, const float* origin3, bs_volume** out) {
+  if (!ctx || !origin3 || !out) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  return guarded(ctx, [&] { *out = bs::volume_sphere_impl(ctx, voxel_size, radius, origin3); });
+}
+
+bs_status bs_volume_cuboid(bs_ctx* ctx, float voxel_size, const float* min3, const float* max3, bs_volume** out) {
+  if (!ctx || !min3 || !max3 || !out) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  return guarded(ctx, [&] { *out = bs::volume_cuboid_impl(ctx, voxel_size, min3, max3); });
+}
+
+bs_status bs_volume_iwp(bs_ctx* ctx, float voxel_size, const float* min3, const float* max3, float cell_size,
+                        bs_volume** out) {
+  if (!ctx || !min3 || !max3 || !out) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  return guarded(ctx, [&] { *out = bs::volume_iwp_impl(ctx, voxel_size, min3, max3, cell_size); });
+}
+
 bs_status bs_volume_export(bs_ctx* ctx, const bs_volume* v, int32_t* h_origins, float* h_values,
                            uint32_t* h_masks) {
   if (!ctx || !v || v->ctx != ctx) return BS_ERR_INVALID_ARG;

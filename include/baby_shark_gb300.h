@@ -134,6 +134,28 @@ bs_status bs_volume_intersect(bs_ctx* ctx, bs_volume* a, bs_volume* b, bs_volume
 /* Volume::offset (volume/mod.rs:95-108), in place. */
 bs_status bs_volume_offset(bs_ctx* ctx, bs_volume* v, float distance);
 
+/* ------------------------------------------- from_fn / VolumeBuilder ---- */
+/* Volume::from_fn (volume/mod.rs:40-72) over values the caller sampled: the
+ * grid points (idx_min + (i, j, k)) * voxel_size for i < dims[0], j < dims[1],
+ * k < dims[2], values x-major (values[(i*dims[1] + j)*dims[2] + k]); points with
+ * |value| <= (band_width + 1) * voxel_size become active voxels.  The closure
+ * of from_fn is evaluated by the caller (on the host or on the device):
+ * h_values is host memory, d_values device memory of the context's GPU.
+ * idx_min = floor(min / voxel_size) and the last point ceil(max / voxel_size)
+ * reproduce from_fn's box. */
+bs_status bs_volume_from_samples(bs_ctx* ctx, float voxel_size, int64_t band_width, const int64_t* idx_min,
+                                 const uint64_t* dims, const float* h_values, bs_volume** out);
+bs_status bs_volume_from_samples_device(bs_ctx* ctx, float voxel_size, int64_t band_width, const int64_t* idx_min,
+                                        const uint64_t* dims, const float* d_values, bs_volume** out);
+/* VolumeBuilder::with_voxel_size(voxel_size).sphere(radius, origin) (volume/builder.rs:21-31). */
+bs_status bs_volume_sphere(bs_ctx* ctx, float voxel_size, float radius, const float* origin3, bs_volume** out);
+/* VolumeBuilder::cuboid(min, max) (volume/builder.rs:33-54). */
+bs_status bs_volume_cuboid(bs_ctx* ctx, float voxel_size, const float* min3, const float* max3, bs_volume** out);
+/* VolumeBuilder::iwp(min, max, cell_size), the IWP triply periodic surface
+ * (volume/builder.rs:57-76); evaluated with CUDA's cosf. */
+bs_status bs_volume_iwp(bs_ctx* ctx, float voxel_size, const float* min3, const float* max3, float cell_size,
+                        bs_volume** out);
+
 /* --------------------------------------------------- dual contouring ---- */
 /* DualContouringMesher::with_voxel_size(..).mesh(&volume) (dual_contouring.rs:16-91).
  * Writes up to `capacity` triangles (9 floats each, world units) to h_tris and

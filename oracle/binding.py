@@ -48,6 +48,10 @@ def lib():
                 "orc_volume_free": (None, [vp]),
                 "orc_volume_from_leaves": (vp, [i32p, f32p, u32p, i64, f32]),
                 "orc_volume_clone": (vp, [vp]),
+                "orc_volume_sphere": (vp, [f32, f32, f32, f32, f32]),
+                "orc_volume_cuboid": (vp, [f32, f32p, f32p]),
+                "orc_volume_iwp": (vp, [f32, f32p, f32p, f32]),
+                "orc_volume_from_samples": (vp, [f32, i64, i64p, i64p, f32p]),
                 "orc_volume_num_leaves": (i64, [vp]),
                 "orc_volume_export": (None, [vp, i32p, vp, vp]),
                 "orc_volume_num_tiles": (i64, [vp]),
@@ -182,6 +186,33 @@ def volume_from_leaves(origins, values, masks, voxel_size):
     v = np.ascontiguousarray(values, np.float32)
     m = np.ascontiguousarray(masks, np.uint32)
     return OracleVolume(lib().orc_volume_from_leaves(o, v, m, len(o), float(voxel_size)), float(voxel_size))
+
+
+def volume_sphere(h, radius, origin):
+    """VolumeBuilder::sphere (volume/builder.rs:21-31)."""
+    o = [float(x) for x in origin]
+    return OracleVolume(lib().orc_volume_sphere(float(h), float(radius), *o), float(h))
+
+
+def volume_cuboid(h, vmin, vmax):
+    """VolumeBuilder::cuboid (volume/builder.rs:33-54)."""
+    a, b = np.asarray(vmin, np.float32), np.asarray(vmax, np.float32)
+    return OracleVolume(lib().orc_volume_cuboid(float(h), a, b), float(h))
+
+
+def volume_iwp(h, vmin, vmax, cell_size):
+    """VolumeBuilder::iwp (volume/builder.rs:57-76)."""
+    a, b = np.asarray(vmin, np.float32), np.asarray(vmax, np.float32)
+    return OracleVolume(lib().orc_volume_iwp(float(h), a, b, float(cell_size)), float(h))
+
+
+def volume_from_samples(h, band, idx_min, values):
+    """Volume::from_fn (volume/mod.rs:40-72) over values sampled at grid
+    points (idx_min + (i, j, k)) * h, values[i, j, k]."""
+    v = np.ascontiguousarray(values, np.float32)
+    lo = np.ascontiguousarray(idx_min, np.int64)
+    dims = np.array(v.shape, np.int64)
+    return OracleVolume(lib().orc_volume_from_samples(float(h), int(band), lo, dims, v), float(h))
 
 
 def fast_wn(verts, tris, points, beta=2.0):

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <string>
 
+#include "oracle_build.hpp"
 #include "oracle_mesh.hpp"
 
 using namespace orc;
@@ -120,6 +121,19 @@ void* orc_volume_from_leaves(const int32_t* origins, const float* values, const 
     g->insert_leaf_at(std::move(leaf));
   }
   return new Volume{std::move(g), voxel_size};
+}
+// Volume::from_fn and VolumeBuilder (voxel/volume/mod.rs:40-72, volume/builder.rs:21-76)
+void* orc_volume_sphere(float h, float radius, float ox, float oy, float oz) {
+  return new Volume(build_sphere(h, radius, v3(ox, oy, oz)));
+}
+void* orc_volume_cuboid(float h, const float* mn, const float* mx) {
+  return new Volume(build_cuboid(h, v3(mn[0], mn[1], mn[2]), v3(mx[0], mx[1], mx[2])));
+}
+void* orc_volume_iwp(float h, const float* mn, const float* mx, float cell) {
+  return new Volume(build_iwp(h, v3(mn[0], mn[1], mn[2]), v3(mx[0], mx[1], mx[2]), cell));
+}
+void* orc_volume_from_samples(float h, int64_t band, const int64_t* idx_min, const int64_t* dims, const float* values) {
+  return new Volume(from_samples(h, band, idx_min, dims, values));
 }
 void* orc_volume_clone(void* v) {
   auto* s = static_cast<Volume*>(v);
