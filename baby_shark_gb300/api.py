@@ -307,6 +307,33 @@ class DualContouringMesher:
         return out[: n.value]
 
 
+class MarchingCubesMesher:
+    """MarchingCubesMesher (voxel/meshing/marching_cubes.rs:17-63) on the GPU:
+    the reference's cubes and edge intersections with a face-consistent
+    polygon tiling of this library's own (see bs_marching_cubes)."""
+
+    def __init__(self):
+        self.voxel_size = 1.0
+
+    def with_voxel_size(self, size):
+        self.voxel_size = float(size)
+        return self
+
+    def set_voxel_size(self, size):
+        self.voxel_size = float(size)
+        return self
+
+    def mesh(self, volume):
+        """Triangle soup as float32[n, 3, 3] in world units."""
+        L = N.load()
+        n = C.c_uint64()
+        N.check(L.bs_marching_cubes(volume.ctx.h, volume.h, self.voxel_size, None, 0, C.byref(n)), volume.ctx.h)
+        out = np.zeros((max(n.value, 1), 3, 3), np.float32)
+        N.check(L.bs_marching_cubes(volume.ctx.h, volume.h, self.voxel_size, out.ctypes.data, n.value, C.byref(n)),
+                volume.ctx.h)
+        return out[: n.value]
+
+
 class CornerTable:
     """Corner-table mesh built from a triangle soup (bs_corner_table)."""
 
@@ -328,6 +355,13 @@ class CornerTable:
         t = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
         out = C.c_void_p()
         N.check(N.load().bs_corner_table_from_soup(ctx.h, t.ctypes.data, len(t), C.byref(out)), ctx.h)
+        return CornerTable(out)
+
+    @staticmethod
+    def from_marching_cubes(volume, voxel_size):
+        out = C.c_void_p()
+        N.check(N.load().bs_corner_table_from_marching_cubes(volume.ctx.h, volume.h, float(voxel_size), C.byref(out)),
+                volume.ctx.h)
         return CornerTable(out)
 
     @staticmethod
@@ -364,10 +398,9 @@ class CornerTable:
 class VoxelRemesher:
     """VoxelRemesher (remeshing/voxel.rs:44-95): mesh -> SDF -> surface -> CornerTable.
 
-    The reference's default meshing method is marching cubes ("Manifold"),
-    which this build does not provide on the GPU; FeaturePreserving (dual
-    contouring) is supported.  The band width defaults to 0 like the
-    reference; with_narrow_band_width is an extension."""
+    Manifold (the reference's default) meshes with MarchingCubesMesher,
+    FeaturePreserving with dual contouring.  The band width defaults to 0
+    like the reference; with_narrow_band_width is an extension."""
 
     FEATURE_PRESERVING = "FeaturePreserving"
     MANIFOLD = "Manifold"
@@ -391,9 +424,9 @@ class VoxelRemesher:
         return self
 
     def remesh(self, mesh):
-        if self.method != self.FEATURE_PRESERVING:
-            raise NotImplementedError("marching cubes is not built on the GPU; use FeaturePreserving")
         vol = self.m2v.convert(mesh)
         if vol is None:
             return None
-        return CornerTable.from_dual_contouring(vol, self.voxel_size)
+        if self.method == self.FEATURE_PRESERVING:
+            return CornerTable.from_dual_contouring(vol, self.voxel_size)
+        return CornerTable.from_marching_cubes(vol, self.voxel_size)

@@ -165,6 +165,11 @@ struct bs_volume {
   uint64_t n_dc_tris = 0;
   bool dc_valid = false;
   float dc_h = 0.0f;
+  // cached marching-cubes output (world-unit triangles)
+  float* d_mc_tris = nullptr;
+  uint64_t n_mc_tris = 0;
+  bool mc_valid = false;
+  float mc_h = 0.0f;
   ~bs_volume();
 };
 
@@ -310,6 +315,7 @@ bs_volume* mesh_to_volume_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, con
                                uint64_t nt, const bs_m2v_params& p);
 void volume_release(bs_volume* v);
 bs_volume* volume_clone_impl(bs_ctx* ctx, const bs_volume* v);
+void marching_cubes_impl(bs_ctx* ctx, bs_volume* v, float voxel_size);
 bs_volume* volume_sphere_impl(bs_ctx* ctx, float h, float radius, const float origin[3]);
 bs_volume* volume_cuboid_impl(bs_ctx* ctx, float h, const float mn[3], const float mx[3]);
 bs_volume* volume_iwp_impl(bs_ctx* ctx, float h, const float mn[3], const float mx[3], float cell);

@@ -34,6 +34,7 @@ bs_volume::~bs_volume() {
   bs::dfree(ctx, d_tiles);
   bs::dfree(ctx, d_tile_values);
   bs::dfree(ctx, d_dc_tris);
+  bs::dfree(ctx, d_mc_tris);
   bs_volume_free_upper(this);
   bs_ctx_release(ctx);
 }
@@ -370,6 +371,20 @@ bs_status bs_dual_contour(bs_ctx* ctx, bs_volume* v, float voxel_size, float* h_
     *n_tris = v->n_dc_tris;
     if (capacity >= v->n_dc_tris && v->n_dc_tris) {
       BS_CUDA(cudaMemcpyAsync(h_tris, v->d_dc_tris, v->n_dc_tris * 9 * sizeof(float), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+      BS_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+  });
+}
+
+bs_status bs_marching_cubes(bs_ctx* ctx, bs_volume* v, float voxel_size, float* h_tris, uint64_t capacity,
+                            uint64_t* n_tris) {
+  if (!ctx || !v || !n_tris || v->ctx != ctx || (capacity && !h_tris)) return BS_ERR_INVALID_ARG;
+  return guarded(ctx, [&] {
+    bs::marching_cubes_impl(ctx, v, voxel_size);
+    *n_tris = v->n_mc_tris;
+    if (capacity >= v->n_mc_tris && v->n_mc_tris) {
+      BS_CUDA(cudaMemcpyAsync(h_tris, v->d_mc_tris, v->n_mc_tris * 9 * sizeof(float), cudaMemcpyDeviceToHost,
                               ctx->stream));
       BS_CUDA(cudaStreamSynchronize(ctx->stream));
     }

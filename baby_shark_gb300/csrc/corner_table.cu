@@ -325,6 +325,22 @@ bs_status bs_corner_table_from_dual_contour(bs_ctx* ctx, bs_volume* v, float vox
   }
 }
 
+bs_status bs_corner_table_from_marching_cubes(bs_ctx* ctx, bs_volume* v, float voxel_size, bs_corner_table** out) {
+  if (!ctx || !v || !out || v->ctx != ctx) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  try {
+    BS_CUDA(cudaSetDevice(ctx->device));
+    bs::marching_cubes_impl(ctx, v, voxel_size);
+    *out = bs::corner_table_from_device_soup(ctx, v->d_mc_tris, v->n_mc_tris * 3);
+    return BS_OK;
+  } catch (const bs::Error& e) {
+    ctx->last_error = e.msg;
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    return BS_ERR_OOM;
+  }
+}
+
 bs_status bs_corner_table_counts(const bs_corner_table* t, uint64_t* n_faces, uint64_t* n_vertices,
                                  uint64_t* n_vertex_slots, uint64_t* n_corners) {
   if (!t) return BS_ERR_INVALID_ARG;

@@ -1,0 +1,246 @@
+// Marching-cubes surface extraction (MarchingCubesMesher::mesh,
+// voxel/meshing/marching_cubes.rs:43-63, 967-1181) for volumes without tiles.
+//
+// Kept from the reference: the cubes (one per voxel of every leaf, its eight
+// corners (0,0,0) (1,0,0) (1,1,0) (0,1,0) (0,0,1) (1,0,1) (1,1,1) (0,1,1) all
+// active), the corner values (|v| < 1e-6 pushed to +-1e-6), inside = negative,
+// the edge intersections t = max(|a|, 1e-6) / (max(|a|, 1e-6) + max(|b|, 1e-6))
+// from the lower corner, the scale by the voxel size and the removal of
+// degenerate triangles.
+//
+// The tiling is this file's own (the reference's MC33 case tables are not
+// used): every face of the cube contributes the segments of its crossing
+// edges, directed from the edge where the counter-clockwise walk around the
+// face (seen from outside) enters the inside to the edge where it leaves; a
+// face with four crossings joins its inside corners when the bilinear saddle
+// is inside (a0 a2 > a1 a3 for inside corners 0, 2).  The segments close into
+// cycles oriented with the outside to the front; each cycle becomes a fan of
+// triangles from its lowest-numbered edge.  Vertex positions match the
+// reference bit for bit; triangle counts match wherever a cube has no
+// ambiguity; interior ambiguities (MC33 tunnels) are not resolved.
+//
+// One warp per leaf stages the leaf and the +x, +y, +z neighbour layers in a
+// 9 x 9 x 9 shared tile; a count pass, a scan and a write pass place the
+// triangles of every leaf, lane and cube in a fixed order.
+#include <cub/device/device_scan.cuh>
+
+#include "bs_internal.cuh"
+#include "leaf_hash.cuh"
+
+namespace bs {
+
+namespace {
+
+constexpr int MC_WARPS = 4;
+constexpr int T9 = 9;
+
+__constant__ int8_t c_edge[12][2] = {{0, 1}, {1, 2}, {3, 2}, {0, 3}, {4, 5}, {5, 6},
+                                     {7, 6}, {4, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+__constant__ int8_t c_edge_axis[12] = {0, 1, 0, 1, 0, 1, 0, 1, 2, 2, 2, 2};
+__constant__ int8_t c_face[6][4] = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4}, {3, 7, 6, 2}, {0, 4, 7, 3}, {1, 2, 6, 5}};
+__constant__ int8_t c_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+// edge between two corners, -1 if none
+__constant__ int8_t c_edge_of[8][8] = {
+    {-1, 0, -1, 3, 8, -1, -1, -1}, {0, -1, 1, -1, -1, 9, -1, -1},  {-1, 1, -1, 2, -1, -1, 10, -1},
+    {3, -1, 2, -1, -1, -1, -1, 11}, {8, -1, -1, -1, -1, 4, -1, 7}, {-1, 9, -1, -1, 4, -1, 5, -1},
+    {-1, -1, 10, -1, -1, 5, -1, 6}, {-1, -1, -1, 11, 7, -1, 6, -1}};
+
+struct McVol {
+  const int4* org;
+  const float* val;
+  const uint32_t* msk;
+  LeafHash hash;
+};
+
+__device__ __forceinline__ int t9(int x, int y, int z) { return (x * T9 + y) * T9 + z; }
+
+// Triangles of one cube: returns the count; writes them when `out` is set.
+__device__ int cube_tris(const float* W, int x, int y, int z, int4 org, float h, float* out) {
+  float raw[8], v[8];
+  uint32_t in = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const float r = W[t9(x + c_corner[i][0], y + c_corner[i][1], z + c_corner[i][2])];
+    if (r == INFINITY) return 0;  // a corner is not active: no cube (Cube::from_voxel)
+    raw[i] = r;
+    v[i] = fabsf(r) < 1e-6f ? copysignf(1e-6f, r) : r;
+    if (v[i] < 0.0f) in |= 1u << i;
+  }
+  if (in == 0u || in == 0xffu) return 0;
+  int8_t next[12];
+#pragma unroll
+  for (int e = 0; e < 12; ++e) next[e] = -1;
+  for (int f = 0; f < 6; ++f) {
+    int c[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) c[s] = c_face[f][s];
+    int k = 0;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) k += ((in >> c[s]) & 1u) != ((in >> c[(s + 1) & 3]) & 1u);
+    if (k == 2) {
+      int entry = -1, exit = -1;
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        const int a = c[s], b = c[(s + 1) & 3];
+        const bool ia = (in >> a) & 1u, ib = (in >> b) & 1u;
+        if (!ia && ib) entry = c_edge_of[a][b];
+        if (ia && !ib) exit = c_edge_of[a][b];
+      }
+      next[entry] = int8_t(exit);
+    } else if (k == 4) {
+      const int p = ((in >> c[0]) & 1u) ? 0 : 1;  // corners p and p + 2 are inside
+      const float prod_in = fmul(v[c[p]], v[c[p + 2]]), prod_out = fmul(v[c[(p + 1) & 3]], v[c[(p + 3) & 3]]);
+      if (prod_in > prod_out) {
+        for (int q = (p + 1) & 3, t = 0; t < 2; ++t, q = (q + 2) & 3)
+          next[c_edge_of[c[q]][c[(q + 1) & 3]]] = c_edge_of[c[(q + 3) & 3]][c[q]];
+      } else {
+        for (int r = p, t = 0; t < 2; ++t, r = (r + 2) & 3)
+          next[c_edge_of[c[(r + 3) & 3]][c[r]]] = c_edge_of[c[r]][c[(r + 1) & 3]];
+      }
+    }
+  }
+  int count = 0;
+  uint32_t seen = 0;
+  for (int e0 = 0; e0 < 12; ++e0) {
+    if (next[e0] < 0 || ((seen >> e0) & 1u)) continue;
+    int poly[12], n = 0;
+    for (int e = e0; !((seen >> e) & 1u) && n < 12; e = next[e]) {
+      seen |= 1u << e;
+      poly[n++] = e;
+    }
+    F3 p[12];
+    for (int i = 0; i < n; ++i) {
+      const int e = poly[i], a = c_edge[e][0], b = c_edge[e][1];
+      const float va = fmaxf(fabsf(raw[a]), 1e-6f), vb = fmaxf(fabsf(raw[b]), 1e-6f);
+      const float t = fdiv(va, fadd(va, vb));
+      float q[3] = {float(org.x + x + c_corner[a][0]), float(org.y + y + c_corner[a][1]), float(org.z + z + c_corner[a][2])};
+      const int ax = c_edge_axis[e];
+      q[ax] = fadd(q[ax], t);
+      p[i] = f3(fmul(q[0], h), fmul(q[1], h), fmul(q[2], h));
+    }
+    for (int i = 1; i + 1 < n; ++i) {
+      const F3 a = p[0], b = p[i], c = p[i + 1];
+      const F3 u = f3(fsub(b.x, a.x), fsub(b.y, a.y), fsub(b.z, a.z));
+      const F3 w = f3(fsub(c.x, a.x), fsub(c.y, a.y), fsub(c.z, a.z));
+      const float cx = fsub(fmul(u.y, w.z), fmul(u.z, w.y));
+      const float cy = fsub(fmul(u.z, w.x), fmul(u.x, w.z));
+      const float cz = fsub(fmul(u.x, w.y), fmul(u.y, w.x));
+      if (fadd(fadd(fmul(cx, cx), fmul(cy, cy)), fmul(cz, cz)) == 0.0f) continue;  // Triangle3::is_degenerate
+      if (out) {
+        float* o = out + 9 * count;
+        o[0] = a.x; o[1] = a.y; o[2] = a.z;
+        o[3] = b.x; o[4] = b.y; o[5] = b.z;
+        o[6] = c.x; o[7] = c.y; o[8] = c.z;
+      }
+      ++count;
+    }
+  }
+  return count;
+}
+
+// One warp per leaf.  Pass 1 (tris == nullptr) stores each leaf's triangle
+// count; pass 2 writes them from the leaf's scanned offset.
+__global__ void __launch_bounds__(32 * MC_WARPS) k_mc(McVol V, uint64_t n, float h, uint32_t* __restrict__ leaf_count,
+                                                     const uint32_t* __restrict__ leaf_off, float* __restrict__ tris) {
+  __shared__ float tile[MC_WARPS][T9 * T9 * T9];
+  __shared__ int snb[MC_WARPS][8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint64_t leaf = blockIdx.x * uint64_t(MC_WARPS) + w;
+  if (leaf >= n) return;
+  float* W = tile[w];
+  const int4 org = V.org[leaf];
+  const float* lv = V.val + leaf * 512;
+  const uint32_t* lm = V.msk + leaf * 16;
+  for (int k = lane; k < 512; k += 32)
+    W[t9(k >> 6, (k >> 3) & 7, k & 7)] = ((lm[k >> 5] >> (k & 31)) & 1u) ? lv[k] : INFINITY;
+  // neighbours +x, +y, +z, +x+y, +x+z, +y+z, +x+y+z
+  if (lane < 7) {
+    const int d = lane + 1;  // bit 0: x, bit 1: y, bit 2: z
+    snb[w][lane] = V.hash.find(org.x + ((d & 1) ? 8 : 0), org.y + ((d & 2) ? 8 : 0), org.z + ((d & 4) ? 8 : 0));
+  }
+  __syncwarp();
+  // the 217 halo cells: x = 8 or y = 8 or z = 8
+  for (int k = lane; k < 217; k += 32) {
+    int x, y, z;
+    if (k < 64) { x = 8; y = k >> 3; z = k & 7; }
+    else if (k < 128) { x = (k - 64) >> 3; y = 8; z = (k - 64) & 7; }
+    else if (k < 192) { x = (k - 128) >> 3; y = (k - 128) & 7; z = 8; }
+    else if (k < 200) { x = 8; y = 8; z = k - 192; }
+    else if (k < 208) { x = 8; y = k - 200; z = 8; }
+    else if (k < 216) { x = k - 208; y = 8; z = 8; }
+    else { x = 8; y = 8; z = 8; }
+    const int d = (x == 8 ? 1 : 0) | (y == 8 ? 2 : 0) | (z == 8 ? 4 : 0);
+    const int n_leaf = snb[w][d - 1];
+    float val = INFINITY;
+    if (n_leaf >= 0) {
+      const int o = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
+      if ((V.msk[uint64_t(n_leaf) * 16 + (o >> 5)] >> (o & 31)) & 1u) val = V.val[uint64_t(n_leaf) * 512 + o];
+    }
+    W[t9(x, y, z)] = val;
+  }
+  __syncwarp();
+  uint32_t mine = 0;
+  for (int j = 0; j < 16; ++j) {
+    const int o = 32 * j + lane;
+    mine += uint32_t(cube_tris(W, o >> 6, (o >> 3) & 7, o & 7, org, h, nullptr));
+  }
+  if (!tris) {
+    uint32_t s = mine;
+    for (int d = 16; d > 0; d >>= 1) s += __shfl_down_sync(0xffffffffu, s, d);
+    if (lane == 0) leaf_count[leaf] = s;
+    return;
+  }
+  uint32_t incl = mine;
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += t;
+  }
+  uint64_t at = uint64_t(leaf_off[leaf]) + (incl - mine);
+  for (int j = 0; j < 16; ++j) {
+    const int o = 32 * j + lane;
+    at += uint64_t(cube_tris(W, o >> 6, (o >> 3) & 7, o & 7, org, h, tris + 9 * at));
+  }
+}
+
+}  // namespace
+
+// MarchingCubesMesher::with_voxel_size(voxel_size).mesh(&volume); the
+// triangles stay cached on the volume until it changes.
+void marching_cubes_impl(bs_ctx* ctx, bs_volume* v, float voxel_size) {
+  if (v->mc_valid && v->mc_h == voxel_size) return;
+  if (v->n_tiles) fail(BS_ERR_UNSUPPORTED, "marching cubes: volumes with active tiles are not supported");
+  cudaStream_t s = ctx->stream;
+  dfree(ctx, v->d_mc_tris);
+  v->d_mc_tris = nullptr;
+  v->n_mc_tris = 0;
+  const uint64_t n = v->n_leaves;
+  if (n == 0) {
+    v->mc_valid = true;
+    v->mc_h = voxel_size;
+    return;
+  }
+  LeafHashBuf hb;
+  hb.build(ctx, v->d_origins, n, n);
+  McVol V{v->d_origins, v->d_values, v->d_masks, hb.h};
+  DBuf<uint32_t> cnt(ctx, n + 1), off(ctx, n + 1);
+  BS_CUDA(cudaMemsetAsync(cnt.p + n, 0, sizeof(uint32_t), s));
+  const unsigned grid = unsigned((n + MC_WARPS - 1) / MC_WARPS);
+  BS_KERNEL(ctx, "k_mc_count", (k_mc<<<grid, 32 * MC_WARPS, 0, s>>>(V, n, voxel_size, cnt.p, nullptr, nullptr)));
+  size_t tmp = 0;
+  BS_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, cnt.p, off.p, n + 1, s));
+  {
+    DBuf<uint8_t> t(ctx, tmp);
+    BS_CUDA(cub::DeviceScan::ExclusiveSum(t.p, tmp, cnt.p, off.p, n + 1, s));
+  }
+  uint32_t nt = 0;
+  read_back(ctx, &nt, off.p + n, sizeof nt);
+  if (nt) {
+    v->d_mc_tris = dalloc<float>(ctx, uint64_t(nt) * 9);
+    BS_KERNEL(ctx, "k_mc_write", (k_mc<<<grid, 32 * MC_WARPS, 0, s>>>(V, n, voxel_size, nullptr, off.p, v->d_mc_tris)));
+  }
+  v->n_mc_tris = nt;
+  v->mc_valid = true;
+  v->mc_h = voxel_size;
+}
+
+}  // namespace bs

@@ -725,6 +725,7 @@ void volume_offset_impl(bs_ctx* ctx, bs_volume* v, float distance) {
   v->d_tile_values = nullptr;
   v->n_tiles = 0;
   v->dc_valid = false;
+  v->mc_valid = false;
   compact_nonempty(ctx, v, h * 2.0f);  // self.voxel_size * 2.0
   // 2. fast sweeping to |d| + 2h with the sign of d (volume/mod.rs:98-102)
   volatile float hv = h;  // (|d| + h) + h in f32, as the reference

@@ -156,6 +156,18 @@ bs_status bs_volume_cuboid(bs_ctx* ctx, float voxel_size, const float* min3, con
 bs_status bs_volume_iwp(bs_ctx* ctx, float voxel_size, const float* min3, const float* max3, float cell_size,
                         bs_volume** out);
 
+/* --------------------------------------------------- marching cubes ---- */
+/* MarchingCubesMesher::with_voxel_size(..).mesh(&volume) (marching_cubes.rs:30-63)
+ * for a volume without active tiles (BS_ERR_UNSUPPORTED otherwise).  Same
+ * calling convention as bs_dual_contour: capacity 0 sizes the buffer, the
+ * result is cached on the volume.  Cubes, corner values and edge
+ * intersections are the reference's; the tiling inside a cube is this
+ * library's own face-consistent polygon fan (not the MC33 case tables), so
+ * vertex positions match the reference and triangle counts match for cubes
+ * without face or interior ambiguity. */
+bs_status bs_marching_cubes(bs_ctx* ctx, bs_volume* v, float voxel_size, float* h_tris, uint64_t capacity,
+                            uint64_t* n_tris);
+
 /* --------------------------------------------------- dual contouring ---- */
 /* DualContouringMesher::with_voxel_size(..).mesh(&volume) (dual_contouring.rs:16-91).
  * Writes up to `capacity` triangles (9 floats each, world units) to h_tris and
@@ -200,6 +212,9 @@ bs_status bs_corner_table_from_soup(bs_ctx* ctx, const float* h_tris, uint64_t n
  * trip of the soup (VoxelRemesher with MeshingMethod::FeaturePreserving,
  * remeshing/voxel.rs:64-85). */
 bs_status bs_corner_table_from_dual_contour(bs_ctx* ctx, bs_volume* v, float voxel_size, bs_corner_table** out);
+/* The same on the marching-cubes output (VoxelRemesher with the default
+ * MeshingMethod::Manifold, remeshing/voxel.rs:64-85). */
+bs_status bs_corner_table_from_marching_cubes(bs_ctx* ctx, bs_volume* v, float voxel_size, bs_corner_table** out);
 /* Faces, live vertices, vertex slots (live + deleted) and corners. */
 bs_status bs_corner_table_counts(const bs_corner_table* t, uint64_t* n_faces, uint64_t* n_vertices,
                                  uint64_t* n_vertex_slots, uint64_t* n_corners);

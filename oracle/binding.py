@@ -63,6 +63,7 @@ def lib():
                 "orc_volume_offset": (C.c_int, [vp, f32]),
                 "orc_dual_contour": (i64, [vp, f32, vp, i64, vp, vp, vp]),
                 "orc_mc_count": (i64, [vp, vp, vp]),
+                "orc_marching_cubes": (i64, [vp, f32, vp, i64]),
                 "orc_corner_table_from_soup": (C.c_int, [f32p, i64, vp, vp]),
                 "orc_corner_table_from_indexed": (C.c_int, [f32p, i64, i64p, i64, vp, vp, vp, vp, vp, vp, vp, vp]),
                 "orc_fast_wn": (None, [f32p, i64, u32p, i64, f32p, i64, f32, f32p, vp]),
@@ -154,6 +155,14 @@ class OracleVolume:
         out = np.zeros((max(n, 1), 9), np.float32)
         lib().orc_dual_contour(self.h, self.voxel_size, _ptr(out), n, C.byref(st), None, None)
         return out[:n].reshape(n, 3, 3), st.value, ne.value, nc.value
+
+    def marching_cubes(self, voxel_size=None):
+        """Triangles (n, 3, 3) of the oracle's marching-cubes mesher (oracle_mc.hpp)."""
+        h = self.voxel_size if voxel_size is None else float(voxel_size)
+        n = lib().orc_marching_cubes(self.h, h, None, 0)
+        out = np.zeros((max(n, 1), 9), np.float32)
+        lib().orc_marching_cubes(self.h, h, _ptr(out), n)
+        return out[:n].reshape(n, 3, 3)
 
     def mc_triangles(self):
         amb, cubes = C.c_int64(0), C.c_int64(0)

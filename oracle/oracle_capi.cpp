@@ -5,9 +5,12 @@
 // 512-bit active mask as 16 x uint32 (bit i&31 of word i>>5 = voxel i, voxel
 // index x<<6 | y<<3 | z).
 #include <cstdio>
+#include <cstring>
+#include <algorithm>
 #include <string>
 
 #include "oracle_build.hpp"
+#include "oracle_mc.hpp"
 #include "oracle_mesh.hpp"
 
 using namespace orc;
@@ -225,6 +228,15 @@ int64_t orc_mc_count(void* v, int64_t* ambiguous_faces, int64_t* cubes) {
   if (ambiguous_faces) *ambiguous_faces = int64_t(mc.ambiguous_faces);
   if (cubes) *cubes = int64_t(mc.cubes);
   return int64_t(mc.triangles);
+}
+
+// Marching-cubes triangles of a volume without tiles (oracle_mc.hpp); returns
+// the triangle count, copies up to `capacity` triangles.
+int64_t orc_marching_cubes(void* v, float voxel_size, float* out, int64_t capacity) {
+  std::vector<float> t = mc_mesh(*static_cast<Volume*>(v)->grid, voxel_size);
+  const int64_t n = int64_t(t.size() / 9);
+  if (out) std::memcpy(out, t.data(), size_t(std::min(n, capacity)) * 9 * sizeof(float));
+  return n;
 }
 
 // CornerTable::from_triangles_soup / builder_soup().finish().

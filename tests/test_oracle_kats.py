@@ -27,6 +27,13 @@ def test_volume_offset_7944():
     n_tri, ambiguous, _ = vol.mc_triangles()
     assert ambiguous == 0  # the triangle counter is exact only without ambiguous faces
     assert 3 * n_tri == g["mc_vertices"]
+    # the marching-cubes mesher the GPU mirrors gives the same soup size
+    tri = vol.marching_cubes(g["voxel_size"])
+    assert 3 * len(tri) == g["mc_vertices"]
+    # every triangle faces the positive (outside) side: normals point away from the box's centre
+    n = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    centre = verts.mean(axis=0)
+    assert np.mean(np.einsum("ij,ij->i", n, tri.mean(axis=1) - centre) > 0) > 0.99
 
 
 @pytest.mark.parametrize("op", ["union", "subtract", "intersect"])
