@@ -286,6 +286,33 @@ class MeshToVolume:
         return Volume(out, self.ctx)
 
 
+def convert_batch(meshes, params, ctx=None):
+    """Many meshes in one set of GPU launches (bs_mesh_to_volume_batch).
+
+    `meshes` is a list of (vertices, triangles) pairs, `params` a list of
+    (voxel_size, band_width) pairs or one pair for all.  Returns one Volume
+    per mesh (None for a mesh without triangles); each equals what
+    MeshToVolume(...).convert returns for that mesh alone."""
+    ctx = ctx or default_context()
+    K = len(meshes)
+    if isinstance(params, tuple):
+        params = [params] * K
+    arrays = [_mesh_arrays(m) for m in meshes]
+    xyz = np.ascontiguousarray(np.concatenate([v for v, _ in arrays]) if K else np.zeros((0, 3), np.float32))
+    tri = np.ascontiguousarray(np.concatenate([f for _, f in arrays]) if K else np.zeros((0, 3), np.uint32))
+    nv = np.array([len(v) for v, _ in arrays], np.uint64)
+    nt = np.array([len(f) for _, f in arrays], np.uint64)
+    P = (N.M2VParams * K)()
+    for k, (h, band) in enumerate(params):
+        N.load().bs_m2v_params_default(C.byref(P[k]))
+        P[k].voxel_size = float(h)
+        P[k].band_width = int(band)
+    out = (C.c_void_p * K)()
+    N.check(N.load().bs_mesh_to_volume_batch(ctx.h, K, xyz.ctypes.data, nv.ctypes.data, tri.ctypes.data,
+                                             nt.ctypes.data, P, out), ctx.h)
+    return [Volume(C.c_void_p(out[k]), ctx) if out[k] else None for k in range(K)]
+
+
 class DualContouringMesher:
     """DualContouringMesher (voxel/meshing/dual_contouring.rs:12-91)."""
 

@@ -314,6 +314,10 @@ namespace bs {
 bs_volume* mesh_to_volume_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri,
                                uint64_t nt, const bs_m2v_params& p);
 void volume_release(bs_volume* v);
+std::vector<bs_volume*> mesh_to_volume_batch_impl(bs_ctx* ctx, const float* d_xyz, const uint32_t* d_tri,
+                                                  const std::vector<uint64_t>& n_vtx,
+                                                  const std::vector<uint64_t>& n_tri,
+                                                  const std::vector<bs_m2v_params>& params);
 bs_volume* volume_clone_impl(bs_ctx* ctx, const bs_volume* v);
 void marching_cubes_impl(bs_ctx* ctx, bs_volume* v, float voxel_size);
 bs_volume* volume_sphere_impl(bs_ctx* ctx, float h, float radius, const float origin[3]);

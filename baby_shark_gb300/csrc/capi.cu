@@ -230,6 +230,47 @@ bs_status bs_mesh_to_volume(bs_ctx* ctx, const float* h_xyz, uint64_t nv, const 
   });
 }
 
+static bs_status batch_common(bs_ctx* ctx, uint64_t K, const float* xyz, const uint64_t* nv, const uint32_t* tri,
+                              const uint64_t* nt, const bs_m2v_params* params, bs_volume** out, bool host) {
+  if (!ctx || !nv || !nt || !params || !out) return BS_ERR_INVALID_ARG;
+  for (uint64_t m = 0; m < K; ++m) out[m] = nullptr;
+  return guarded(ctx, [&] {
+    if (K == 0) bs::fail(BS_ERR_EMPTY, "no meshes");
+    std::vector<uint64_t> vn(nv, nv + K), tn(nt, nt + K);
+    std::vector<bs_m2v_params> ps(params, params + K);
+    uint64_t V = 0, T = 0;
+    for (uint64_t m = 0; m < K; ++m) {
+      V += vn[m];
+      T += tn[m];
+    }
+    if (T && (!xyz || !tri)) bs::fail(BS_ERR_INVALID_ARG, "null vertex or triangle array");
+    std::vector<bs_volume*> r;
+    if (host) {
+      bs::DBuf<float> dx(ctx, std::max<uint64_t>(3 * V, 1));
+      bs::DBuf<uint32_t> dt(ctx, std::max<uint64_t>(3 * T, 1));
+      if (V) BS_CUDA(cudaMemcpyAsync(dx.p, xyz, 3 * V * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+      if (T) BS_CUDA(cudaMemcpyAsync(dt.p, tri, 3 * T * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
+      r = bs::mesh_to_volume_batch_impl(ctx, dx.p, dt.p, vn, tn, ps);
+    } else {
+      r = bs::mesh_to_volume_batch_impl(ctx, xyz, tri, vn, tn, ps);
+    }
+    for (uint64_t m = 0; m < K; ++m) out[m] = r[m];
+  });
+}
+
+bs_status bs_mesh_to_volume_batch(bs_ctx* ctx, uint64_t n_meshes, const float* h_xyz, const uint64_t* vertex_counts,
+                                  const uint32_t* h_tri, const uint64_t* triangle_counts,
+                                  const bs_m2v_params* params, bs_volume** out) {
+  return batch_common(ctx, n_meshes, h_xyz, vertex_counts, h_tri, triangle_counts, params, out, true);
+}
+
+bs_status bs_mesh_to_volume_batch_device(bs_ctx* ctx, uint64_t n_meshes, const float* d_xyz,
+                                         const uint64_t* vertex_counts, const uint32_t* d_tri,
+                                         const uint64_t* triangle_counts, const bs_m2v_params* params,
+                                         bs_volume** out) {
+  return batch_common(ctx, n_meshes, d_xyz, vertex_counts, d_tri, triangle_counts, params, out, false);
+}
+
 bs_status bs_volume_free(bs_volume* v) {
   if (!v) return BS_ERR_INVALID_ARG;
   delete v;

@@ -16,6 +16,8 @@
 // Steps 1-3 use IEEE-exact arithmetic (bs_internal.cuh) so distances and the
 // active set match the reference bit for bit.
 #include <cub/device/device_radix_sort.cuh>
+
+#include <vector>
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
@@ -62,33 +64,98 @@ struct M2VStats {
   unsigned long long wn_exact;       // warp-level exact solid angles
 };
 
+// Per-mesh parameters of a batch.  Triangles of mesh m are [tri_base,
+// tri_base + n_tri) of the concatenated index array; their indices are local
+// to the mesh's vertices [vtx_base, vtx_base + n_vtx).
+struct MeshInfo {
+  float h, inv_h, beta, thresh;
+  int band, pad;
+  uint32_t tri_base, n_tri;
+  uint64_t vtx_base, n_vtx;
+};
+
+// Largest m in [0, k) with base[m] <= i (segments may be empty).
+template <class T>
+__device__ __forceinline__ int find_seg(const T* __restrict__ base, int k, uint64_t i) {
+  int lo = 0, hi = k - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (uint64_t(__ldg(base + mid)) <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Adds v to *dst once per warp when every active lane targets the same mesh.
+__device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long long v, int m) {
+  const unsigned mask = __activemask();
+  const int leader = __ffs(mask) - 1;
+  const int m0 = __shfl_sync(mask, m, leader);
+  if (__all_sync(mask, m == m0)) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(mask, v, o);
+    if ((threadIdx.x & 31) == leader) atomicAdd(dst, v);
+  } else {
+    atomicAdd(dst, v);
+  }
+}
+
+// atomicMin / atomicMax of v into *dst, one atomic per warp when every active
+// lane targets the same mesh (the address is then warp-uniform).
+__device__ __forceinline__ bool warp_one_mesh(unsigned mask, int m) {
+  return __all_sync(mask, m == __shfl_sync(mask, m, __ffs(mask) - 1));
+}
+template <class T>
+__device__ __forceinline__ void warp_min(T* dst, T v, bool uniform, unsigned mask) {
+  if (uniform) {
+    const T r = __reduce_min_sync(mask, v);
+    if ((threadIdx.x & 31) == __ffs(mask) - 1) atomicMin(dst, r);
+  } else {
+    atomicMin(dst, v);
+  }
+}
+template <class T>
+__device__ __forceinline__ void warp_max(T* dst, T v, bool uniform, unsigned mask) {
+  if (uniform) {
+    const T r = __reduce_max_sync(mask, v);
+    if ((threadIdx.x & 31) == __ffs(mask) - 1) atomicMax(dst, r);
+  } else {
+    atomicMax(dst, v);
+  }
+}
+
 struct SubTri {  // 64 B: vertices and the widened inclusive integer box
   float4 p0;     // a.x a.y a.z b.x
   float4 p1;     // b.y b.z c.x c.y
   float4 p2;     // c.z, -, -, -
-  int4 lo;       // box min (x, y, z), -
+  int4 lo;       // box min (x, y, z), mesh
   int4 hi;       // box max
 };
 
 // ------------------------------------------- 1. triangles and subdivision --
-__global__ void k_gather(const float* __restrict__ xyz, uint64_t nv, const uint32_t* __restrict__ tri,
-                         uint64_t nt, float h, float inv_h, int band, float4* __restrict__ T,
-                         uint32_t* __restrict__ nsub, M2VStats* st) {
+__global__ void k_gather(const float* __restrict__ xyz, const uint32_t* __restrict__ tri, uint64_t nt,
+                         const MeshInfo* __restrict__ mi, const uint32_t* __restrict__ tri_base, int K,
+                         float4* __restrict__ T, uint32_t* __restrict__ nsub, M2VStats* st) {
   uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (i >= nt) {
     if (i == nt) nsub[nt] = 0;
     return;
   }
+  const int mesh = find_seg(tri_base, K, i);
+  const MeshInfo M = mi[mesh];
+  M2VStats* S = st + mesh;
+  const float h = M.h, inv_h = M.inv_h;
+  const int band = M.band;
   uint32_t ia = tri[3 * i], ib = tri[3 * i + 1], ic = tri[3 * i + 2];
-  if (ia >= nv || ib >= nv || ic >= nv) {
-    atomicExch(&st->error, 1);
+  if (ia >= M.n_vtx || ib >= M.n_vtx || ic >= M.n_vtx) {
+    atomicExch(&S->error, 1);
     nsub[i] = 0;
     T[3 * i] = T[3 * i + 1] = T[3 * i + 2] = make_float4(0, 0, 0, 0);
     return;
   }
-  F3 a = f3(xyz[3 * ia], xyz[3 * ia + 1], xyz[3 * ia + 2]);
-  F3 b = f3(xyz[3 * ib], xyz[3 * ib + 1], xyz[3 * ib + 2]);
-  F3 c = f3(xyz[3 * ic], xyz[3 * ic + 1], xyz[3 * ic + 2]);
+  const float* X = xyz + 3 * M.vtx_base;
+  F3 a = f3(X[3 * ia], X[3 * ia + 1], X[3 * ia + 2]);
+  F3 b = f3(X[3 * ib], X[3 * ib + 1], X[3 * ib + 2]);
+  F3 c = f3(X[3 * ic], X[3 * ic + 1], X[3 * ic + 2]);
   T[3 * i] = make_float4(a.x, a.y, a.z, 0.f);
   T[3 * i + 1] = make_float4(b.x, b.y, b.z, 0.f);
   T[3 * i + 2] = make_float4(c.x, c.y, c.z, 0.f);
@@ -102,37 +169,36 @@ __global__ void k_gather(const float* __restrict__ xyz, uint64_t nv, const uint3
     cnt = 1;
   } else if (!(ns < 65536.0f)) {
     cnt = 0;
-    atomicExch(&st->error, 4);
+    atomicExch(&S->error, 4);
   } else {
     uint32_t n = uint32_t(ns);
     cnt = n * n;
   }
   nsub[i] = cnt;
-  {
-    unsigned long long wsum = cnt;
-    unsigned mask = __activemask();
-    for (int o = 16; o > 0; o >>= 1) wsum += __shfl_down_sync(mask, wsum, o);
-    if ((threadIdx.x & 31) == __ffs(mask) - 1) atomicAdd(&st->n_sub, wsum);
-  }
+  warp_add(&S->n_sub, cnt, mesh);
   F3 mn = min3(c, min3(a, b)), mx = max3(c, max3(a, b));
   float lo[3] = {mn.x, mn.y, mn.z}, hi[3] = {mx.x, mx.y, mx.z};
+  const unsigned mask = __activemask();
+  const bool uniform = warp_one_mesh(mask, mesh);
   for (int k = 0; k < 3; ++k) {
     float fl = floorf(fmul(lo[k], inv_h)), fh = ceilf(fmul(hi[k], inv_h));
+    int vlo = 0x7fffffff, vhi = -0x7fffffff;  // identities for a lane out of range
     if (!(fabsf(fl) < 1.0e9f) || !(fabsf(fh) < 1.0e9f)) {
-      atomicExch(&st->error, 4);
-      continue;
+      atomicExch(&S->error, 4);
+    } else {
+      vlo = int(fl) - band - 3;
+      vhi = int(fh) + band + 3;
     }
-    atomicMin(&st->vmin[k], int(fl) - band - 3);
-    atomicMax(&st->vmax[k], int(fh) + band + 3);
+    warp_min(&S->vmin[k], vlo, uniform, mask);
+    warp_max(&S->vmax[k], vhi, uniform, mask);
   }
   F3 cen = f3((a.x + b.x + c.x) * (1.0f / 3.0f), (a.y + b.y + c.y) * (1.0f / 3.0f),
               (a.z + b.z + c.z) * (1.0f / 3.0f));
-  atomicMin(&st->cmin[0], f2ord(cen.x));
-  atomicMin(&st->cmin[1], f2ord(cen.y));
-  atomicMin(&st->cmin[2], f2ord(cen.z));
-  atomicMax(&st->cmax[0], f2ord(cen.x));
-  atomicMax(&st->cmax[1], f2ord(cen.y));
-  atomicMax(&st->cmax[2], f2ord(cen.z));
+  const float cc[3] = {cen.x, cen.y, cen.z};
+  for (int k = 0; k < 3; ++k) {
+    warp_min(&S->cmin[k], f2ord(cc[k]), uniform, mask);
+    warp_max(&S->cmax[k], f2ord(cc[k]), uniform, mask);
+  }
 }
 
 __device__ __forceinline__ void widened_box(F3 a, F3 b, F3 c, float inv_h, int band, int lo[3], int hi[3]) {
@@ -151,29 +217,33 @@ __device__ __forceinline__ void widened_box(F3 a, F3 b, F3 c, float inv_h, int b
   }
 }
 
-__device__ __forceinline__ void put_subtri(SubTri* S, uint64_t idx, F3 a, F3 b, F3 c, float inv_h, int band) {
+__device__ __forceinline__ void put_subtri(SubTri* S, uint64_t idx, F3 a, F3 b, F3 c, float inv_h, int band,
+                                           int mesh) {
   int lo[3], hi[3];
   widened_box(a, b, c, inv_h, band, lo, hi);
   SubTri s;
   s.p0 = make_float4(a.x, a.y, a.z, b.x);
   s.p1 = make_float4(b.y, b.z, c.x, c.y);
   s.p2 = make_float4(c.z, 0.f, 0.f, 0.f);
-  s.lo = make_int4(lo[0], lo[1], lo[2], 0);
+  s.lo = make_int4(lo[0], lo[1], lo[2], mesh);
   s.hi = make_int4(hi[0], hi[1], hi[2], 0);
   S[idx] = s;
 }
 
 // mesh_to_volume.rs:75-116, same stepping and accumulation order.
 __global__ void k_subdivide(const float4* __restrict__ T, const uint32_t* __restrict__ nsub,
-                            const uint32_t* __restrict__ off, uint64_t nt, float h, float inv_h, int band,
-                            SubTri* __restrict__ S) {
+                            const uint32_t* __restrict__ off, uint64_t nt, const MeshInfo* __restrict__ mi,
+                            const uint32_t* __restrict__ tri_base, int K, SubTri* __restrict__ S) {
   uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (i >= nt || nsub[i] == 0) return;
+  const int mesh = find_seg(tri_base, K, i);
+  const float h = mi[mesh].h, inv_h = mi[mesh].inv_h;
+  const int band = mi[mesh].band;
   float4 ta = T[3 * i], tb = T[3 * i + 1], tc = T[3 * i + 2];
   F3 p1 = f3(ta.x, ta.y, ta.z), p2 = f3(tb.x, tb.y, tb.z), p3 = f3(tc.x, tc.y, tc.z);
   uint64_t o = off[i];
   if (nsub[i] == 1) {
-    put_subtri(S, o, p1, p2, p3, inv_h, band);
+    put_subtri(S, o, p1, p2, p3, inv_h, band, mesh);
     return;
   }
   F3 e0 = sub3(p2, p1), e1 = sub3(p3, p1), e2 = sub3(p3, p2);
@@ -190,14 +260,14 @@ __global__ void k_subdivide(const float4* __restrict__ T, const uint32_t* __rest
     F3 a_s = add3(a, s2), b_s = add3(b, s2), c_s = add3(c, s2);
     F3 a_prev = a;
     for (uint32_t k = 0; k < r; ++k) {
-      put_subtri(S, o++, a_prev, b_s, a_s, inv_h, band);
-      put_subtri(S, o++, a_s, b_s, c_s, inv_h, band);
+      put_subtri(S, o++, a_prev, b_s, a_s, inv_h, band, mesh);
+      put_subtri(S, o++, a_s, b_s, c_s, inv_h, band, mesh);
       a_prev = a_s;
       a_s = add3(a_s, s2);
       b_s = add3(b_s, s2);
       c_s = add3(c_s, s2);
     }
-    put_subtri(S, o++, a, b, c, inv_h, band);
+    put_subtri(S, o++, a, b, c, inv_h, band, mesh);
     a = add3(a, s1);
   }
 }
@@ -215,31 +285,27 @@ __device__ __forceinline__ bool brick_range(const SubTri& s, const Dir& d, int l
   return lo[0] >= 0 && lo[1] >= 0 && lo[2] >= 0 && hi[0] < d.dx && hi[1] < d.dy && hi[2] < d.dz;
 }
 
-__global__ void k_count_pairs(const SubTri* __restrict__ S, uint64_t ns, Dir d, uint32_t* __restrict__ cnt,
-                              M2VStats* st) {
+__global__ void k_count_pairs(const SubTri* __restrict__ S, uint64_t ns, const Dir* __restrict__ dirs,
+                              const uint64_t* __restrict__ dir_base, uint32_t* __restrict__ cnt, M2VStats* st) {
   uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (i >= ns) return;
   SubTri s = S[i];
+  const int mesh = s.lo.w;
+  const Dir d = dirs[mesh];
+  uint32_t* C = cnt + dir_base[mesh];
   int lo[3], hi[3];
   if (!brick_range(s, d, lo, hi)) {
-    atomicExch(&st->error, 2);
+    atomicExch(&st[mesh].error, 2);
     return;
   }
   for (int x = lo[0]; x <= hi[0]; ++x)
     for (int y = lo[1]; y <= hi[1]; ++y)
       for (int z = lo[2]; z <= hi[2]; ++z)
-        atomicAdd(&cnt[(uint64_t(x) * d.dy + y) * d.dz + z], 1u);
+        atomicAdd(&C[(uint64_t(x) * d.dy + y) * d.dz + z], 1u);
   unsigned long long np = uint64_t(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
   unsigned long long vp = uint64_t(s.hi.x - s.lo.x + 1) * (s.hi.y - s.lo.y + 1) * (s.hi.z - s.lo.z + 1);
-  unsigned mask = __activemask();
-  for (int o = 16; o > 0; o >>= 1) {
-    np += __shfl_down_sync(mask, np, o);
-    vp += __shfl_down_sync(mask, vp, o);
-  }
-  if ((threadIdx.x & 31) == __ffs(mask) - 1) {
-    atomicAdd(&st->n_pairs, np);
-    atomicAdd(&st->n_vpairs, vp);
-  }
+  warp_add(&st[mesh].n_pairs, np, mesh);
+  warp_add(&st[mesh].n_vpairs, vp, mesh);
 }
 
 __global__ void k_dir_flags(const uint32_t* __restrict__ cnt, uint64_t n, uint32_t* __restrict__ flag) {
@@ -248,35 +314,55 @@ __global__ void k_dir_flags(const uint32_t* __restrict__ cnt, uint64_t n, uint32
   if (i == n) flag[n] = 0u;
 }
 
-// Compacts non-empty directory entries into bricks in (x, y, z) order and
-// turns cnt[] into per-entry fill cursors.
+// Compacts non-empty directory entries into bricks in (mesh, x, y, z) order
+// and turns cnt[] into per-entry fill cursors.
 __global__ void k_dir_compact(uint32_t* __restrict__ cnt, const uint32_t* __restrict__ pair_off,
-                              const uint32_t* __restrict__ bidx, uint64_t n, Dir d, int4* __restrict__ origins,
+                              const uint32_t* __restrict__ bidx, uint64_t n, const Dir* __restrict__ dirs,
+                              const uint64_t* __restrict__ dir_base, int K, int4* __restrict__ origins,
                               uint32_t* __restrict__ list_off) {
   uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (e >= n) return;
   if (cnt[e]) {
+    const int mesh = find_seg(dir_base, K, e);
+    const Dir d = dirs[mesh];
+    const uint64_t l = e - dir_base[mesh];
     uint32_t b = bidx[e];
-    int z = int(e % d.dz), y = int((e / d.dz) % d.dy), x = int(e / (uint64_t(d.dz) * d.dy));
+    int z = int(l % d.dz), y = int((l / d.dz) % d.dy), x = int(l / (uint64_t(d.dz) * d.dy));
     origins[b] = make_int4((x + d.bx0) * 8, (y + d.by0) * 8, (z + d.bz0) * 8, 0);
     list_off[b] = pair_off[e];
   }
   cnt[e] = pair_off[e];
 }
 
-__global__ void k_fill_pairs(const SubTri* __restrict__ S, uint64_t ns, Dir d, uint32_t* __restrict__ cursor,
+__global__ void k_fill_pairs(const SubTri* __restrict__ S, uint64_t ns, const Dir* __restrict__ dirs,
+                             const uint64_t* __restrict__ dir_base, uint32_t* __restrict__ cursor,
                              uint32_t* __restrict__ list) {
   uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (i >= ns) return;
   SubTri s = S[i];
+  const int mesh = s.lo.w;
+  const Dir d = dirs[mesh];
+  uint32_t* C = cursor + dir_base[mesh];
   int lo[3], hi[3];
   if (!brick_range(s, d, lo, hi)) return;
   for (int x = lo[0]; x <= hi[0]; ++x)
     for (int y = lo[1]; y <= hi[1]; ++y)
       for (int z = lo[2]; z <= hi[2]; ++z) {
-        uint32_t p = atomicAdd(&cursor[(uint64_t(x) * d.dy + y) * d.dz + z], 1u);
+        uint32_t p = atomicAdd(&C[(uint64_t(x) * d.dy + y) * d.dz + z], 1u);
         list[p] = uint32_t(i);
       }
+}
+
+// Per mesh: first brick (from the directory scan) and first active voxel.
+__global__ void k_seg_starts(const uint32_t* __restrict__ bidx, const uint64_t* __restrict__ dir_base, int K,
+                             uint32_t* __restrict__ leaf_base) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m <= K) leaf_base[m] = bidx[dir_base[m]];
+}
+__global__ void k_act_starts(const uint32_t* __restrict__ voff, const uint32_t* __restrict__ leaf_base, int K,
+                             uint32_t* __restrict__ act_base) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m <= K) act_base[m] = voff[leaf_base[m]];
 }
 
 // ----------------------------------------------- 3. per-brick distances ----
@@ -295,14 +381,16 @@ struct BatchTri {
   float rnyz, rnz;
 };
 
-__global__ void __launch_bounds__(DIST_THREADS) k_brick_distance(
+__global__ void __launch_bounds__(DIST_THREADS, 9) k_brick_distance(
     const int4* __restrict__ origins, const uint32_t* __restrict__ list_off, const uint32_t* __restrict__ list,
-    const SubTri* __restrict__ S, float h, float* __restrict__ values, uint32_t* __restrict__ masks) {
+    const SubTri* __restrict__ S, const MeshInfo* __restrict__ mi, const uint32_t* __restrict__ leaf_base, int K,
+    float* __restrict__ values, uint32_t* __restrict__ masks) {
   __shared__ uint32_t dmin[512];
   __shared__ BatchTri bt[DIST_THREADS / 32][DIST_BATCH];
   __shared__ int pre[DIST_THREADS / 32][DIST_BATCH + 1];
   const int b = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int4 org = origins[b];
+  const float h = mi[find_seg(leaf_base, K, uint64_t(b))].h;
   for (int o = t; o < 512; o += DIST_THREADS) dmin[o] = 0x7f800000u;  // +inf
   __syncthreads();
   const uint32_t beg = list_off[b], end = list_off[b + 1];
@@ -452,10 +540,12 @@ __device__ __forceinline__ uint64_t expand21(uint64_t v) {
   return v;
 }
 
-__global__ void k_morton(const float4* __restrict__ T, uint64_t nt, const M2VStats* st, uint64_t* __restrict__ keys,
+__global__ void k_morton(const float4* __restrict__ T, uint64_t nt, const M2VStats* stats,
+                         const uint32_t* __restrict__ tri_base, int K, uint64_t* __restrict__ keys,
                          uint32_t* __restrict__ vals) {
   uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (i >= nt) return;
+  const M2VStats* st = stats + find_seg(tri_base, K, i);
   float4 a = T[3 * i], b = T[3 * i + 1], c = T[3 * i + 2];
   float cen[3] = {(a.x + b.x + c.x) * (1.0f / 3.0f), (a.y + b.y + c.y) * (1.0f / 3.0f),
                   (a.z + b.z + c.z) * (1.0f / 3.0f)};
@@ -469,6 +559,17 @@ __global__ void k_morton(const float4* __restrict__ T, uint64_t nt, const M2VSta
   }
   keys[i] = (expand21(q[0]) << 2) | (expand21(q[1]) << 1) | expand21(q[2]);
   vals[i] = uint32_t(i);
+}
+
+__global__ void k_mesh_keys(const uint32_t* __restrict__ order, uint64_t nt, const uint32_t* __restrict__ tri_base,
+                            int K, uint32_t* __restrict__ mk) {
+  const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i < nt) mk[i] = uint32_t(find_seg(tri_base, K, order[i]));
+}
+__global__ void k_gather_keys(const uint32_t* __restrict__ order, uint64_t nt, const uint64_t* __restrict__ keys,
+                              uint64_t* __restrict__ out) {
+  const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i < nt) out[i] = keys[order[i]];
 }
 
 __global__ void k_leaves(const float4* __restrict__ T, const uint32_t* __restrict__ order, uint64_t nt,
@@ -514,10 +615,19 @@ __device__ __forceinline__ int delta(const uint64_t* __restrict__ k, int n, int 
 }
 
 // Karras, "Maximizing Parallelism in the Construction of BVHs, Octrees, and
-// k-d Trees" (HPG 2012), with index tie-break for equal codes.
-__global__ void k_karras(const uint64_t* __restrict__ k, int n, int2* __restrict__ child, int* __restrict__ parent) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n - 1) return;
+// k-d Trees" (HPG 2012), with index tie-break for equal codes.  One tree per
+// mesh: mesh m's n_m leaves sit at tri_base[m], its n_m - 1 internal nodes at
+// inode_base[m] = tri_base[m] - m; child and parent indices are local to the
+// mesh (child >= 0 internal, < 0 leaf ~index; parent -1 at the root).
+__global__ void k_karras(const uint64_t* __restrict__ keys, uint64_t n_internal, const uint32_t* __restrict__ tri_base,
+                         const uint32_t* __restrict__ inode_base, int K, int2* __restrict__ child,
+                         int* __restrict__ parent_i, int* __restrict__ parent_l) {
+  const uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (g >= n_internal) return;
+  const int mesh = find_seg(inode_base, K, g);
+  const int i = int(g - inode_base[mesh]);
+  const int n = int(tri_base[mesh + 1] - tri_base[mesh]);
+  const uint64_t* k = keys + tri_base[mesh];
   int d = (delta(k, n, i, i + 1) - delta(k, n, i, i - 1)) >= 0 ? 1 : -1;
   int dmin = delta(k, n, i, i - d);
   int lmax = 2;
@@ -537,10 +647,11 @@ __global__ void k_karras(const uint64_t* __restrict__ k, int n, int2* __restrict
   int lo = min(i, j), hi = max(i, j);
   int left = (lo == gamma) ? ~gamma : gamma;
   int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
-  child[i] = make_int2(left, right);
-  // parent[] holds internal parents: [0, n-1) internal nodes, [n-1, 2n-1) leaves
-  parent[left >= 0 ? left : (n - 1) + ~left] = i;
-  parent[right >= 0 ? right : (n - 1) + ~right] = i;
+  child[g] = make_int2(left, right);
+  if (left >= 0) parent_i[inode_base[mesh] + left] = i;
+  else parent_l[tri_base[mesh] + ~left] = i;
+  if (right >= 0) parent_i[inode_base[mesh] + right] = i;
+  else parent_l[tri_base[mesh] + ~right] = i;
 }
 
 __device__ __forceinline__ void sums_add(Sums& r, const Sums& a, const Sums& b) {
@@ -562,22 +673,27 @@ __device__ __forceinline__ Sums load_sums_cg(const Sums* p) {
 }
 
 // Bottom-up: the second thread to reach a node combines both children.
-__global__ void k_refit(int n, const int2* __restrict__ child, const int* __restrict__ parent,
-                        const Sums* __restrict__ lsum, Sums* __restrict__ isum, int* __restrict__ flags,
-                        float4* __restrict__ inode) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int node = parent[(n - 1) + i];
+__global__ void k_refit(uint64_t nt, const uint32_t* __restrict__ tri_base, const uint32_t* __restrict__ inode_base,
+                        int K, const int2* __restrict__ child, const int* __restrict__ parent_i,
+                        const int* __restrict__ parent_l, const Sums* __restrict__ lsum, Sums* __restrict__ isum,
+                        int* __restrict__ flags, float4* __restrict__ inode) {
+  const uint64_t gl = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (gl >= nt) return;
+  const int mesh = find_seg(tri_base, K, gl);
+  const uint32_t ib = inode_base[mesh], lb = tri_base[mesh];
+  const int n = int(tri_base[mesh + 1] - lb);
+  int node = parent_l[gl];
   for (int guard = 0; node >= 0 && guard < n; ++guard) {
+    const uint64_t gn = ib + uint64_t(node);
     __threadfence();
-    if (atomicAdd(&flags[node], 1) == 0) return;  // first arrival stops
+    if (atomicAdd(&flags[gn], 1) == 0) return;  // first arrival stops
     __threadfence();
-    int2 c = child[node];
-    Sums a = c.x >= 0 ? load_sums_cg(isum + c.x) : lsum[~c.x];
-    Sums b = c.y >= 0 ? load_sums_cg(isum + c.y) : lsum[~c.y];
+    int2 c = child[gn];
+    Sums a = c.x >= 0 ? load_sums_cg(isum + ib + c.x) : lsum[lb + ~c.x];
+    Sums b = c.y >= 0 ? load_sums_cg(isum + ib + c.y) : lsum[lb + ~c.y];
     Sums r;
     sums_add(r, a, b);
-    isum[node] = r;
+    isum[gn] = r;
     float px = r.cx / r.s, py = r.cy / r.s, pz = r.cz / r.s;
     float B[9];
     float p[3] = {px, py, pz}, A[3] = {r.ax, r.ay, r.az};
@@ -585,12 +701,12 @@ __global__ void k_refit(int n, const int2* __restrict__ child, const int* __rest
       for (int q = 0; q < 3; ++q) B[3 * rr + q] = r.m[3 * rr + q] - p[rr] * A[q];
     float d0 = (r.lo[0] - px) * (r.lo[0] - px) + (r.lo[1] - py) * (r.lo[1] - py) + (r.lo[2] - pz) * (r.lo[2] - pz);
     float d1 = (r.hi[0] - px) * (r.hi[0] - px) + (r.hi[1] - py) * (r.hi[1] - py) + (r.hi[2] - pz) * (r.hi[2] - pz);
-    inode[5 * node + 0] = make_float4(px, py, pz, sqrtf(fmaxf(d0, d1)));
-    inode[5 * node + 1] = make_float4(r.ax, r.ay, r.az, B[0] + B[4] + B[8]);
-    inode[5 * node + 2] = make_float4(B[0], B[1], B[2], B[3]);
-    inode[5 * node + 3] = make_float4(B[4], B[5], B[6], B[7]);
-    inode[5 * node + 4] = make_float4(B[8], __int_as_float(c.x), __int_as_float(c.y), 0.f);
-    node = parent[node];
+    inode[5 * gn + 0] = make_float4(px, py, pz, sqrtf(fmaxf(d0, d1)));
+    inode[5 * gn + 1] = make_float4(r.ax, r.ay, r.az, B[0] + B[4] + B[8]);
+    inode[5 * gn + 2] = make_float4(B[0], B[1], B[2], B[3]);
+    inode[5 * gn + 3] = make_float4(B[4], B[5], B[6], B[7]);
+    inode[5 * gn + 4] = make_float4(B[8], __int_as_float(c.x), __int_as_float(c.y), 0.f);
+    node = parent_i[gn];
   }
 }
 
@@ -655,17 +771,51 @@ __device__ __forceinline__ void kahan(float& sum, float& comp, float w) {
   sum = t;
 }
 
-__global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restrict__ act, uint64_t na,
+// Warps are numbered per mesh (warp_base[m] .. warp_base[m+1]) so that a warp
+// never holds voxels of two meshes.
+// The single-mesh instance (MULTI = false) takes its mesh's values from the
+// kernel parameters `one`, so they cost no registers.
+struct WnOne {
+  float h, beta, thresh;
+  int n;
+  uint32_t na;
+};
+
+template <bool MULTI>
+__global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restrict__ act,
+                                                        const uint32_t* __restrict__ act_base,
+                                                        const uint32_t* __restrict__ warp_base, int K,
+                                                        const MeshInfo* __restrict__ mi,
+                                                        const uint32_t* __restrict__ tri_base,
+                                                        const uint32_t* __restrict__ inode_base, WnOne one,
                                                         const int4* __restrict__ origins, float* __restrict__ values,
-                                                        const float4* __restrict__ inode,
-                                                        const float4* __restrict__ leaf, int n, float h, float beta,
-                                                        float thresh, M2VStats* st) {
+                                                        const float4* __restrict__ inodes,
+                                                        const float4* __restrict__ leaves, M2VStats* stats) {
   __shared__ int stk[WN_WARPS][WN_STACK];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const uint64_t i = (blockIdx.x * uint64_t(WN_WARPS) + w) * 32 + lane;
-  if ((blockIdx.x * uint64_t(WN_WARPS) + w) * 32 >= na) return;  // whole warp out of range
-  const bool valid = i < na;
-  const uint32_t v = valid ? act[i] : act[na - 1];
+  const uint64_t gw = blockIdx.x * uint64_t(WN_WARPS) + w;
+  int mesh = 0;
+  uint64_t a0 = 0, a1 = one.na, i = gw * 32 + lane;
+  float h = one.h, beta = one.beta;
+  int n = one.n;
+  const float4* __restrict__ inode = inodes;
+  const float4* __restrict__ leaf = leaves;
+  if (MULTI) {
+    if (gw >= warp_base[K]) return;  // whole warp out of range
+    mesh = find_seg(warp_base, K, gw);
+    a0 = act_base[mesh];
+    a1 = act_base[mesh + 1];
+    i = a0 + (gw - warp_base[mesh]) * 32 + lane;
+    h = mi[mesh].h;
+    beta = mi[mesh].beta;
+    n = int(mi[mesh].n_tri);
+    inode = inodes + 5u * inode_base[mesh];
+    leaf = leaves + 5u * tri_base[mesh];
+  } else if (gw * 32 >= a1) {
+    return;
+  }
+  const bool valid = i < a1;
+  const uint32_t v = valid ? act[i] : act[a1 - 1];
   const uint32_t b = v >> 9, o = v & 511;
   const int4 org = origins[b];
   const F3 q = f3(fmul(__int2float_rn(org.x + int(o >> 6)), h), fmul(__int2float_rn(org.y + int((o >> 3) & 7)), h),
@@ -681,13 +831,13 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restri
     bool have = true;
     ++c_visit;
     if (node >= 0) {
-      const float4 P = inode[5 * node];
+      const float4 P = __ldg(&inode[5 * node]);
       const float rx = P.x - q.x, ry = P.y - q.y, rz = P.z - q.z;
       const float r2 = rx * rx + ry * ry + rz * rz;
       if (__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) {
         ++c_far;
-        const float4 A = inode[5 * node + 1], B0 = inode[5 * node + 2], B1 = inode[5 * node + 3],
-                     B2 = inode[5 * node + 4];
+        const float4 A = __ldg(&inode[5 * node + 1]), B0 = __ldg(&inode[5 * node + 2]), B1 = __ldg(&inode[5 * node + 3]),
+                     B2 = __ldg(&inode[5 * node + 4]);
         // a.r / (4 pi r^3) + trace(B) / (4 pi r^3) - 3 r^T B r / (4 pi r^5)
         const float ri = rsqrtf(r2);
         const float ri2 = ri * ri;
@@ -699,7 +849,7 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restri
         const float rbr = rx * brx + ry * bry + rz * brz;
         wv = inv * ((ar + A.w) - 3.0f * ri2 * rbr);
       } else {
-        const float4 E = inode[5 * node + 4];
+        const float4 E = __ldg(&inode[5 * node + 4]);
         if (sp < WN_STACK) {
           if (lane == 0) stk[w][sp] = __float_as_int(E.z);
           ++sp;
@@ -711,17 +861,17 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restri
       }
     } else {
       const int li = ~node;
-      const float4 P = leaf[5 * li];
+      const float4 P = __ldg(&leaf[5 * li]);
       const float rx = P.x - q.x, ry = P.y - q.y, rz = P.z - q.z;
       const float r2 = rx * rx + ry * ry + rz * rz;
       if (__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) {
         ++c_far;
-        const float4 A = leaf[5 * li + 1];
+        const float4 A = __ldg(&leaf[5 * li + 1]);
         const float ri = rsqrtf(r2);
         wv = (A.x * rx + A.y * ry + A.z * rz) * (ri * ri * ri * (1.0f / FOUR_PI));
       } else {
         ++c_exact;
-        wv = tri_wn(leaf[5 * li + 2], leaf[5 * li + 3], leaf[5 * li + 4], q);
+        wv = tri_wn(__ldg(&leaf[5 * li + 2]), __ldg(&leaf[5 * li + 3]), __ldg(&leaf[5 * li + 4]), q);
       }
     }
     __syncwarp();
@@ -733,6 +883,8 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restri
     }
     __syncwarp();
   }
+  M2VStats* st = stats + mesh;
+  const float thresh = MULTI ? mi[mesh].thresh : one.thresh;
   if (overflow && lane == 0) atomicExch(&st->error, 3);
   if (lane == 0) {
     atomicAdd(&st->wn_visits, (unsigned long long)c_visit);
@@ -748,156 +900,381 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restri
 // ------------------------------------------------------------ driver ------
 static inline unsigned blocks(uint64_t n, unsigned t) { return unsigned((n + t - 1) / t); }
 
-bs_volume* mesh_to_volume_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
-                               const bs_m2v_params& p) {
-  if (nt == 0) fail(BS_ERR_EMPTY, "mesh has no triangles");
-  if (nt >= (1ull << 31)) fail(BS_ERR_CAPACITY, "more than 2^31 triangles");
-  if (!(p.voxel_size > 0.f) || !std::isfinite(p.voxel_size)) fail(BS_ERR_INVALID_ARG, "voxel_size must be > 0");
-  if (p.band_width < 0 || p.band_width > 1000000) fail(BS_ERR_INVALID_ARG, "band_width out of range");
-  cudaStream_t s = ctx->stream;
-  const float h = p.voxel_size;
-  const float inv_h = 1.0f / h;  // mesh_to_volume.rs:48 (reciprocal, then multiply)
-  const int band = p.band_width;
+// One set of launches for a batch of meshes (the single-mesh call is a batch
+// of one).  Every kernel covers all meshes' triangles, bricks or voxels and
+// finds its mesh by a binary search of the per-mesh offsets; host syncs do
+// not grow with the number of meshes.  Meshes without triangles get no
+// volume (nullptr), as MeshToVolume::convert returns None for them.
+struct SplitDst {
+  int4* o;
+  float* v;
+  uint32_t* m;
+};
 
-  DBuf<M2VStats> st(ctx, 1);
-  M2VStats init{};
-  for (int k = 0; k < 3; ++k) {
-    init.vmin[k] = 0x7fffffff;
-    init.vmax[k] = -0x7fffffff;
-    init.cmin[k] = 0xffffffffu;
-    init.cmax[k] = 0u;
+__global__ void k_split(const uint32_t* __restrict__ leaf_base, int K, const SplitDst* __restrict__ dst,
+                        const int4* __restrict__ oi, const float* __restrict__ vi, const uint32_t* __restrict__ mi_,
+                        uint64_t nb) {
+  const uint64_t b = blockIdx.x;
+  if (b >= nb) return;
+  const int mesh = find_seg(leaf_base, K, b);
+  const uint64_t d = b - leaf_base[mesh];
+  const SplitDst D = dst[mesh];
+  reinterpret_cast<float4*>(D.v + d * 512)[threadIdx.x] = reinterpret_cast<const float4*>(vi + b * 512)[threadIdx.x];
+  if (threadIdx.x < 16) D.m[d * 16 + threadIdx.x] = mi_[b * 16 + threadIdx.x];
+  if (threadIdx.x == 0) D.o[d] = oi[b];
+}
+
+// A batch over one of the per-call limits: each mesh's share of the limit.
+struct SplitNeeded {
+  std::vector<double> share;  // indexed like the batch's meshes
+};
+
+// Throws SplitNeeded (several meshes) or BS_ERR_CAPACITY (one mesh) when the
+// per-mesh quantities q exceed `limit` in total.
+static void check_limit(const std::vector<uint64_t>& q, const std::vector<int>& which, size_t K_all, double limit,
+                        const char* what) {
+  double total = 0;
+  for (uint64_t v : q) total += double(v);
+  if (total < limit) return;
+  if (q.size() == 1) fail(BS_ERR_CAPACITY, what);
+  SplitNeeded sn;
+  sn.share.assign(K_all, 0.0);
+  for (size_t m = 0; m < q.size(); ++m) sn.share[size_t(which[m])] = double(q[m]) / limit;
+  throw sn;
+}
+
+static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const uint32_t* d_tri,
+                                          const std::vector<uint64_t>& n_vtx, const std::vector<uint64_t>& n_tri,
+                                          const std::vector<bs_m2v_params>& params);
+
+std::vector<bs_volume*> mesh_to_volume_batch_impl(bs_ctx* ctx, const float* d_xyz, const uint32_t* d_tri,
+                                                  const std::vector<uint64_t>& n_vtx,
+                                                  const std::vector<uint64_t>& n_tri,
+                                                  const std::vector<bs_m2v_params>& params) {
+  const size_t K = n_tri.size();
+  if (n_vtx.size() != K || params.size() != K) fail(BS_ERR_INVALID_ARG, "batch arrays differ in length");
+  try {
+    return batch_core(ctx, d_xyz, d_tri, n_vtx, n_tri, params);
+  } catch (const SplitNeeded& sn) {
+    // pack consecutive meshes into chunks holding at most half of the limit
+    // and run each chunk on its own (recursively, in case another limit bites)
+    std::vector<bs_volume*> out;
+    out.reserve(K);
+    size_t beg = 0;
+    uint64_t vtx_off = 0, tri_off = 0;
+    try {
+      while (beg < K) {
+        size_t end = beg;
+        double acc = 0.0;
+        do {
+          acc += sn.share[end];
+          ++end;
+        } while (end < K && acc + sn.share[end] <= 0.5);
+        std::vector<uint64_t> v(n_vtx.begin() + beg, n_vtx.begin() + end), t(n_tri.begin() + beg, n_tri.begin() + end);
+        std::vector<bs_m2v_params> p(params.begin() + beg, params.begin() + end);
+        std::vector<bs_volume*> part;
+        bool any = false;
+        for (uint64_t x : t) any |= x != 0;
+        if (any) part = mesh_to_volume_batch_impl(ctx, d_xyz + 3 * vtx_off, d_tri + 3 * tri_off, v, t, p);
+        else part.assign(t.size(), nullptr);
+        out.insert(out.end(), part.begin(), part.end());
+        for (size_t m = beg; m < end; ++m) {
+          vtx_off += n_vtx[m];
+          tri_off += n_tri[m];
+        }
+        beg = end;
+      }
+    } catch (...) {
+      for (bs_volume* v : out)
+        if (v) volume_release(v);
+      throw;
+    }
+    return out;
   }
-  BS_CUDA(cudaMemcpyAsync(st.p, &init, sizeof init, cudaMemcpyHostToDevice, s));
+}
+
+static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const uint32_t* d_tri,
+                                          const std::vector<uint64_t>& n_vtx, const std::vector<uint64_t>& n_tri,
+                                          const std::vector<bs_m2v_params>& params) {
+  const size_t K_all = n_tri.size();
+  std::vector<bs_volume*> result(K_all, nullptr);
+  // meshes with triangles, in order
+  std::vector<int> which;
+  std::vector<MeshInfo> mi;
+  std::vector<uint32_t> tri_base(1, 0);
+  uint64_t vtx_at = 0, tri_at = 0, nt = 0;
+  for (size_t m = 0; m < K_all; ++m) {
+    const bs_m2v_params& p = params[m];
+    if (!(p.voxel_size > 0.f) || !std::isfinite(p.voxel_size)) fail(BS_ERR_INVALID_ARG, "voxel_size must be > 0");
+    if (p.band_width < 0 || p.band_width > 1000000) fail(BS_ERR_INVALID_ARG, "band_width out of range");
+    if (n_tri[m]) {
+      MeshInfo q{};
+      q.h = p.voxel_size;
+      q.inv_h = 1.0f / p.voxel_size;  // mesh_to_volume.rs:48 (reciprocal, then multiply)
+      q.beta = p.wn_beta;
+      q.thresh = p.wn_threshold;
+      q.band = p.band_width;
+      q.tri_base = uint32_t(tri_at);
+      q.n_tri = uint32_t(n_tri[m]);
+      q.vtx_base = vtx_at;
+      q.n_vtx = n_vtx[m];
+      mi.push_back(q);
+      which.push_back(int(m));
+      nt += n_tri[m];
+      if (nt >= (1ull << 31)) fail(BS_ERR_CAPACITY, "more than 2^31 triangles");
+      tri_base.push_back(uint32_t(nt));
+    }
+    vtx_at += n_vtx[m];
+    tri_at += n_tri[m];
+  }
+  const int K = int(mi.size());
+  if (K == 0) fail(BS_ERR_EMPTY, "mesh has no triangles");
+  cudaStream_t s = ctx->stream;
+
+  // per-mesh tables on the device: MeshInfo[K], tri_base[K+1], inode_base[K+1]
+  std::vector<uint32_t> inode_base(K + 1);
+  for (int m = 0; m <= K; ++m) inode_base[m] = tri_base[m] - uint32_t(m);
+  DBuf<MeshInfo> d_mi(ctx, K);
+  DBuf<uint32_t> d_tb(ctx, K + 1), d_ib(ctx, K + 1);
+  BS_CUDA(cudaMemcpyAsync(d_mi.p, mi.data(), K * sizeof(MeshInfo), cudaMemcpyHostToDevice, s));
+  BS_CUDA(cudaMemcpyAsync(d_tb.p, tri_base.data(), (K + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+  BS_CUDA(cudaMemcpyAsync(d_ib.p, inode_base.data(), (K + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+
+  DBuf<M2VStats> st(ctx, K);
+  std::vector<M2VStats> hst(K);
+  {
+    M2VStats init{};
+    for (int k = 0; k < 3; ++k) {
+      init.vmin[k] = 0x7fffffff;
+      init.vmax[k] = -0x7fffffff;
+      init.cmin[k] = 0xffffffffu;
+      init.cmax[k] = 0u;
+    }
+    std::fill(hst.begin(), hst.end(), init);
+    BS_CUDA(cudaMemcpyAsync(st.p, hst.data(), K * sizeof(M2VStats), cudaMemcpyHostToDevice, s));
+  }
 
   DBuf<float4> T(ctx, 3 * nt);
   DBuf<uint32_t> nsub(ctx, nt + 1), soff(ctx, nt + 1);
-  BS_KERNEL(ctx, "k_gather", (k_gather<<<blocks(nt + 1, 256), 256, 0, s>>>(d_xyz, nv, d_tri, nt, h, inv_h, band, T.p, nsub.p, st.p)));
+  BS_KERNEL(ctx, "k_gather", (k_gather<<<blocks(nt + 1, 256), 256, 0, s>>>(d_xyz, d_tri, nt, d_mi.p, d_tb.p, K, T.p, nsub.p, st.p)));
   exclusive_scan(ctx, nsub.p, soff.p, nt + 1);
-
-  struct {
-    M2VStats st;
-    uint32_t total;
-  } hb;
-  read_back(ctx, &hb.st, st.p, sizeof(M2VStats));
-  read_back(ctx, &hb.total, soff.p + nt, sizeof(uint32_t));
-  if (hb.st.error == 1) fail(BS_ERR_INVALID_ARG, "triangle vertex index out of range");
-  if (hb.st.error == 4) fail(BS_ERR_CAPACITY, "coordinates / voxel size exceed the int32 voxel grid");
-  for (int k = 0; k < 3; ++k)  // leaf keys pack 21 bits per axis of origin / 8
-    if (hb.st.vmin[k] < -(1 << 23) + 64 || hb.st.vmax[k] > (1 << 23) - 64)
-      fail(BS_ERR_CAPACITY, "mesh extent / voxel size exceeds +-2^23 voxels per axis");
+  uint32_t total = 0;
+  read_back(ctx, hst.data(), st.p, K * sizeof(M2VStats));
+  read_back(ctx, &total, soff.p + nt, sizeof(uint32_t));
+  std::vector<uint64_t> q_sub(K), q_dir(K);
+  std::vector<Dir> dirs(K);
+  std::vector<uint64_t> dir_base(K + 1, 0);
+  for (int m = 0; m < K; ++m) {
+    const M2VStats& q = hst[m];
+    if (q.error == 1) fail(BS_ERR_INVALID_ARG, "triangle vertex index out of range");
+    if (q.error == 4) fail(BS_ERR_CAPACITY, "coordinates / voxel size exceed the int32 voxel grid");
+    for (int k = 0; k < 3; ++k)  // leaf keys pack 21 bits per axis of origin / 8
+      if (q.vmin[k] < -(1 << 23) + 64 || q.vmax[k] > (1 << 23) - 64)
+        fail(BS_ERR_CAPACITY, "mesh extent / voxel size exceeds +-2^23 voxels per axis");
+    q_sub[m] = q.n_sub;
+    Dir& d = dirs[m];
+    d.bx0 = q.vmin[0] >> 3; d.by0 = q.vmin[1] >> 3; d.bz0 = q.vmin[2] >> 3;
+    d.dx = (q.vmax[0] >> 3) - d.bx0 + 1;
+    d.dy = (q.vmax[1] >> 3) - d.by0 + 1;
+    d.dz = (q.vmax[2] >> 3) - d.bz0 + 1;
+    q_dir[m] = uint64_t(d.dx) * d.dy * d.dz;
+    dir_base[m + 1] = dir_base[m] + q_dir[m];
+  }
   // count of sub-triangles in 64 bit: nsub sums can wrap in uint32
-  if (hb.st.n_sub >= (1ull << 32)) fail(BS_ERR_CAPACITY, "more than 2^32 sub-triangles");
-  const uint64_t ns = hb.total;
+  check_limit(q_sub, which, K_all, 4294967296.0, "more than 2^32 sub-triangles");
+  check_limit(q_dir, which, K_all, 4294967294.0, "brick directory exceeds 2^32 entries");
+  const uint64_t ns = total;
   if (ns == 0) fail(BS_ERR_EMPTY, "no sub-triangles");
-
-  Dir d;
-  d.bx0 = hb.st.vmin[0] >> 3; d.by0 = hb.st.vmin[1] >> 3; d.bz0 = hb.st.vmin[2] >> 3;
-  d.dx = (hb.st.vmax[0] >> 3) - d.bx0 + 1;
-  d.dy = (hb.st.vmax[1] >> 3) - d.by0 + 1;
-  d.dz = (hb.st.vmax[2] >> 3) - d.bz0 + 1;
-  const uint64_t D = uint64_t(d.dx) * d.dy * d.dz;
-  if (D >= (1ull << 32) - 2) fail(BS_ERR_CAPACITY, "brick directory exceeds 2^32 entries");
+  const uint64_t D = dir_base[K];
+  DBuf<Dir> d_dirs(ctx, K);
+  DBuf<uint64_t> d_db(ctx, K + 1);
+  BS_CUDA(cudaMemcpyAsync(d_dirs.p, dirs.data(), K * sizeof(Dir), cudaMemcpyHostToDevice, s));
+  BS_CUDA(cudaMemcpyAsync(d_db.p, dir_base.data(), (K + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
 
   DBuf<SubTri> S(ctx, ns);
-  BS_KERNEL(ctx, "k_subdivide", (k_subdivide<<<blocks(nt, 128), 128, 0, s>>>(T.p, nsub.p, soff.p, nt, h, inv_h, band, S.p)));
+  BS_KERNEL(ctx, "k_subdivide", (k_subdivide<<<blocks(nt, 128), 128, 0, s>>>(T.p, nsub.p, soff.p, nt, d_mi.p, d_tb.p, K, S.p)));
   nsub.reset();
   soff.reset();
 
   DBuf<uint32_t> cnt(ctx, D + 1), pair_off(ctx, D + 1), flag(ctx, D + 1), bidx(ctx, D + 1);
   BS_CUDA(cudaMemsetAsync(cnt.p, 0, (D + 1) * sizeof(uint32_t), s));
-  BS_KERNEL(ctx, "k_count_pairs", (k_count_pairs<<<blocks(ns, 256), 256, 0, s>>>(S.p, ns, d, cnt.p, st.p)));
+  BS_KERNEL(ctx, "k_count_pairs", (k_count_pairs<<<blocks(ns, 256), 256, 0, s>>>(S.p, ns, d_dirs.p, d_db.p, cnt.p, st.p)));
   exclusive_scan(ctx, cnt.p, pair_off.p, D + 1);
   BS_KERNEL(ctx, "k_dir_flags", (k_dir_flags<<<blocks(D + 1, 256), 256, 0, s>>>(cnt.p, D, flag.p)));
   exclusive_scan(ctx, flag.p, bidx.p, D + 1);
+  DBuf<uint32_t> leaf_base(ctx, K + 1), act_base(ctx, K + 1);
+  BS_KERNEL(ctx, "k_seg_starts", (k_seg_starts<<<blocks(K + 1, 128), 128, 0, s>>>(bidx.p, d_db.p, K, leaf_base.p)));
   uint32_t nb_np[2];
   read_back(ctx, &nb_np[0], bidx.p + D, sizeof(uint32_t));
   read_back(ctx, &nb_np[1], pair_off.p + D, sizeof(uint32_t));
-  read_back(ctx, &hb.st, st.p, sizeof(M2VStats));
-  if (hb.st.error == 2) fail(BS_ERR_CAPACITY, "sub-triangle outside the brick directory");
-  if (hb.st.n_pairs >= (1ull << 32)) fail(BS_ERR_CAPACITY, "more than 2^32 brick/sub-triangle pairs");
+  read_back(ctx, hst.data(), st.p, K * sizeof(M2VStats));
+  std::vector<uint64_t> q_pairs(K);
+  for (int m = 0; m < K; ++m) {
+    if (hst[m].error == 2) fail(BS_ERR_CAPACITY, "sub-triangle outside the brick directory");
+    q_pairs[m] = hst[m].n_pairs;
+  }
+  check_limit(q_pairs, which, K_all, 4294967296.0, "more than 2^32 brick/sub-triangle pairs");
   const uint64_t nb = nb_np[0], np = nb_np[1];
+  if (nb >= (1ull << 23)) {  // active voxels are listed as brick << 9 | voxel in 32 bits
+    std::vector<uint32_t> lb(K + 1);
+    read_back(ctx, lb.data(), leaf_base.p, (K + 1) * sizeof(uint32_t));
+    std::vector<uint64_t> q_bricks(K);
+    for (int m = 0; m < K; ++m) q_bricks[m] = lb[m + 1] - lb[m];
+    check_limit(q_bricks, which, K_all, 8388608.0, "more than 2^23 bricks in one call");
+  }
   flag.reset();
 
-  bs_volume* vol = new bs_volume(ctx);
-  vol->h = h;
-  try {
-    vol->n_leaves = nb;
-    vol->d_origins = dalloc<int4>(ctx, nb);
-    vol->d_values = dalloc<float>(ctx, nb * 512);
-    vol->d_masks = dalloc<uint32_t>(ctx, nb * 16);
+  DBuf<int4> origins(ctx, nb);
+  DBuf<float> values(ctx, nb * 512);
+  DBuf<uint32_t> masks(ctx, nb * 16);
+  {
     DBuf<uint32_t> list_off(ctx, nb + 1), list(ctx, np);
-    BS_KERNEL(ctx, "k_dir_compact", (k_dir_compact<<<blocks(D, 256), 256, 0, s>>>(cnt.p, pair_off.p, bidx.p, D, d, vol->d_origins, list_off.p)));
+    BS_KERNEL(ctx, "k_dir_compact", (k_dir_compact<<<blocks(D, 256), 256, 0, s>>>(cnt.p, pair_off.p, bidx.p, D, d_dirs.p, d_db.p, K, origins.p, list_off.p)));
     BS_CUDA(cudaMemcpyAsync(list_off.p + nb, pair_off.p + D, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
     pair_off.reset();
     bidx.reset();
-    BS_KERNEL(ctx, "k_fill_pairs", (k_fill_pairs<<<blocks(ns, 256), 256, 0, s>>>(S.p, ns, d, cnt.p, list.p)));
+    BS_KERNEL(ctx, "k_fill_pairs", (k_fill_pairs<<<blocks(ns, 256), 256, 0, s>>>(S.p, ns, d_dirs.p, d_db.p, cnt.p, list.p)));
     cnt.reset();
-    BS_KERNEL(ctx, "k_brick_distance", (k_brick_distance<<<unsigned(nb), DIST_THREADS, 0, s>>>(vol->d_origins, list_off.p, list.p, S.p, h,
-                                                          vol->d_values, vol->d_masks)));
-    list.reset();
-    list_off.reset();
-    S.reset();
+    BS_KERNEL(ctx, "k_brick_distance", (k_brick_distance<<<unsigned(nb), DIST_THREADS, 0, s>>>(origins.p, list_off.p, list.p, S.p, d_mi.p,
+                                                          leaf_base.p, K, values.p, masks.p)));
+  }
+  S.reset();
 
-    // active voxels
-    DBuf<uint32_t> vc(ctx, nb + 1), voff(ctx, nb + 1);
-    BS_KERNEL(ctx, "k_brick_popcount", (k_brick_popcount<<<blocks(nb + 1, 256), 256, 0, s>>>(vol->d_masks, nb, vc.p)));
-    exclusive_scan(ctx, vc.p, voff.p, nb + 1);
-    uint32_t na32 = 0;
-    read_back(ctx, &na32, voff.p + nb, sizeof(uint32_t));
-    const uint64_t na = na32;
-    vol->n_active = na;
-    DBuf<uint32_t> act(ctx, na);
-    BS_KERNEL(ctx, "k_emit_active", (k_emit_active<<<blocks(nb * 32, 256), 256, 0, s>>>(vol->d_masks, voff.p, nb, act.p)));
-    vc.reset();
-    voff.reset();
+  // active voxels, and per mesh its first brick / voxel
+  DBuf<uint32_t> vc(ctx, nb + 1), voff(ctx, nb + 1);
+  BS_KERNEL(ctx, "k_brick_popcount", (k_brick_popcount<<<blocks(nb + 1, 256), 256, 0, s>>>(masks.p, nb, vc.p)));
+  exclusive_scan(ctx, vc.p, voff.p, nb + 1);
+  BS_KERNEL(ctx, "k_act_starts", (k_act_starts<<<blocks(K + 1, 128), 128, 0, s>>>(voff.p, leaf_base.p, K, act_base.p)));
+  std::vector<uint32_t> h_leaf_base(K + 1), h_act_base(K + 1);
+  read_back(ctx, h_leaf_base.data(), leaf_base.p, (K + 1) * sizeof(uint32_t));
+  read_back(ctx, h_act_base.data(), act_base.p, (K + 1) * sizeof(uint32_t));
+  const uint64_t na = h_act_base[K];
+  std::vector<uint32_t> warp_base(K + 1, 0);
+  for (int m = 0; m < K; ++m) warp_base[m + 1] = warp_base[m] + (h_act_base[m + 1] - h_act_base[m] + 31) / 32;
+  DBuf<uint32_t> d_wb(ctx, K + 1);
+  BS_CUDA(cudaMemcpyAsync(d_wb.p, warp_base.data(), (K + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+  DBuf<uint32_t> act(ctx, std::max<uint64_t>(na, 1));
+  BS_KERNEL(ctx, "k_emit_active", (k_emit_active<<<blocks(nb * 32, 256), 256, 0, s>>>(masks.p, voff.p, nb, act.p)));
+  vc.reset();
+  voff.reset();
 
-    // LBVH over the original triangles
-    const int n = int(nt);
-    DBuf<uint64_t> keys(ctx, nt), keys2(ctx, nt);
-    DBuf<uint32_t> vals(ctx, nt), order(ctx, nt);
-    BS_KERNEL(ctx, "k_morton", (k_morton<<<blocks(nt, 256), 256, 0, s>>>(T.p, nt, st.p, keys.p, vals.p)));
-    {
-      size_t tmp = 0;
-      BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, keys.p, keys2.p, vals.p, order.p, int(nt), 0, 64, s));
-      DBuf<uint8_t> t(ctx, tmp);
-      BS_CUDA(cub::DeviceRadixSort::SortPairs(t.p, tmp, keys.p, keys2.p, vals.p, order.p, int(nt), 0, 64, s));
+  // LBVH per mesh over its original triangles
+  DBuf<uint64_t> keys(ctx, nt), keys2(ctx, nt);
+  DBuf<uint32_t> vals(ctx, nt), order(ctx, nt);
+  BS_KERNEL(ctx, "k_morton", (k_morton<<<blocks(nt, 256), 256, 0, s>>>(T.p, nt, st.p, d_tb.p, K, keys.p, vals.p)));
+  {
+    size_t tmp = 0;
+    BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, keys.p, keys2.p, vals.p, order.p, int(nt), 0, 64, s));
+    DBuf<uint8_t> t(ctx, tmp);
+    BS_CUDA(cub::DeviceRadixSort::SortPairs(t.p, tmp, keys.p, keys2.p, vals.p, order.p, int(nt), 0, 64, s));
+  }
+  if (K > 1) {
+    // stable second pass by mesh: every mesh keeps its full-precision Morton
+    // order, so its tree is the one a call for that mesh alone would build
+    int mesh_bits = 1;
+    while ((1 << mesh_bits) < K) ++mesh_bits;
+    DBuf<uint32_t> mk(ctx, nt), mk2(ctx, nt), order2(ctx, nt);
+    BS_KERNEL(ctx, "k_mesh_keys", (k_mesh_keys<<<blocks(nt, 256), 256, 0, s>>>(order.p, nt, d_tb.p, K, mk.p)));
+    size_t tmp = 0;
+    BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, mk.p, mk2.p, order.p, order2.p, int(nt), 0, mesh_bits, s));
+    DBuf<uint8_t> t(ctx, tmp);
+    BS_CUDA(cub::DeviceRadixSort::SortPairs(t.p, tmp, mk.p, mk2.p, order.p, order2.p, int(nt), 0, mesh_bits, s));
+    BS_KERNEL(ctx, "k_gather_keys", (k_gather_keys<<<blocks(nt, 256), 256, 0, s>>>(order2.p, nt, keys.p, keys2.p)));
+    std::swap(order.p, order2.p);
+  }
+  keys.reset();
+  vals.reset();
+  const uint64_t n_int = nt - uint64_t(K);
+  DBuf<float4> leaf(ctx, 5 * nt), inode(ctx, 5 * std::max<uint64_t>(n_int, 1));
+  DBuf<Sums> lsum(ctx, nt), isum(ctx, std::max<uint64_t>(n_int, 1));
+  BS_KERNEL(ctx, "k_leaves", (k_leaves<<<blocks(nt, 256), 256, 0, s>>>(T.p, order.p, nt, leaf.p, lsum.p)));
+  {
+    DBuf<int2> child(ctx, std::max<uint64_t>(n_int, 1));
+    DBuf<int> parent_i(ctx, std::max<uint64_t>(n_int, 1)), parent_l(ctx, nt), flags(ctx, std::max<uint64_t>(n_int, 1));
+    BS_CUDA(cudaMemsetAsync(parent_l.p, 0xff, nt * sizeof(int), s));  // single-triangle meshes: no parent
+    if (n_int) {
+      BS_CUDA(cudaMemsetAsync(flags.p, 0, n_int * sizeof(int), s));
+      BS_CUDA(cudaMemsetAsync(parent_i.p, 0xff, n_int * sizeof(int), s));  // roots keep -1
+      BS_KERNEL(ctx, "k_karras", (k_karras<<<blocks(n_int, 256), 256, 0, s>>>(keys2.p, n_int, d_tb.p, d_ib.p, K, child.p, parent_i.p, parent_l.p)));
+      BS_KERNEL(ctx, "k_refit", (k_refit<<<blocks(nt, 256), 256, 0, s>>>(nt, d_tb.p, d_ib.p, K, child.p, parent_i.p, parent_l.p, lsum.p, isum.p,
+                                                                      flags.p, inode.p)));
     }
-    keys.reset();
-    vals.reset();
-    DBuf<float4> leaf(ctx, 5 * nt), inode(ctx, 5 * std::max<uint64_t>(nt - 1, 1));
-    DBuf<Sums> lsum(ctx, nt), isum(ctx, std::max<uint64_t>(nt - 1, 1));
-    BS_KERNEL(ctx, "k_leaves", (k_leaves<<<blocks(nt, 256), 256, 0, s>>>(T.p, order.p, nt, leaf.p, lsum.p)));
-    if (n > 1) {
-      DBuf<int2> child(ctx, nt - 1);
-      DBuf<int> parent(ctx, 2 * nt - 1), flags(ctx, nt - 1);
-      BS_CUDA(cudaMemsetAsync(flags.p, 0, (nt - 1) * sizeof(int), s));
-      BS_CUDA(cudaMemsetAsync(parent.p, 0xff, sizeof(int), s));  // root has no parent
-      BS_KERNEL(ctx, "k_karras", (k_karras<<<blocks(nt - 1, 256), 256, 0, s>>>(keys2.p, n, child.p, parent.p)));
-      BS_KERNEL(ctx, "k_refit", (k_refit<<<blocks(nt, 256), 256, 0, s>>>(n, child.p, parent.p, lsum.p, isum.p, flags.p, inode.p)));
+  }
+  keys2.reset();
+  order.reset();
+  lsum.reset();
+  isum.reset();
+  T.reset();
+  if (na > 0) {
+    const uint64_t n_warps = warp_base[K];
+    WnOne one{mi[0].h, mi[0].beta, mi[0].thresh, int(mi[0].n_tri), uint32_t(na)};
+    if (K == 1)
+      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<false><<<blocks(n_warps, WN_WARPS), WN_THREADS, 0, s>>>(act.p, act_base.p, d_wb.p, K, d_mi.p, d_tb.p,
+                                                                                    d_ib.p, one, origins.p, values.p, inode.p, leaf.p, st.p)));
+    else
+      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<true><<<blocks(n_warps, WN_WARPS), WN_THREADS, 0, s>>>(act.p, act_base.p, d_wb.p, K, d_mi.p, d_tb.p,
+                                                                                   d_ib.p, one, origins.p, values.p, inode.p, leaf.p, st.p)));
+  }
+  read_back(ctx, hst.data(), st.p, K * sizeof(M2VStats));
+  uint64_t n_vp = 0, n_p = 0, visits = 0, far = 0, exact = 0;
+  for (int m = 0; m < K; ++m) {
+    if (hst[m].error == 3) fail(BS_ERR_CAPACITY, "winding-number traversal stack overflow");
+    n_vp += hst[m].n_vpairs;
+    n_p += hst[m].n_pairs;
+    visits += hst[m].wn_visits;
+    far += hst[m].wn_far;
+    exact += hst[m].wn_exact;
+  }
+  ctx->last_stats[0] = nt;
+  ctx->last_stats[1] = ns;
+  ctx->last_stats[2] = n_p;
+  ctx->last_stats[3] = n_vp;
+  ctx->last_stats[4] = nb;
+  ctx->last_stats[5] = na;
+  ctx->last_stats[6] = visits;
+  ctx->last_stats[7] = (far & 0xffffffffull) | (exact << 32);
+
+  // hand out the volumes
+  std::vector<bs_volume*> vols(K, nullptr);
+  try {
+    for (int m = 0; m < K; ++m) {
+      vols[m] = new bs_volume(ctx);
+      vols[m]->h = mi[m].h;
+      vols[m]->n_leaves = h_leaf_base[m + 1] - h_leaf_base[m];
+      vols[m]->n_active = h_act_base[m + 1] - h_act_base[m];
     }
-    keys2.reset();
-    order.reset();
-    lsum.reset();
-    isum.reset();
-    if (na > 0) {
-      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<<<blocks(na, WN_THREADS), WN_THREADS, 0, s>>>(act.p, na, vol->d_origins, vol->d_values, inode.p, leaf.p, n, h,
-                                                p.wn_beta, p.wn_threshold, st.p)));
+    if (K == 1) {
+      vols[0]->d_origins = origins.release();
+      vols[0]->d_values = values.release();
+      vols[0]->d_masks = masks.release();
+    } else {
+      std::vector<SplitDst> dst(K);
+      for (int m = 0; m < K; ++m) {
+        const uint64_t n = std::max<uint64_t>(vols[m]->n_leaves, 1);
+        vols[m]->d_origins = dalloc<int4>(ctx, n);
+        vols[m]->d_values = dalloc<float>(ctx, n * 512);
+        vols[m]->d_masks = dalloc<uint32_t>(ctx, n * 16);
+        dst[m] = SplitDst{vols[m]->d_origins, vols[m]->d_values, vols[m]->d_masks};
+      }
+      DBuf<SplitDst> d_dst(ctx, K);
+      BS_CUDA(cudaMemcpyAsync(d_dst.p, dst.data(), K * sizeof(SplitDst), cudaMemcpyHostToDevice, s));
+      if (nb)
+        BS_KERNEL(ctx, "k_split", (k_split<<<unsigned(nb), 128, 0, s>>>(leaf_base.p, K, d_dst.p, origins.p, values.p, masks.p, nb)));
+      BS_CUDA(cudaStreamSynchronize(s));  // the pointer table leaves scope
     }
-    read_back(ctx, &hb.st, st.p, sizeof(M2VStats));
-    if (hb.st.error == 3) fail(BS_ERR_CAPACITY, "winding-number traversal stack overflow");
-    ctx->last_stats[0] = nt;
-    ctx->last_stats[1] = ns;
-    ctx->last_stats[2] = hb.st.n_pairs;
-    ctx->last_stats[3] = hb.st.n_vpairs;
-    ctx->last_stats[4] = nb;
-    ctx->last_stats[5] = na;
-    ctx->last_stats[6] = hb.st.wn_visits;
-    ctx->last_stats[7] = (hb.st.wn_far & 0xffffffffull) | (hb.st.wn_exact << 32);
   } catch (...) {
-    volume_release(vol);
+    for (bs_volume* v : vols)
+      if (v) volume_release(v);
     throw;
   }
-  return vol;
+  for (int m = 0; m < K; ++m) result[size_t(which[m])] = vols[m];
+  return result;
+}
+
+bs_volume* mesh_to_volume_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
+                               const bs_m2v_params& p) {
+  if (nt == 0) fail(BS_ERR_EMPTY, "mesh has no triangles");
+  return mesh_to_volume_batch_impl(ctx, d_xyz, d_tri, {nv}, {nt}, {p})[0];
 }
 
 }  // namespace bs

@@ -13,6 +13,11 @@ numpy's PCG64 generator (numpy.random.default_rng):
   gradient_noise(p, seed)
       3-D gradient (Perlin-style) noise in roughly [-1, 1]: a seeded 256-entry
       permutation, 12 edge gradients, quintic fade, trilinear blend.
+  uneven_batch(n, seed)
+      n meshes alternating icospheres and displaced tori, triangle counts
+      log-uniform in [1k, 500k] (icospheres take the nearest subdivision),
+      noise amplitude uniform in [0.01, 0.1], and a voxel size that makes the
+      bounding grid log-uniform between 64^3 and 512^3.
 All triangles are oriented with outward normals.
 """
 import numpy as np
@@ -122,3 +127,22 @@ def config2(seed=2, nu=1024, nv=512):
     a = torus(1.0, 0.3, nu, nv, 0.02, seed)
     b = torus(1.0, 0.3, nu, nv, 0.02, seed + 1, rotate_x_deg=90.0, shift=(0.5, 0.0, 0.0))
     return a, b
+
+
+def uneven_batch(n=256, seed=4):
+    """[(vertices, triangles, voxel_size)] of the batched workload (band 3)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        target = float(np.exp(rng.uniform(np.log(1000.0), np.log(500000.0))))
+        noise = float(rng.uniform(0.01, 0.1))
+        res = float(np.exp(rng.uniform(np.log(64.0), np.log(512.0))))
+        if k % 2 == 0:
+            sub = int(np.clip(np.round(np.log(target / 20.0) / np.log(4.0)), 3, 7))
+            v, f = icosphere(sub, 1.0, noise, seed=seed * 100003 + k)
+        else:
+            nv = max(8, int(round((target / 4.0) ** 0.5)))
+            v, f = torus(1.0, float(rng.uniform(0.2, 0.4)), 2 * nv, nv, noise, seed=seed * 100003 + k)
+        extent = float((v.max(axis=0) - v.min(axis=0)).max())
+        out.append((v, f, np.float32(extent / res)))
+    return out

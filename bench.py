@@ -330,6 +330,7 @@ def run_ours(args):
     roof["launch_ms"] = tot_ms / nl
 
     pipe = pipeline_secondary(ctx, params, dev, L, N, bs, C) if args.pipeline else None
+    batch = batch_secondary(ctx, L, N, bs, C, args.batch_meshes) if args.batch_meshes else None
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -345,7 +346,8 @@ def run_ours(args):
             "clocks": clk,
             "stages_ms_per_step": {k: v[0] / args.steps for k, v in sorted(stages.items(), key=lambda kv: -kv[1][0])},
             "last_stats": stats,
-            "pipeline": pipe}
+            "pipeline": pipe,
+            "batched": batch}
     if rank == 0:
         if world == 1:
             line["cpu_baseline"] = cpu_baseline()
@@ -353,6 +355,81 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def batch_secondary(ctx, L, N, bs, C, n_meshes, reps=3):
+    """The uneven-batch workload (synthetic.uneven_batch: icospheres and
+    displaced tori, 1k-500k triangles, grids 64^3-512^3, band 3), resident in
+    HBM: the meshes one call each (bs_mesh_to_volume_device, volume freed
+    after each) against one bs_mesh_to_volume_batch_device call.  Both are
+    timed from the host around the whole set, best of `reps`, after one
+    warm-up run each."""
+    import torch
+    from baby_shark_gb300 import synthetic
+    t_gen = time.perf_counter()
+    batch = synthetic.uneven_batch(n_meshes)
+    t_gen = time.perf_counter() - t_gen
+    K = len(batch)
+    xyz = torch.from_numpy(np.concatenate([v for v, _, _ in batch])).cuda()
+    tri = torch.from_numpy(np.concatenate([f for _, f, _ in batch]).astype(np.int32)).cuda()
+    nv = np.array([len(v) for v, _, _ in batch], np.uint64)
+    nt = np.array([len(f) for _, f, _ in batch], np.uint64)
+    vb = np.concatenate([[0], np.cumsum(nv)]).astype(np.int64)
+    tb = np.concatenate([[0], np.cumsum(nt)]).astype(np.int64)
+    P = (N.M2VParams * K)()
+    for k, (_, _, h) in enumerate(batch):
+        L.bs_m2v_params_default(C.byref(P[k]))
+        P[k].voxel_size = float(h)
+        P[k].band_width = BAND
+    torch.cuda.synchronize()
+
+    def sequential():
+        band = 0
+        for k in range(K):
+            out = C.c_void_p()
+            N.check(L.bs_mesh_to_volume_device(ctx.h, xyz.data_ptr() + 12 * int(vb[k]), int(nv[k]),
+                                               tri.data_ptr() + 12 * int(tb[k]), int(nt[k]), C.byref(P[k]),
+                                               C.byref(out)), ctx.h)
+            vol = bs.Volume(out, ctx)
+            band += vol.counts()["active_voxels"]
+            del vol
+        return band
+
+    def batched():
+        outs = (C.c_void_p * K)()
+        N.check(L.bs_mesh_to_volume_batch_device(ctx.h, K, xyz.data_ptr(), nv.ctypes.data, tri.data_ptr(),
+                                                 nt.ctypes.data, P, outs), ctx.h)
+        vols = [bs.Volume(C.c_void_p(outs[k]), ctx) for k in range(K)]
+        band = sum(v.counts()["active_voxels"] for v in vols)
+        del vols
+        return band
+
+    def best(fn):
+        fn()
+        ctx.synchronize()
+        ts, band = [], 0
+        for _ in range(reps):
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            band = fn()
+            ctx.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return min(ts), band
+
+    l0 = ctx.kernel_launches
+    t_seq, band_seq = best(sequential)
+    l1 = ctx.kernel_launches
+    t_bat, band_bat = best(batched)
+    l2 = ctx.kernel_launches
+    assert band_seq == band_bat
+    return {"workload": "%d meshes (synthetic.uneven_batch): %d triangles, icospheres and displaced tori of "
+                        "1k-500k triangles, grids 64^3-512^3, band 3" % (K, int(nt.sum())),
+            "band_voxels": int(band_bat),
+            "sequential_ms": t_seq * 1e3, "batched_ms": t_bat * 1e3,
+            "sequential_band_voxels_per_s": band_seq / t_seq, "batched_band_voxels_per_s": band_bat / t_bat,
+            "batched_over_sequential": t_seq / t_bat,
+            "launches_sequential": int((l1 - l0) // (reps + 1)), "launches_batched": int((l2 - l1) // (reps + 1)),
+            "generation_s": t_gen}
 
 
 def pipeline_secondary(ctx, params, dev, L, N, bs, C):
@@ -426,6 +503,8 @@ def main():
                     help="skip the secondary boolean / offset / dual-contouring timings")
     ap.add_argument("--tris-fraction", type=float, default=1.0,
                     help="use only the first part of each torus ring (smaller case for profiling)")
+    ap.add_argument("--batch-meshes", type=int, default=256,
+                    help="meshes of the uneven-batch comparison (0 skips it)")
     ap.add_argument("--pipeline-only", action="store_true",
                     help="run only the boolean / offset / dual-contouring tail once and print its stage times")
     ap.add_argument("--voxel-size", type=float, default=H,

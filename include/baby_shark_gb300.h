@@ -107,6 +107,21 @@ bs_status bs_mesh_to_volume_device(bs_ctx* ctx, const float* d_xyz, uint64_t nv,
                                    const uint32_t* d_tri, uint64_t nt,
                                    const bs_m2v_params* params, bs_volume** out);
 
+/* A batch of meshes in one set of launches: n_meshes meshes whose vertices
+ * (3 floats each) and triangles (3 uint32 each, indices local to the mesh's
+ * own vertices) are concatenated in mesh order; vertex_counts[m] and
+ * triangle_counts[m] give each mesh's share and params[m] its
+ * MeshToVolume settings.  out[m] receives mesh m's volume, or NULL for a mesh
+ * without triangles (convert's None).  Each volume equals what
+ * bs_mesh_to_volume returns for that mesh alone.  No reference counterpart:
+ * the reference converts one mesh per call. */
+bs_status bs_mesh_to_volume_batch(bs_ctx* ctx, uint64_t n_meshes, const float* h_xyz, const uint64_t* vertex_counts,
+                                  const uint32_t* h_tri, const uint64_t* triangle_counts,
+                                  const bs_m2v_params* params, bs_volume** out);
+bs_status bs_mesh_to_volume_batch_device(bs_ctx* ctx, uint64_t n_meshes, const float* d_xyz,
+                                         const uint64_t* vertex_counts, const uint32_t* d_tri,
+                                         const uint64_t* triangle_counts, const bs_m2v_params* params,
+                                         bs_volume** out);
 /* ------------------------------------------------------------- volumes --- */
 bs_status bs_volume_free(bs_volume* v);
 /* Volume::voxel_size (volume/mod.rs:31-34). */
