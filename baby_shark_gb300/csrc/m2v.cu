@@ -773,49 +773,14 @@ __device__ __forceinline__ void kahan(float& sum, float& comp, float w) {
 
 // Warps are numbered per mesh (warp_base[m] .. warp_base[m+1]) so that a warp
 // never holds voxels of two meshes.
-// The single-mesh instance (MULTI = false) takes its mesh's values from the
-// kernel parameters `one`, so they cost no registers.
-struct WnOne {
-  float h, beta, thresh;
-  int n;
-  uint32_t na;
-};
-
-template <bool MULTI>
-__global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restrict__ act,
-                                                        const uint32_t* __restrict__ act_base,
-                                                        const uint32_t* __restrict__ warp_base, int K,
-                                                        const MeshInfo* __restrict__ mi,
-                                                        const uint32_t* __restrict__ tri_base,
-                                                        const uint32_t* __restrict__ inode_base, WnOne one,
-                                                        const int4* __restrict__ origins, float* __restrict__ values,
-                                                        const float4* __restrict__ inodes,
-                                                        const float4* __restrict__ leaves, M2VStats* stats) {
-  __shared__ int stk[WN_WARPS][WN_STACK];
+// Traversal of one warp's 32 voxels (act[i] for the lanes with valid) in one
+// mesh's tree, then the sign of each voxel's distance.
+__device__ __forceinline__ void wn_warp(const uint32_t* __restrict__ act, uint64_t i, bool valid, uint64_t last,
+                                        const int4* __restrict__ origins, float* __restrict__ values,
+                                        const float4* __restrict__ inode, const float4* __restrict__ leaf, int n,
+                                        float h, float beta, float thresh, M2VStats* st, int (*stk)[WN_STACK]) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const uint64_t gw = blockIdx.x * uint64_t(WN_WARPS) + w;
-  int mesh = 0;
-  uint64_t a0 = 0, a1 = one.na, i = gw * 32 + lane;
-  float h = one.h, beta = one.beta;
-  int n = one.n;
-  const float4* __restrict__ inode = inodes;
-  const float4* __restrict__ leaf = leaves;
-  if (MULTI) {
-    if (gw >= warp_base[K]) return;  // whole warp out of range
-    mesh = find_seg(warp_base, K, gw);
-    a0 = act_base[mesh];
-    a1 = act_base[mesh + 1];
-    i = a0 + (gw - warp_base[mesh]) * 32 + lane;
-    h = mi[mesh].h;
-    beta = mi[mesh].beta;
-    n = int(mi[mesh].n_tri);
-    inode = inodes + 5u * inode_base[mesh];
-    leaf = leaves + 5u * tri_base[mesh];
-  } else if (gw * 32 >= a1) {
-    return;
-  }
-  const bool valid = i < a1;
-  const uint32_t v = valid ? act[i] : act[a1 - 1];
+  const uint32_t v = valid ? act[i] : act[last];
   const uint32_t b = v >> 9, o = v & 511;
   const int4 org = origins[b];
   const F3 q = f3(fmul(__int2float_rn(org.x + int(o >> 6)), h), fmul(__int2float_rn(org.y + int((o >> 3) & 7)), h),
@@ -831,13 +796,13 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restri
     bool have = true;
     ++c_visit;
     if (node >= 0) {
-      const float4 P = __ldg(&inode[5 * node]);
+      const float4 P = inode[5 * node];
       const float rx = P.x - q.x, ry = P.y - q.y, rz = P.z - q.z;
       const float r2 = rx * rx + ry * ry + rz * rz;
       if (__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) {
         ++c_far;
-        const float4 A = __ldg(&inode[5 * node + 1]), B0 = __ldg(&inode[5 * node + 2]), B1 = __ldg(&inode[5 * node + 3]),
-                     B2 = __ldg(&inode[5 * node + 4]);
+        const float4 A = inode[5 * node + 1], B0 = inode[5 * node + 2], B1 = inode[5 * node + 3],
+                     B2 = inode[5 * node + 4];
         // a.r / (4 pi r^3) + trace(B) / (4 pi r^3) - 3 r^T B r / (4 pi r^5)
         const float ri = rsqrtf(r2);
         const float ri2 = ri * ri;
@@ -849,7 +814,7 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restri
         const float rbr = rx * brx + ry * bry + rz * brz;
         wv = inv * ((ar + A.w) - 3.0f * ri2 * rbr);
       } else {
-        const float4 E = __ldg(&inode[5 * node + 4]);
+        const float4 E = inode[5 * node + 4];
         if (sp < WN_STACK) {
           if (lane == 0) stk[w][sp] = __float_as_int(E.z);
           ++sp;
@@ -861,17 +826,17 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restri
       }
     } else {
       const int li = ~node;
-      const float4 P = __ldg(&leaf[5 * li]);
+      const float4 P = leaf[5 * li];
       const float rx = P.x - q.x, ry = P.y - q.y, rz = P.z - q.z;
       const float r2 = rx * rx + ry * ry + rz * rz;
       if (__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) {
         ++c_far;
-        const float4 A = __ldg(&leaf[5 * li + 1]);
+        const float4 A = leaf[5 * li + 1];
         const float ri = rsqrtf(r2);
         wv = (A.x * rx + A.y * ry + A.z * rz) * (ri * ri * ri * (1.0f / FOUR_PI));
       } else {
         ++c_exact;
-        wv = tri_wn(__ldg(&leaf[5 * li + 2]), __ldg(&leaf[5 * li + 3]), __ldg(&leaf[5 * li + 4]), q);
+        wv = tri_wn(leaf[5 * li + 2], leaf[5 * li + 3], leaf[5 * li + 4], q);
       }
     }
     __syncwarp();
@@ -883,8 +848,6 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restri
     }
     __syncwarp();
   }
-  M2VStats* st = stats + mesh;
-  const float thresh = MULTI ? mi[mesh].thresh : one.thresh;
   if (overflow && lane == 0) atomicExch(&st->error, 3);
   if (lane == 0) {
     atomicAdd(&st->wn_visits, (unsigned long long)c_visit);
@@ -895,6 +858,42 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restri
     const float d = values[uint64_t(b) * 512 + o];
     values[uint64_t(b) * 512 + o] = (sum < thresh) ? copysignf(d, 1.0f) : copysignf(d, -1.0f);
   }
+}
+
+__global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restrict__ act, uint64_t na,
+                                                        const int4* __restrict__ origins, float* __restrict__ values,
+                                                        const float4* __restrict__ inode,
+                                                        const float4* __restrict__ leaf, int n, float h, float beta,
+                                                        float thresh, M2VStats* st) {
+  __shared__ int stk[WN_WARPS][WN_STACK];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint64_t i = (blockIdx.x * uint64_t(WN_WARPS) + w) * 32 + lane;
+  if ((blockIdx.x * uint64_t(WN_WARPS) + w) * 32 >= na) return;  // whole warp out of range
+  wn_warp(act, i, i < na, na - 1, origins, values, inode, leaf, n, h, beta, thresh, st, stk);
+}
+
+// Batches: warps are numbered per mesh (warp_base[m] .. warp_base[m+1]) so
+// that a warp never holds voxels of two meshes.
+__global__ void __launch_bounds__(WN_THREADS) k_wn_sign_batch(const uint32_t* __restrict__ act,
+                                                              const uint32_t* __restrict__ act_base,
+                                                              const uint32_t* __restrict__ warp_base, int K,
+                                                              const MeshInfo* __restrict__ mi,
+                                                              const uint32_t* __restrict__ tri_base,
+                                                              const uint32_t* __restrict__ inode_base,
+                                                              const int4* __restrict__ origins,
+                                                              float* __restrict__ values,
+                                                              const float4* __restrict__ inodes,
+                                                              const float4* __restrict__ leaves, M2VStats* stats) {
+  __shared__ int stk[WN_WARPS][WN_STACK];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint64_t gw = blockIdx.x * uint64_t(WN_WARPS) + w;
+  if (gw >= warp_base[K]) return;  // whole warp out of range
+  const int mesh = find_seg(warp_base, K, gw);
+  const uint64_t a1 = act_base[mesh + 1];
+  const uint64_t i = act_base[mesh] + (gw - warp_base[mesh]) * 32 + lane;
+  const MeshInfo M = mi[mesh];
+  wn_warp(act, i, i < a1, a1 - 1, origins, values, inodes + 5 * uint64_t(inode_base[mesh]),
+          leaves + 5 * uint64_t(tri_base[mesh]), int(M.n_tri), M.h, M.beta, M.thresh, stats + mesh, stk);
 }
 
 // ------------------------------------------------------------ driver ------
@@ -1207,13 +1206,13 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   T.reset();
   if (na > 0) {
     const uint64_t n_warps = warp_base[K];
-    WnOne one{mi[0].h, mi[0].beta, mi[0].thresh, int(mi[0].n_tri), uint32_t(na)};
     if (K == 1)
-      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<false><<<blocks(n_warps, WN_WARPS), WN_THREADS, 0, s>>>(act.p, act_base.p, d_wb.p, K, d_mi.p, d_tb.p,
-                                                                                    d_ib.p, one, origins.p, values.p, inode.p, leaf.p, st.p)));
+      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<<<blocks(na, WN_THREADS), WN_THREADS, 0, s>>>(act.p, na, origins.p, values.p, inode.p, leaf.p,
+                                                                                 int(nt), mi[0].h, mi[0].beta,
+                                                                                 mi[0].thresh, st.p)));
     else
-      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<true><<<blocks(n_warps, WN_WARPS), WN_THREADS, 0, s>>>(act.p, act_base.p, d_wb.p, K, d_mi.p, d_tb.p,
-                                                                                   d_ib.p, one, origins.p, values.p, inode.p, leaf.p, st.p)));
+      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign_batch<<<blocks(n_warps, WN_WARPS), WN_THREADS, 0, s>>>(act.p, act_base.p, d_wb.p, K, d_mi.p, d_tb.p,
+                                                                                    d_ib.p, origins.p, values.p, inode.p, leaf.p, st.p)));
   }
   read_back(ctx, hst.data(), st.p, K * sizeof(M2VStats));
   uint64_t n_vp = 0, n_p = 0, visits = 0, far = 0, exact = 0;
