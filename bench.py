@@ -46,8 +46,10 @@ WN_FAR_PER_VOXEL = 110.1    # the oracle's traversal of the reference's SAH tree
 WN_EXACT_PER_VOXEL = 14.4   # torus (1/8 ring sample, 4.5 M band voxels): counts per band voxel
 WN_FLOP_PER_VOXEL = int(round(WN_FAR_PER_VOXEL * WN_FLOP_FAR + WN_EXACT_PER_VOXEL * WN_FLOP_EXACT))
 # dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture of
-# the half-ring case, scaled to a full torus by the units processed
-TRAFFIC_PER_LAUNCH = {}
+# the half-ring case (k_wn_sign 321 MB for 17,900,503 band voxels,
+# k_brick_distance 716 MB for 3,416,413,115 voxel pairs), scaled to a full
+# torus by the units processed (35,669,277 voxels; 6,848,421,294 pairs)
+TRAFFIC_PER_LAUNCH = {"k_wn_sign": 640e6, "k_brick_distance": 1436e6}
 METRIC = "band voxels/s mesh→SDF+sign: learned/batched vs plain GPU, 0 sign flips"
 UNIT = "band_voxels/s"
 WORKLOAD = "two displaced tori, 1,048,576 triangles each, voxel 0.002, band 3: mesh->SDF+sign (plain GPU path)"
@@ -434,9 +436,9 @@ def batch_secondary(ctx, L, N, bs, C, n_meshes, reps=3):
 
 def pipeline_secondary(ctx, params, dev, L, N, bs, C):
     """The boolean workload's tail, once per boolean: A op B, then offset +0.01
-    and -0.01 (each on its own copy), then dual contouring of each; CUDA events
-    on the library stream around every stage.  Returns ms per stage and the
-    output triangles."""
+    and -0.01 (each on its own copy), then dual contouring of each (and, as the
+    reference's other mesher, marching cubes); CUDA events on the library
+    stream around every stage.  Returns ms per stage and the output triangles."""
     import torch
     stream = torch.cuda.ExternalStream(ctx.stream)
 
@@ -456,7 +458,7 @@ def pipeline_secondary(ctx, params, dev, L, N, bs, C):
         return r, e0.elapsed_time(e1)
 
     res = {}
-    tris_total, dc_ms_total = 0, 0.0
+    tris_total, dc_ms_total, mc_total, mc_ms_total = 0, 0.0, 0, 0.0
     for op in ("subtract", "union", "intersect"):
         a, b = m2v(0), m2v(1)
         c, t_csg = timed(lambda: getattr(a, op)(b))
@@ -475,10 +477,18 @@ def pipeline_secondary(ctx, params, dev, L, N, bs, C):
             d["dc_%s_triangles" % sign] = int(n.value)
             tris_total += int(n.value)
             dc_ms_total += t_dc
+            nm = C.c_uint64()
+            _, t_mc = timed(lambda: N.check(L.bs_marching_cubes(ctx.h, cc.h, params.voxel_size, None, 0, C.byref(nm)),
+                                            ctx.h))
+            d["mc_%s_ms" % sign] = t_mc
+            d["mc_%s_triangles" % sign] = int(nm.value)
+            mc_total += int(nm.value)
+            mc_ms_total += t_mc
             del cc
         res[op] = d
         del a, b, c
     res["output_triangles_per_s_dc"] = tris_total / (dc_ms_total / 1000.0) if dc_ms_total else None
+    res["output_triangles_per_s_mc"] = mc_total / (mc_ms_total / 1000.0) if mc_ms_total else None
     return res
 
 
