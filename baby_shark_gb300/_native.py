@@ -40,6 +40,7 @@ SIGNATURES = {
     "bs_ctx_stage_reset": (i32, [vp]),
     "bs_ctx_last_stats": (i32, [vp, C.POINTER(u64)]),
     "bs_diag_fp32_peak": (i32, [vp, C.POINTER(C.c_double)]),
+    "bs_winding_numbers_exact": (i32, [vp, vp, u64, vp, u64, vp, u64, vp]),
     "bs_m2v_params_default": (None, [C.POINTER(M2VParams)]),
     "bs_mesh_to_volume": (i32, [vp, vp, u64, vp, u64, C.POINTER(M2VParams), PP]),
     "bs_mesh_to_volume_device": (i32, [vp, vp, u64, vp, u64, C.POINTER(M2VParams), PP]),

@@ -313,6 +313,29 @@ def convert_batch(meshes, params, ctx=None):
     return [Volume(C.c_void_p(out[k]), ctx) if out[k] else None for k in range(K)]
 
 
+def winding_numbers_exact(vertices, triangles, points, ctx=None):
+    """Exact generalised winding numbers (float64) of `points` w.r.t. a mesh by
+    direct summation on the GPU (bs_winding_numbers_exact).  Arguments are
+    numpy arrays or torch CUDA tensors."""
+    import torch
+    ctx = ctx or default_context()
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    def as_dev(a, dtype):
+        t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a))
+        return t.to(device=dev, dtype=dtype).contiguous()
+
+    v = as_dev(vertices, torch.float32).reshape(-1, 3)
+    f = as_dev(np.asarray(triangles, np.int64) if not isinstance(triangles, torch.Tensor) else triangles,
+               torch.int32).reshape(-1, 3)
+    p = as_dev(points, torch.float32).reshape(-1, 3)
+    out = torch.empty(p.shape[0], dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    N.check(N.load().bs_winding_numbers_exact(ctx.h, v.data_ptr(), v.shape[0], f.data_ptr(), f.shape[0],
+                                              p.data_ptr(), p.shape[0], out.data_ptr()), ctx.h)
+    return out
+
+
 class DualContouringMesher:
     """DualContouringMesher (voxel/meshing/dual_contouring.rs:12-91)."""
 

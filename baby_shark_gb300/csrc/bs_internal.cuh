@@ -319,6 +319,8 @@ std::vector<bs_volume*> mesh_to_volume_batch_impl(bs_ctx* ctx, const float* d_xy
                                                   const std::vector<uint64_t>& n_tri,
                                                   const std::vector<bs_m2v_params>& params);
 bs_volume* volume_clone_impl(bs_ctx* ctx, const bs_volume* v);
+bs_status exact_winding_numbers_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri,
+                                     uint64_t nt, const float* d_pts, uint64_t np, double* d_out);
 void marching_cubes_impl(bs_ctx* ctx, bs_volume* v, float voxel_size);
 bs_volume* volume_sphere_impl(bs_ctx* ctx, float h, float radius, const float origin[3]);
 bs_volume* volume_cuboid_impl(bs_ctx* ctx, float h, const float mn[3], const float mx[3]);

@@ -271,6 +271,12 @@ bs_status bs_mesh_to_volume_batch_device(bs_ctx* ctx, uint64_t n_meshes, const f
   return batch_common(ctx, n_meshes, d_xyz, vertex_counts, d_tri, triangle_counts, params, out, false);
 }
 
+bs_status bs_winding_numbers_exact(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri,
+                                   uint64_t nt, const float* d_points, uint64_t n_points, double* d_out) {
+  if (!ctx || (nt && (!d_xyz || !d_tri)) || (n_points && (!d_points || !d_out))) return BS_ERR_INVALID_ARG;
+  return guarded(ctx, [&] { bs::exact_winding_numbers_impl(ctx, d_xyz, nv, d_tri, nt, d_points, n_points, d_out); });
+}
+
 bs_status bs_volume_free(bs_volume* v) {
   if (!v) return BS_ERR_INVALID_ARG;
   delete v;

@@ -896,6 +896,56 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign_batch(const uint32_t* __
           leaves + 5 * uint64_t(tri_base[mesh]), int(M.n_tri), M.h, M.beta, M.thresh, stats + mesh, stk);
 }
 
+// ------------------------------------------------ exact winding numbers ---
+// Direct sum over every triangle (no tree, no far field): the solid angle of
+// each triangle in the reference's operation order (IEEE, unfused), the sum
+// in double.  A validation instrument for the approximate traversal.
+constexpr int EX_THREADS = 256, EX_TILE = 1024;
+
+__global__ void __launch_bounds__(EX_THREADS) k_wn_exact(const float* __restrict__ xyz, uint64_t nv,
+                                                         const uint32_t* __restrict__ tri, uint64_t nt,
+                                                         const float* __restrict__ pts, uint64_t np,
+                                                         double* __restrict__ out, int* __restrict__ err) {
+  __shared__ float4 tv[EX_TILE][3];
+  const uint64_t i = blockIdx.x * uint64_t(EX_THREADS) + threadIdx.x;
+  const bool valid = i < np;
+  const F3 q = valid ? f3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]) : f3(0.f, 0.f, 0.f);
+  double sum = 0.0;
+  for (uint64_t t0 = 0; t0 < nt; t0 += EX_TILE) {
+    const int cnt = int((nt - t0) < uint64_t(EX_TILE) ? (nt - t0) : uint64_t(EX_TILE));
+    __syncthreads();
+    for (int k = threadIdx.x; k < cnt; k += EX_THREADS) {
+      const uint64_t t = t0 + k;
+      for (int c = 0; c < 3; ++c) {
+        const uint32_t vi = tri[3 * t + c];
+        if (vi >= nv) {
+          atomicExch(err, 1);
+          tv[k][c] = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+          tv[k][c] = make_float4(xyz[3 * vi], xyz[3 * vi + 1], xyz[3 * vi + 2], 0.f);
+        }
+      }
+    }
+    __syncthreads();
+    if (valid)
+      for (int k = 0; k < cnt; ++k) sum += double(tri_wn_exact(tv[k][0], tv[k][1], tv[k][2], q));
+  }
+  if (valid) out[i] = sum;
+}
+
+bs_status exact_winding_numbers_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri,
+                                     uint64_t nt, const float* d_pts, uint64_t np, double* d_out) {
+  DBuf<int> err(ctx, 1);
+  BS_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), ctx->stream));
+  if (np)
+    BS_KERNEL(ctx, "k_wn_exact", (k_wn_exact<<<unsigned((np + EX_THREADS - 1) / EX_THREADS), EX_THREADS, 0, ctx->stream>>>(
+                                     d_xyz, nv, d_tri, nt, d_pts, np, d_out, err.p)));
+  int e = 0;
+  read_back(ctx, &e, err.p, sizeof e);
+  if (e) fail(BS_ERR_INVALID_ARG, "triangle vertex index out of range");
+  return BS_OK;
+}
+
 // ------------------------------------------------------------ driver ------
 static inline unsigned blocks(uint64_t n, unsigned t) { return unsigned((n + t - 1) / t); }
 

@@ -13,6 +13,11 @@ numpy's PCG64 generator (numpy.random.default_rng):
   gradient_noise(p, seed)
       3-D gradient (Perlin-style) noise in roughly [-1, 1]: a seeded 256-entry
       permutation, 12 edge gradients, quintic fade, trilinear blend.
+  open_icosphere(subdiv, amplitude, octaves, remove, seed)
+      icosphere displaced radially by `octaves` octaves of gradient noise
+      (frequency doubling, amplitude halving, peak displacement `amplitude`),
+      then a `remove` fraction of its faces dropped uniformly at random — a
+      triangle soup with holes.
   uneven_batch(n, seed)
       n meshes alternating icospheres and displaced tori, triangle counts
       log-uniform in [1k, 500k] (icospheres take the nearest subdivision),
@@ -146,3 +151,15 @@ def uneven_batch(n=256, seed=4):
         extent = float((v.max(axis=0) - v.min(axis=0)).max())
         out.append((v, f, np.float32(extent / res)))
     return out
+
+
+def open_icosphere(subdiv=9, amplitude=0.1, octaves=4, remove=0.1, seed=3):
+    """Non-watertight workload: subdivision-9 icosphere (5,242,880 triangles),
+    4-octave radial noise of amplitude 0.1, 10 % of faces removed."""
+    v, f = icosphere(subdiv, 1.0, 0.0, seed)
+    p = v.astype(np.float64)
+    disp = np.zeros(len(p))
+    for k in range(octaves):
+        disp += 0.5 ** k * gradient_noise(2.0 ** k * 2.0 * p + 31.0 * (k + 1), seed + k)
+    p = p * (1.0 + amplitude * disp / np.abs(disp).max())[:, None]  # peak displacement = amplitude
+    return p.astype(np.float32), remove_faces(f, remove, seed + 99)

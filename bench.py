@@ -359,6 +359,84 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_open(args):
+    """The non-watertight workload: subdivision-9 icosphere (5,242,880
+    triangles) with 4-octave radial noise of amplitude 0.1 and 10 % of faces
+    removed, voxel 0.001, band 3.  Band voxels/s of mesh -> SDF + sign with the
+    mesh resident in HBM, and the signs of a seeded sample of band voxels
+    against exact winding numbers (direct sum, bs_winding_numbers_exact)."""
+    import ctypes as C
+
+    import torch
+
+    import baby_shark_gb300 as bs
+    from baby_shark_gb300 import _native as N
+    from baby_shark_gb300 import build as bs_build
+    from baby_shark_gb300 import synthetic
+
+    bs_build.build()
+    L = N.load()
+    ctx = bs.Context(0)
+    t_gen = time.perf_counter()
+    v, f = synthetic.open_icosphere()
+    t_gen = time.perf_counter() - t_gen
+    h = 0.001
+    x = torch.from_numpy(v).cuda()
+    t = torch.from_numpy(f.astype(np.int32)).cuda()
+    params = N.M2VParams()
+    L.bs_m2v_params_default(C.byref(params))
+    params.voxel_size = h
+    params.band_width = BAND
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def step():
+        out = C.c_void_p()
+        N.check(L.bs_mesh_to_volume_device(ctx.h, x.data_ptr(), x.shape[0], t.data_ptr(), t.shape[0],
+                                           C.byref(params), C.byref(out)), ctx.h)
+        return bs.Volume(out, ctx)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    ms = []
+    vol = None
+    for _ in range(args.steps):
+        vol = None
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        vol = step()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    band = vol.counts()["active_voxels"]
+    stats = ctx.last_stats()
+    # sign check on a seeded sample of band voxels
+    o, val, m = vol.export()
+    act = np.unpackbits(m.view(np.uint8), bitorder="little").reshape(len(o), 512).astype(bool)
+    li, vi = np.nonzero(act)
+    rng = np.random.default_rng(7)
+    pick = rng.choice(len(li), size=min(args.validation, len(li)), replace=False)
+    li, vi = li[pick], vi[pick]
+    vox = o[li] + np.stack([vi >> 6, (vi >> 3) & 7, vi & 7], 1)
+    pts = vox.astype(np.float32) * np.float32(h)
+    t0 = time.perf_counter()
+    wn = bs.winding_numbers_exact(x, t, pts, ctx=ctx).cpu().numpy()
+    t_exact = time.perf_counter() - t0
+    inside = np.signbit(val[li, vi])
+    mism = inside != (wn >= 0.2)
+    line = {"metric": METRIC, "value": band / (min(ms) / 1000.0), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": min(ms), "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "open icosphere: subdivision 9, 4-octave radial noise 0.1, 10%% of faces "
+                                   "removed (%d triangles), voxel 0.001, band 3" % len(f),
+                       "band_voxels_per_step": int(band), "generation_s": t_gen},
+            "sign_vs_exact": {"sample": int(len(li)), "mismatches": int(mism.sum()),
+                              "mismatches_within_0.01_of_threshold": int((mism & (np.abs(wn - 0.2) < 0.01)).sum()),
+                              "exact_pass_s": t_exact},
+            "last_stats": stats}
+    print(json.dumps(line))
+
+
 def batch_secondary(ctx, L, N, bs, C, n_meshes, reps=3):
     """The uneven-batch workload (synthetic.uneven_batch: icospheres and
     displaced tori, 1k-500k triangles, grids 64^3-512^3, band 3), resident in
@@ -515,6 +593,11 @@ def main():
                     help="use only the first part of each torus ring (smaller case for profiling)")
     ap.add_argument("--batch-meshes", type=int, default=256,
                     help="meshes of the uneven-batch comparison (0 skips it)")
+    ap.add_argument("--workload", default="tori", choices=["tori", "open-icosphere"],
+                    help="tori: the boolean workload's two tori (the headline line); open-icosphere: the "
+                         "non-watertight subdivision-9 icosphere with an exact-sign check")
+    ap.add_argument("--validation", type=int, default=200000,
+                    help="band voxels checked against exact winding numbers (open-icosphere)")
     ap.add_argument("--pipeline-only", action="store_true",
                     help="run only the boolean / offset / dual-contouring tail once and print its stage times")
     ap.add_argument("--voxel-size", type=float, default=H,
@@ -522,6 +605,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "open-icosphere":
+        run_open(args)
     else:
         run_ours(args)
 

@@ -84,6 +84,13 @@ bs_status bs_ctx_last_stats(const bs_ctx* ctx, uint64_t* out8);
 /* Measured FP32 FMA throughput of the context's device in TFLOP/s (a timed
  * FFMA loop over all SMs); the denominator of FP32-bound roofline fractions. */
 bs_status bs_diag_fp32_peak(bs_ctx* ctx, double* tflops);
+/* Exact generalised winding numbers of n_points points (device float3) with
+ * respect to a mesh (device arrays): the direct sum over every triangle of
+ * the solid angle of aabb_tree.rs:582-615, summed in double into d_out.  A
+ * validation instrument for the approximate sign pass (no reference
+ * counterpart: the reference only has the tree approximation). */
+bs_status bs_winding_numbers_exact(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri,
+                                   uint64_t nt, const float* d_points, uint64_t n_points, double* d_out);
 
 /* ----------------------------------------------------- mesh -> volume ---- */
 typedef struct bs_m2v_params {

@@ -169,3 +169,30 @@ def test_full_size_torus_sign_property():
     assert np.all(np.signbit(vals[sure]) == (d_tube[sure] < 0))
     assert np.all(np.abs(vals) <= (3 + 2) * h * np.sqrt(3) + 1e-6)
     assert vol.counts()["active_voxels"] == act.sum()
+
+
+def test_exact_winding_numbers_match_oracle_f64():
+    """bs_winding_numbers_exact against the oracle's float64 direct sum."""
+    v, f = synthetic.icosphere(3, 0.8, 0.04, seed=4)
+    f = synthetic.remove_faces(f, 0.1, seed=5)
+    rng = np.random.default_rng(6)
+    pts = rng.uniform(-1.0, 1.0, (4000, 3)).astype(np.float32)
+    g = bs.winding_numbers_exact(v, f, pts, ctx=context()).cpu().numpy()
+    o = ob.exact_wn_f64(v, f.astype(np.uint32), pts)
+    assert np.max(np.abs(g - o)) < 2e-5
+
+
+def test_fast_sign_agrees_with_exact_on_watertight():
+    """Every band voxel's sign from the tree approximation equals the exact
+    winding number's classification (wn < 0.2 outside) on a closed mesh."""
+    v, f = synthetic.config1()
+    vol = bs.MeshToVolume(context()).with_voxel_size(0.02).with_narrow_band_width(3).convert((v, f))
+    o, val, m = vol.export()
+    act = np.unpackbits(m.view(np.uint8), bitorder="little").reshape(len(o), 512).astype(bool)
+    idx = np.nonzero(act)
+    off = idx[1]
+    vox = o[idx[0]] + np.stack([off >> 6, (off >> 3) & 7, off & 7], 1)
+    pts = vox.astype(np.float32) * np.float32(0.02)
+    wn = bs.winding_numbers_exact(v, f, pts, ctx=context()).cpu().numpy()
+    inside_gpu = np.signbit(val[idx])
+    assert np.array_equal(inside_gpu, wn >= 0.2)
