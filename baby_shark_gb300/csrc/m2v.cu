@@ -597,10 +597,13 @@ __global__ void k_leaves(const float4* __restrict__ T, const uint32_t* __restric
   s.lo[1] = fminf(A.y, fminf(B.y, C.y)); s.hi[1] = fmaxf(A.y, fmaxf(B.y, C.y));
   s.lo[2] = fminf(A.z, fminf(B.z, C.z)); s.hi[2] = fmaxf(A.z, fmaxf(B.z, C.z));
   lsum[i] = s;
-  // a single triangle's dipole centre is its centroid; order-2 term vanishes
-  float d0 = (s.lo[0] - cx) * (s.lo[0] - cx) + (s.lo[1] - cy) * (s.lo[1] - cy) + (s.lo[2] - cz) * (s.lo[2] - cz);
-  float d1 = (s.hi[0] - cx) * (s.hi[0] - cx) + (s.hi[1] - cy) * (s.hi[1] - cy) + (s.hi[2] - cz) * (s.hi[2] - cz);
-  leaf[5 * i + 0] = make_float4(cx, cy, cz, sqrtf(fmaxf(d0, d1)));
+  // a single triangle's dipole centre is its centroid; order-2 term vanishes.
+  // Radius: the farthest vertex from the centroid (the cluster's extent),
+  // rounded up by a few ulps so that it bounds the vertices.
+  float da = (A.x - cx) * (A.x - cx) + (A.y - cy) * (A.y - cy) + (A.z - cz) * (A.z - cz);
+  float db = (B.x - cx) * (B.x - cx) + (B.y - cy) * (B.y - cy) + (B.z - cz) * (B.z - cz);
+  float dc = (C.x - cx) * (C.x - cx) + (C.y - cy) * (C.y - cy) + (C.z - cz) * (C.z - cz);
+  leaf[5 * i + 0] = make_float4(cx, cy, cz, sqrtf(fmaxf(fmaxf(da, db), dc)) * 1.000001f);
   leaf[5 * i + 1] = make_float4(s.ax, s.ay, s.az, 0.f);
   leaf[5 * i + 2] = A;
   leaf[5 * i + 3] = B;
@@ -673,10 +676,12 @@ __device__ __forceinline__ Sums load_sums_cg(const Sums* p) {
 }
 
 // Bottom-up: the second thread to reach a node combines both children.
+__device__ __forceinline__ float4 ld_cg4(const float4* p) { return __ldcg(p); }
+
 __global__ void k_refit(uint64_t nt, const uint32_t* __restrict__ tri_base, const uint32_t* __restrict__ inode_base,
                         int K, const int2* __restrict__ child, const int* __restrict__ parent_i,
                         const int* __restrict__ parent_l, const Sums* __restrict__ lsum, Sums* __restrict__ isum,
-                        int* __restrict__ flags, float4* __restrict__ inode) {
+                        int* __restrict__ flags, float4* __restrict__ inode, const float4* __restrict__ leaf_rec) {
   const uint64_t gl = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (gl >= nt) return;
   const int mesh = find_seg(tri_base, K, gl);
@@ -701,7 +706,14 @@ __global__ void k_refit(uint64_t nt, const uint32_t* __restrict__ tri_base, cons
       for (int q = 0; q < 3; ++q) B[3 * rr + q] = r.m[3 * rr + q] - p[rr] * A[q];
     float d0 = (r.lo[0] - px) * (r.lo[0] - px) + (r.lo[1] - py) * (r.lo[1] - py) + (r.lo[2] - pz) * (r.lo[2] - pz);
     float d1 = (r.hi[0] - px) * (r.hi[0] - px) + (r.hi[1] - py) * (r.hi[1] - py) + (r.hi[2] - pz) * (r.hi[2] - pz);
-    inode[5 * gn + 0] = make_float4(px, py, pz, sqrtf(fmaxf(d0, d1)));
+    // radius: the smaller of the reference's bounding-box bound (aabb_tree.rs:738-741)
+    // and the sphere around p holding both children's spheres
+    const float4 ca = c.x >= 0 ? ld_cg4(inode + 5 * (ib + uint64_t(c.x))) : leaf_rec[5 * (lb + uint64_t(~c.x))];
+    const float4 cb = c.y >= 0 ? ld_cg4(inode + 5 * (ib + uint64_t(c.y))) : leaf_rec[5 * (lb + uint64_t(~c.y))];
+    const float ea = sqrtf((ca.x - px) * (ca.x - px) + (ca.y - py) * (ca.y - py) + (ca.z - pz) * (ca.z - pz)) + ca.w;
+    const float eb = sqrtf((cb.x - px) * (cb.x - px) + (cb.y - py) * (cb.y - py) + (cb.z - pz) * (cb.z - pz)) + cb.w;
+    const float rad = fminf(sqrtf(fmaxf(d0, d1)), fmaxf(ea, eb) * 1.000001f);
+    inode[5 * gn + 0] = make_float4(px, py, pz, rad);
     inode[5 * gn + 1] = make_float4(r.ax, r.ay, r.az, B[0] + B[4] + B[8]);
     inode[5 * gn + 2] = make_float4(B[0], B[1], B[2], B[3]);
     inode[5 * gn + 3] = make_float4(B[4], B[5], B[6], B[7]);
@@ -1246,7 +1258,7 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
       BS_CUDA(cudaMemsetAsync(parent_i.p, 0xff, n_int * sizeof(int), s));  // roots keep -1
       BS_KERNEL(ctx, "k_karras", (k_karras<<<blocks(n_int, 256), 256, 0, s>>>(keys2.p, n_int, d_tb.p, d_ib.p, K, child.p, parent_i.p, parent_l.p)));
       BS_KERNEL(ctx, "k_refit", (k_refit<<<blocks(nt, 256), 256, 0, s>>>(nt, d_tb.p, d_ib.p, K, child.p, parent_i.p, parent_l.p, lsum.p, isum.p,
-                                                                      flags.p, inode.p)));
+                                                                      flags.p, inode.p, leaf.p)));
     }
   }
   keys2.reset();
