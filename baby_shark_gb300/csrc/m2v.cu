@@ -566,12 +566,6 @@ __global__ void k_mesh_keys(const uint32_t* __restrict__ order, uint64_t nt, con
   const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (i < nt) mk[i] = uint32_t(find_seg(tri_base, K, order[i]));
 }
-__global__ void k_gather_keys(const uint32_t* __restrict__ order, uint64_t nt, const uint64_t* __restrict__ keys,
-                              uint64_t* __restrict__ out) {
-  const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
-  if (i < nt) out[i] = keys[order[i]];
-}
-
 __global__ void k_leaves(const float4* __restrict__ T, const uint32_t* __restrict__ order, uint64_t nt,
                          float4* __restrict__ leaf, Sums* __restrict__ lsum) {
   uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
@@ -610,51 +604,116 @@ __global__ void k_leaves(const float4* __restrict__ T, const uint32_t* __restric
   leaf[5 * i + 4] = C;
 }
 
-__device__ __forceinline__ int delta(const uint64_t* __restrict__ k, int n, int i, int j) {
-  if (j < 0 || j >= n) return -1;
-  uint64_t a = k[i], b = k[j];
-  if (a == b) return 64 + __clz(uint32_t(i) ^ uint32_t(j));
-  return __clzll(a ^ b);
+// ---- PLOC: Meister & Bittner, "Parallel Locally-Ordered Clustering for
+// Bounding Volume Hierarchy Construction" (TVCG 2018).  Clusters start as the
+// triangles in Morton order; each round every cluster finds the cluster of
+// its own mesh within +-PLOC_R positions whose merged bounding box has the
+// smallest surface area, mutual nearest neighbours merge into a new internal
+// node at the lower position, and the array is compacted.  Internal node ids
+// of a mesh count down from n - 2, so its last merge, the root, is node 0.
+constexpr int PLOC_R = 16;
+constexpr int PLOC_T = 256;
+
+struct Cluster {
+  float lo[3], hi[3];
+  int node;  // local child encoding: >= 0 internal, < 0 leaf ~index
+  int mesh;
+};
+
+__device__ __forceinline__ float merged_area(const Cluster& a, const Cluster& b) {
+  const float dx = fmaxf(a.hi[0], b.hi[0]) - fminf(a.lo[0], b.lo[0]);
+  const float dy = fmaxf(a.hi[1], b.hi[1]) - fminf(a.lo[1], b.lo[1]);
+  const float dz = fmaxf(a.hi[2], b.hi[2]) - fminf(a.lo[2], b.lo[2]);
+  return dx * dy + dx * dz + dy * dz;
 }
 
-// Karras, "Maximizing Parallelism in the Construction of BVHs, Octrees, and
-// k-d Trees" (HPG 2012), with index tie-break for equal codes.  One tree per
-// mesh: mesh m's n_m leaves sit at tri_base[m], its n_m - 1 internal nodes at
-// inode_base[m] = tri_base[m] - m; child and parent indices are local to the
-// mesh (child >= 0 internal, < 0 leaf ~index; parent -1 at the root).
-__global__ void k_karras(const uint64_t* __restrict__ keys, uint64_t n_internal, const uint32_t* __restrict__ tri_base,
-                         const uint32_t* __restrict__ inode_base, int K, int2* __restrict__ child,
-                         int* __restrict__ parent_i, int* __restrict__ parent_l) {
-  const uint64_t g = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
-  if (g >= n_internal) return;
-  const int mesh = find_seg(inode_base, K, g);
-  const int i = int(g - inode_base[mesh]);
-  const int n = int(tri_base[mesh + 1] - tri_base[mesh]);
-  const uint64_t* k = keys + tri_base[mesh];
-  int d = (delta(k, n, i, i + 1) - delta(k, n, i, i - 1)) >= 0 ? 1 : -1;
-  int dmin = delta(k, n, i, i - d);
-  int lmax = 2;
-  while (delta(k, n, i, i + lmax * d) > dmin) lmax <<= 1;
-  int l = 0;
-  for (int t = lmax >> 1; t >= 1; t >>= 1)
-    if (delta(k, n, i, i + (l + t) * d) > dmin) l += t;
-  int j = i + l * d;
-  int dnode = delta(k, n, i, j);
-  int s = 0;
-  int t = l;
-  do {
-    t = (t + 1) >> 1;
-    if (delta(k, n, i, i + (s + t) * d) > dnode) s += t;
-  } while (t > 1);
-  int gamma = i + s * d + min(d, 0);
-  int lo = min(i, j), hi = max(i, j);
-  int left = (lo == gamma) ? ~gamma : gamma;
-  int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
-  child[g] = make_int2(left, right);
-  if (left >= 0) parent_i[inode_base[mesh] + left] = i;
-  else parent_l[tri_base[mesh] + ~left] = i;
-  if (right >= 0) parent_i[inode_base[mesh] + right] = i;
-  else parent_l[tri_base[mesh] + ~right] = i;
+__global__ void k_ploc_init(const Sums* __restrict__ lsum, uint64_t nt, const uint32_t* __restrict__ tri_base, int K,
+                            Cluster* __restrict__ cl) {
+  const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= nt) return;
+  const int mesh = find_seg(tri_base, K, i);
+  const Sums& s = lsum[i];
+  Cluster c;
+  for (int k = 0; k < 3; ++k) {
+    c.lo[k] = s.lo[k];
+    c.hi[k] = s.hi[k];
+  }
+  c.node = ~int(i - tri_base[mesh]);
+  c.mesh = mesh;
+  cl[i] = c;
+}
+
+// Nearest neighbour of every cluster within the window (ties: lower index).
+__global__ void __launch_bounds__(PLOC_T) k_ploc_nn(const Cluster* __restrict__ cl, uint32_t nc, int* __restrict__ nn) {
+  __shared__ Cluster sc[PLOC_T + 2 * PLOC_R];
+  const int64_t b0 = int64_t(blockIdx.x) * PLOC_T;
+  for (int k = threadIdx.x; k < PLOC_T + 2 * PLOC_R; k += PLOC_T) {
+    const int64_t g = b0 - PLOC_R + k;
+    if (g >= 0 && g < int64_t(nc)) sc[k] = cl[g];
+    else sc[k].mesh = -1;
+  }
+  __syncthreads();
+  const int64_t i = b0 + threadIdx.x;
+  if (i >= int64_t(nc)) return;
+  const Cluster& me = sc[threadIdx.x + PLOC_R];
+  float best = INFINITY;
+  int bj = -1;
+  for (int d = -PLOC_R; d <= PLOC_R; ++d) {
+    if (d == 0) continue;
+    const Cluster& o = sc[threadIdx.x + PLOC_R + d];
+    if (o.mesh != me.mesh) continue;
+    const float a = merged_area(me, o);
+    if (a < best) {  // d ascends, so ties keep the lower index
+      best = a;
+      bj = int(i + d);
+    }
+  }
+  nn[i] = bj;
+}
+
+// Merges mutual pairs; keep[i] says whether position i survives the round.
+__global__ void k_ploc_merge(Cluster* __restrict__ cl, uint32_t nc, const int* __restrict__ nn,
+                             const uint32_t* __restrict__ tri_base, const uint32_t* __restrict__ inode_base,
+                             int* __restrict__ next_id, int2* __restrict__ child, int* __restrict__ parent_i,
+                             int* __restrict__ parent_l, uint32_t* __restrict__ keep) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) {
+    if (i == nc) keep[nc] = 0u;
+    return;
+  }
+  const int j = nn[i];
+  if (j < 0 || nn[j] != int(i)) {
+    keep[i] = 1u;
+    return;
+  }
+  if (int(i) > j) {
+    keep[i] = 0u;
+    return;
+  }
+  Cluster a = cl[i];
+  const Cluster b = cl[j];
+  const int m = a.mesh;
+  const int n = int(tri_base[m + 1] - tri_base[m]);
+  const int id = (n - 2) - atomicAdd(&next_id[m], 1);
+  const uint64_t ib = inode_base[m], lb = tri_base[m];
+  child[ib + id] = make_int2(a.node, b.node);
+  if (a.node >= 0) parent_i[ib + a.node] = id;
+  else parent_l[lb + ~a.node] = id;
+  if (b.node >= 0) parent_i[ib + b.node] = id;
+  else parent_l[lb + ~b.node] = id;
+  for (int k = 0; k < 3; ++k) {
+    a.lo[k] = fminf(a.lo[k], b.lo[k]);
+    a.hi[k] = fmaxf(a.hi[k], b.hi[k]);
+  }
+  a.node = id;
+  cl[i] = a;
+  keep[i] = 1u;
+}
+
+__global__ void k_ploc_compact(const Cluster* __restrict__ cl, uint32_t nc, const uint32_t* __restrict__ keep,
+                               const uint32_t* __restrict__ pos, Cluster* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nc && keep[i]) out[pos[i]] = cl[i];
 }
 
 __device__ __forceinline__ void sums_add(Sums& r, const Sums& a, const Sums& b) {
@@ -1231,7 +1290,7 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   }
   if (K > 1) {
     // stable second pass by mesh: every mesh keeps its full-precision Morton
-    // order, so its tree is the one a call for that mesh alone would build
+    // order, so its tree is the one a call for that mesh alone builds
     int mesh_bits = 1;
     while ((1 << mesh_bits) < K) ++mesh_bits;
     DBuf<uint32_t> mk(ctx, nt), mk2(ctx, nt), order2(ctx, nt);
@@ -1240,7 +1299,6 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
     BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, mk.p, mk2.p, order.p, order2.p, int(nt), 0, mesh_bits, s));
     DBuf<uint8_t> t(ctx, tmp);
     BS_CUDA(cub::DeviceRadixSort::SortPairs(t.p, tmp, mk.p, mk2.p, order.p, order2.p, int(nt), 0, mesh_bits, s));
-    BS_KERNEL(ctx, "k_gather_keys", (k_gather_keys<<<blocks(nt, 256), 256, 0, s>>>(order2.p, nt, keys.p, keys2.p)));
     std::swap(order.p, order2.p);
   }
   keys.reset();
@@ -1256,7 +1314,26 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
     if (n_int) {
       BS_CUDA(cudaMemsetAsync(flags.p, 0, n_int * sizeof(int), s));
       BS_CUDA(cudaMemsetAsync(parent_i.p, 0xff, n_int * sizeof(int), s));  // roots keep -1
-      BS_KERNEL(ctx, "k_karras", (k_karras<<<blocks(n_int, 256), 256, 0, s>>>(keys2.p, n_int, d_tb.p, d_ib.p, K, child.p, parent_i.p, parent_l.p)));
+      // topology by PLOC over the Morton-ordered triangles, one tree per mesh
+      DBuf<Cluster> ca(ctx, nt), cb(ctx, nt);
+      DBuf<int> nn(ctx, nt), next_id(ctx, K);
+      DBuf<uint32_t> keep(ctx, nt + 1), pos(ctx, nt + 1);
+      BS_CUDA(cudaMemsetAsync(next_id.p, 0, K * sizeof(int), s));
+      BS_KERNEL(ctx, "k_ploc_init", (k_ploc_init<<<blocks(nt, 256), 256, 0, s>>>(lsum.p, nt, d_tb.p, K, ca.p)));
+      uint32_t nc = uint32_t(nt);
+      for (int round = 0; nc > uint32_t(K); ++round) {
+        if (round >= 4096) fail(BS_ERR_CAPACITY, "tree build did not converge");
+        BS_KERNEL(ctx, "k_ploc_nn", (k_ploc_nn<<<blocks(nc, PLOC_T), PLOC_T, 0, s>>>(ca.p, nc, nn.p)));
+        BS_KERNEL(ctx, "k_ploc_merge", (k_ploc_merge<<<blocks(nc + 1, 256), 256, 0, s>>>(ca.p, nc, nn.p, d_tb.p, d_ib.p, next_id.p, child.p,
+                                                                                   parent_i.p, parent_l.p, keep.p)));
+        exclusive_scan(ctx, keep.p, pos.p, uint64_t(nc) + 1);
+        BS_KERNEL(ctx, "k_ploc_compact", (k_ploc_compact<<<blocks(nc, 256), 256, 0, s>>>(ca.p, nc, keep.p, pos.p, cb.p)));
+        std::swap(ca.p, cb.p);
+        uint32_t next = 0;
+        read_back(ctx, &next, pos.p + nc, sizeof next);
+        if (next >= nc) fail(BS_ERR_CAPACITY, "tree build made no progress");
+        nc = next;
+      }
       BS_KERNEL(ctx, "k_refit", (k_refit<<<blocks(nt, 256), 256, 0, s>>>(nt, d_tb.p, d_ib.p, K, child.p, parent_i.p, parent_l.p, lsum.p, isum.p,
                                                                       flags.p, inode.p, leaf.p)));
     }
