@@ -152,6 +152,20 @@ def cpu_baseline(seconds_target=15.0):
                       % (len(fs), stats["band_voxels"], dt)}
 
 
+def combine_ranks(ms, band, world, device="cuda"):
+    """Replicas: the job's step time is the slowest rank's, its band voxels
+    the sum over ranks (every rank converts its own copy of the workload)."""
+    if world == 1:
+        return ms, band
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    b = torch.tensor([float(band)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(b, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(b.item())
+
+
 def run_reference(args):
     rank, world, _ = rank_info()
     if rank != 0:
@@ -300,12 +314,8 @@ def run_ours(args):
     ctx.set_stage_timing(False)
     stats = ctx.last_stats()
     ms = sum(per_step) / len(per_step)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * band / (ms / 1000.0)
+    ms, band_all = combine_ranks(ms, band, world, "cuda")
+    value = band_all / (ms / 1000.0)
 
     # ---- e2e: host buffers through the C ABI, upload + export inside each step ----
     for _ in range(max(1, args.warmup // 2)):
@@ -317,7 +327,8 @@ def run_ours(args):
         b_e2e, h2d, d2h = step_e2e()
         ctx.synchronize()
         t_e2e.append(time.perf_counter() - t0)
-    e2e_value = world * b_e2e / (sum(t_e2e) / len(t_e2e))
+    e2e_ms, e2e_band = combine_ranks(1000.0 * sum(t_e2e) / len(t_e2e), b_e2e, world, "cuda")
+    e2e_value = e2e_band / (e2e_ms / 1000.0)
 
     # ---- roofline of the dominant kernel ----
     top = max(stages.items(), key=lambda kv: kv[1][0])
