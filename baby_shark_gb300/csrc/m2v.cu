@@ -677,24 +677,30 @@ __global__ void k_ploc_merge(Cluster* __restrict__ cl, uint32_t nc, const int* _
                              int* __restrict__ next_id, int2* __restrict__ child, int* __restrict__ parent_i,
                              int* __restrict__ parent_l, uint32_t* __restrict__ keep) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nc) {
-    if (i == nc) keep[nc] = 0u;
-    return;
-  }
-  const int j = nn[i];
-  if (j < 0 || nn[j] != int(i)) {
-    keep[i] = 1u;
-    return;
-  }
-  if (int(i) > j) {
-    keep[i] = 0u;
-    return;
+  const int j = i < nc ? nn[i] : -1;
+  const bool lead = j >= 0 && nn[j] == int(i) && int(i) < j;  // this lane creates a node
+  if (i == nc) keep[nc] = 0u;
+  if (i < nc && !lead) keep[i] = (j >= 0 && nn[j] == int(i)) ? 0u : 1u;
+  // node ids: one atomic per warp when all creating lanes belong to one mesh
+  const int m = lead ? cl[i].mesh : -1;
+  const unsigned warp_all = __activemask();
+  const unsigned creators = __ballot_sync(warp_all, lead);
+  if (!lead) return;
+  const int leader = __ffs(creators) - 1;
+  const int m0 = __shfl_sync(creators, m, leader);
+  int slot;
+  if (__all_sync(creators, m == m0)) {
+    int base = 0;
+    if ((threadIdx.x & 31) == leader) base = atomicAdd(&next_id[m], __popc(creators));
+    base = __shfl_sync(creators, base, leader);
+    slot = base + __popc(creators & ((1u << (threadIdx.x & 31)) - 1u));
+  } else {
+    slot = atomicAdd(&next_id[m], 1);
   }
   Cluster a = cl[i];
   const Cluster b = cl[j];
-  const int m = a.mesh;
   const int n = int(tri_base[m + 1] - tri_base[m]);
-  const int id = (n - 2) - atomicAdd(&next_id[m], 1);
+  const int id = (n - 2) - slot;
   const uint64_t ib = inode_base[m], lb = tri_base[m];
   child[ib + id] = make_int2(a.node, b.node);
   if (a.node >= 0) parent_i[ib + a.node] = id;
@@ -714,6 +720,140 @@ __global__ void k_ploc_compact(const Cluster* __restrict__ cl, uint32_t nc, cons
                                const uint32_t* __restrict__ pos, Cluster* __restrict__ out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < nc && keep[i]) out[pos[i]] = cl[i];
+}
+
+// Clusters per mesh (the array is sorted by mesh), and the largest count.
+__global__ void k_ploc_counts(const Cluster* __restrict__ cl, uint32_t nc, uint32_t* __restrict__ cnt,
+                              uint32_t* __restrict__ max_cnt, int K) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nc) {
+    const uint32_t c = atomicAdd(&cnt[cl[i].mesh], 1u) + 1u;
+    atomicMax(max_cnt, c);
+  }
+}
+
+// The last rounds of every mesh in one block per mesh, in shared memory (at
+// most PLOC_FIN clusters per mesh): the same nearest-neighbour, merge and
+// compaction steps as the global rounds, separated by block barriers.
+constexpr int PLOC_FIN = 2048;
+constexpr int PLOC_FIN_T = 512;
+
+__global__ void __launch_bounds__(PLOC_FIN_T) k_ploc_finish(const Cluster* __restrict__ cl, uint32_t nc,
+                                                            const uint32_t* __restrict__ tri_base,
+                                                            const uint32_t* __restrict__ inode_base,
+                                                            int* __restrict__ next_id, int2* __restrict__ child,
+                                                            int* __restrict__ parent_i, int* __restrict__ parent_l,
+                                                            int* __restrict__ err) {
+  extern __shared__ unsigned char fin_smem[];
+  Cluster* A = reinterpret_cast<Cluster*>(fin_smem);
+  Cluster* B = A + PLOC_FIN;
+  int* nn = reinterpret_cast<int*>(B + PLOC_FIN);
+  int* pos = nn + PLOC_FIN;
+  __shared__ int s_n, s_id;
+  __shared__ int wsum[PLOC_FIN_T / 32];
+  const int m = blockIdx.x;
+  // this mesh's segment [s0, s1) of the sorted cluster array
+  uint32_t lo = 0, hi = nc;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (cl[mid].mesh < m) lo = mid + 1;
+    else hi = mid;
+  }
+  const uint32_t s0 = lo;
+  hi = nc;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (cl[mid].mesh < m + 1) lo = mid + 1;
+    else hi = mid;
+  }
+  const int n0 = int(lo - s0);
+  if (n0 <= 1) return;
+  if (n0 > PLOC_FIN) {
+    if (threadIdx.x == 0) atomicExch(err, 1);
+    return;
+  }
+  for (int k = threadIdx.x; k < n0; k += PLOC_FIN_T) A[k] = cl[s0 + k];
+  if (threadIdx.x == 0) {
+    s_n = n0;
+    s_id = next_id[m];
+  }
+  __syncthreads();
+  const int n_tri = int(tri_base[m + 1] - tri_base[m]);
+  const uint64_t ib = inode_base[m], lb = tri_base[m];
+  for (int round = 0; round < 4096 && s_n > 1; ++round) {
+    const int n = s_n;
+    for (int i = threadIdx.x; i < n; i += PLOC_FIN_T) {
+      float best = INFINITY;
+      int bj = -1;
+      for (int d = -PLOC_R; d <= PLOC_R; ++d) {
+        const int j = i + d;
+        if (d == 0 || j < 0 || j >= n) continue;
+        const float a = merged_area(A[i], A[j]);
+        if (a < best) {
+          best = a;
+          bj = j;
+        }
+      }
+      nn[i] = bj;
+    }
+    __syncthreads();
+    // merge mutual pairs into B (position kept), flag survivors in pos
+    for (int i = threadIdx.x; i < n; i += PLOC_FIN_T) {
+      const int j = nn[i];
+      int keep = 1;
+      Cluster c = A[i];
+      if (j >= 0 && nn[j] == i) {
+        if (i > j) {
+          keep = 0;
+        } else {
+          const Cluster b = A[j];
+          const int id = (n_tri - 2) - atomicAdd(&s_id, 1);
+          child[ib + id] = make_int2(c.node, b.node);
+          if (c.node >= 0) parent_i[ib + c.node] = id;
+          else parent_l[lb + ~c.node] = id;
+          if (b.node >= 0) parent_i[ib + b.node] = id;
+          else parent_l[lb + ~b.node] = id;
+          for (int k = 0; k < 3; ++k) {
+            c.lo[k] = fminf(c.lo[k], b.lo[k]);
+            c.hi[k] = fmaxf(c.hi[k], b.hi[k]);
+          }
+          c.node = id;
+        }
+      }
+      B[i] = c;
+      pos[i] = keep;
+    }
+    __syncthreads();
+    // exclusive scan of pos over n <= PLOC_FIN entries: 4 per thread
+    const int t = threadIdx.x, base = 4 * t;
+    int v[4], local = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      v[k] = (base + k < n) ? pos[base + k] : 0;
+      local += v[k];
+    }
+    int incl = local;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, d);
+      if ((t & 31) >= d) incl += u;
+    }
+    if ((t & 31) == 31) wsum[t >> 5] = incl;
+    __syncthreads();
+    int woff = 0;
+    for (int w = 0; w < (t >> 5); ++w) woff += wsum[w];
+    int run = woff + incl - local;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (base + k < n) {
+        if (v[k]) A[run] = B[base + k];
+        run += v[k];
+      }
+    }
+    if (t == PLOC_FIN_T - 1) s_n = run;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && s_n != 1) atomicExch(err, 2);
 }
 
 __device__ __forceinline__ void sums_add(Sums& r, const Sums& a, const Sums& b) {
@@ -1321,7 +1461,27 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
       BS_CUDA(cudaMemsetAsync(next_id.p, 0, K * sizeof(int), s));
       BS_KERNEL(ctx, "k_ploc_init", (k_ploc_init<<<blocks(nt, 256), 256, 0, s>>>(lsum.p, nt, d_tb.p, K, ca.p)));
       uint32_t nc = uint32_t(nt);
+      DBuf<uint32_t> mcnt(ctx, K + 1);
+      DBuf<int> ferr(ctx, 1);
       for (int round = 0; nc > uint32_t(K); ++round) {
+        if (nc <= uint32_t(PLOC_FIN) * uint32_t(K)) {
+          // every mesh small enough: finish each in one block
+          BS_CUDA(cudaMemsetAsync(mcnt.p, 0, (K + 1) * sizeof(uint32_t), s));
+          BS_KERNEL(ctx, "k_ploc_counts", (k_ploc_counts<<<blocks(nc, 256), 256, 0, s>>>(ca.p, nc, mcnt.p, mcnt.p + K, K)));
+          uint32_t mx = 0;
+          read_back(ctx, &mx, mcnt.p + K, sizeof mx);
+          if (mx <= uint32_t(PLOC_FIN)) {
+            const size_t smem = 2 * PLOC_FIN * sizeof(Cluster) + 2 * PLOC_FIN * sizeof(int);
+            BS_CUDA(cudaFuncSetAttribute(k_ploc_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+            BS_CUDA(cudaMemsetAsync(ferr.p, 0, sizeof(int), s));
+            BS_KERNEL(ctx, "k_ploc_finish", (k_ploc_finish<<<unsigned(K), PLOC_FIN_T, smem, s>>>(ca.p, nc, d_tb.p, d_ib.p, next_id.p, child.p,
+                                                                                     parent_i.p, parent_l.p, ferr.p)));
+            int fe = 0;
+            read_back(ctx, &fe, ferr.p, sizeof fe);
+            if (fe) fail(BS_ERR_CAPACITY, "tree build did not converge");
+            break;
+          }
+        }
         if (round >= 4096) fail(BS_ERR_CAPACITY, "tree build did not converge");
         BS_KERNEL(ctx, "k_ploc_nn", (k_ploc_nn<<<blocks(nc, PLOC_T), PLOC_T, 0, s>>>(ca.p, nc, nn.p)));
         BS_KERNEL(ctx, "k_ploc_merge", (k_ploc_merge<<<blocks(nc + 1, 256), 256, 0, s>>>(ca.p, nc, nn.p, d_tb.p, d_ib.p, next_id.p, child.p,
