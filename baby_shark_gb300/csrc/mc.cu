@@ -1,5 +1,5 @@
 // Marching-cubes surface extraction (MarchingCubesMesher::mesh,
-// voxel/meshing/marching_cubes.rs:43-63, 967-1181) for volumes without tiles.
+// voxel/meshing/marching_cubes.rs:43-63, 967-1181).
 //
 // Kept from the reference: the cubes (one per voxel of every leaf, its eight
 // corners (0,0,0) (1,0,0) (1,1,0) (0,1,0) (0,0,1) (1,0,1) (1,1,1) (0,1,1) all
@@ -21,11 +21,16 @@
 //
 // One warp per leaf stages the leaf and the +x, +y, +z neighbour layers in a
 // 9 x 9 x 9 shared tile; a count pass, a scan and a write pass place the
-// triangles of every leaf, lane and cube in a fixed order.
+// triangles of every leaf, lane and cube in a fixed order.  Active tiles
+// (after booleans) are values too: a corner outside every leaf takes the
+// value of the active tile holding it, and the cubes on the six boundary
+// faces of every tile are meshed as the reference's tile visitor does
+// (marching_cubes.rs:969-994, cubes on a tile's edges visited once per face).
 #include <cub/device/device_scan.cuh>
 
 #include "bs_internal.cuh"
 #include "leaf_hash.cuh"
+#include "volume_upper.cuh"
 
 namespace bs {
 
@@ -52,17 +57,60 @@ struct McVol {
   LeafHash hash;
 };
 
+// Active tiles of the internal levels: node origin -> node index hashes and
+// the slot tables (state -2 = active tile, value in tile[]).
+struct McTiles {
+  LeafHash h1, h2;
+  const int* s1;
+  const float* t1;
+  const int* s2;
+  const float* t2;
+  int any;
+};
+
+// Value of voxel (x, y, z) from an active tile, for a voxel outside every leaf.
+__device__ __forceinline__ bool tile_value(const McTiles& T, int x, int y, int z, float& v) {
+  if (!T.any) return false;
+  const int n1 = T.h1.find(x & ~127, y & ~127, z & ~127);
+  if (n1 >= 0) {
+    const int slot = (((x >> 3) & 15) << 8) | (((y >> 3) & 15) << 4) | ((z >> 3) & 15);
+    const uint64_t k = uint64_t(n1) * L1_SLOTS + slot;
+    if (T.s1[k] != -2) return false;
+    v = T.t1[k];
+    return true;
+  }
+  const int n2 = T.h2.find(x & ~4095, y & ~4095, z & ~4095);
+  if (n2 < 0) return false;
+  const int slot = (((x >> 7) & 31) << 10) | (((y >> 7) & 31) << 5) | ((z >> 7) & 31);
+  const uint64_t k = uint64_t(n2) * L2_SLOTS + slot;
+  if (T.s2[k] != -2) return false;
+  v = T.t2[k];
+  return true;
+}
+
+// Value of an arbitrary voxel: its leaf decides when it has one (inactive =
+// absent, Grid::at), else an active tile.
+__device__ __forceinline__ float value_at(const McVol& V, const McTiles& T, int x, int y, int z) {
+  const int l = V.hash.find(x & ~7, y & ~7, z & ~7);
+  if (l >= 0) {
+    const int o = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
+    return ((V.msk[uint64_t(l) * 16 + (o >> 5)] >> (o & 31)) & 1u) ? V.val[uint64_t(l) * 512 + o] : INFINITY;
+  }
+  float v;
+  return tile_value(T, x, y, z, v) ? v : INFINITY;
+}
+
 __device__ __forceinline__ int t9(int x, int y, int z) { return (x * T9 + y) * T9 + z; }
 
-// Triangles of one cube: returns the count; writes them when `out` is set.
-__device__ int cube_tris(const float* W, int x, int y, int z, int4 org, float h, float* out) {
-  float raw[8], v[8];
+// Triangles of the cube at absolute voxel (x, y, z) with corner values
+// raw[8] (+inf = not active): returns the count; writes them when `out` is set.
+__device__ int cube_tris(const float* raw, int x, int y, int z, float h, float* out) {
+  float v[8];
   uint32_t in = 0;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    const float r = W[t9(x + c_corner[i][0], y + c_corner[i][1], z + c_corner[i][2])];
+    const float r = raw[i];
     if (r == INFINITY) return 0;  // a corner is not active: no cube (Cube::from_voxel)
-    raw[i] = r;
     v[i] = fabsf(r) < 1e-6f ? copysignf(1e-6f, r) : r;
     if (v[i] < 0.0f) in |= 1u << i;
   }
@@ -113,7 +161,7 @@ __device__ int cube_tris(const float* W, int x, int y, int z, int4 org, float h,
       const int e = poly[i], a = c_edge[e][0], b = c_edge[e][1];
       const float va = fmaxf(fabsf(raw[a]), 1e-6f), vb = fmaxf(fabsf(raw[b]), 1e-6f);
       const float t = fdiv(va, fadd(va, vb));
-      float q[3] = {float(org.x + x + c_corner[a][0]), float(org.y + y + c_corner[a][1]), float(org.z + z + c_corner[a][2])};
+      float q[3] = {float(x + c_corner[a][0]), float(y + c_corner[a][1]), float(z + c_corner[a][2])};
       const int ax = c_edge_axis[e];
       q[ax] = fadd(q[ax], t);
       p[i] = f3(fmul(q[0], h), fmul(q[1], h), fmul(q[2], h));
@@ -138,9 +186,17 @@ __device__ int cube_tris(const float* W, int x, int y, int z, int4 org, float h,
   return count;
 }
 
+__device__ __forceinline__ int leaf_cube(const float* W, int x, int y, int z, int4 org, float h, float* out) {
+  float raw[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) raw[i] = W[t9(x + c_corner[i][0], y + c_corner[i][1], z + c_corner[i][2])];
+  return cube_tris(raw, org.x + x, org.y + y, org.z + z, h, out);
+}
+
 // One warp per leaf.  Pass 1 (tris == nullptr) stores each leaf's triangle
 // count; pass 2 writes them from the leaf's scanned offset.
-__global__ void __launch_bounds__(32 * MC_WARPS) k_mc(McVol V, uint64_t n, float h, uint32_t* __restrict__ leaf_count,
+__global__ void __launch_bounds__(32 * MC_WARPS) k_mc(McVol V, McTiles T, uint64_t n, float h,
+                                                     uint32_t* __restrict__ leaf_count,
                                                      const uint32_t* __restrict__ leaf_off, float* __restrict__ tris) {
   __shared__ float tile[MC_WARPS][T9 * T9 * T9];
   __shared__ int snb[MC_WARPS][8];
@@ -175,6 +231,9 @@ __global__ void __launch_bounds__(32 * MC_WARPS) k_mc(McVol V, uint64_t n, float
     if (n_leaf >= 0) {
       const int o = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
       if ((V.msk[uint64_t(n_leaf) * 16 + (o >> 5)] >> (o & 31)) & 1u) val = V.val[uint64_t(n_leaf) * 512 + o];
+    } else {
+      float tv;
+      if (tile_value(T, org.x + x, org.y + y, org.z + z, tv)) val = tv;
     }
     W[t9(x, y, z)] = val;
   }
@@ -182,7 +241,7 @@ __global__ void __launch_bounds__(32 * MC_WARPS) k_mc(McVol V, uint64_t n, float
   uint32_t mine = 0;
   for (int j = 0; j < 16; ++j) {
     const int o = 32 * j + lane;
-    mine += uint32_t(cube_tris(W, o >> 6, (o >> 3) & 7, o & 7, org, h, nullptr));
+    mine += uint32_t(leaf_cube(W, o >> 6, (o >> 3) & 7, o & 7, org, h, nullptr));
   }
   if (!tris) {
     uint32_t s = mine;
@@ -198,8 +257,61 @@ __global__ void __launch_bounds__(32 * MC_WARPS) k_mc(McVol V, uint64_t n, float
   uint64_t at = uint64_t(leaf_off[leaf]) + (incl - mine);
   for (int j = 0; j < 16; ++j) {
     const int o = 32 * j + lane;
-    at += uint64_t(cube_tris(W, o >> 6, (o >> 3) & 7, o & 7, org, h, tris + 9 * at));
+    at += uint64_t(leaf_cube(W, o >> 6, (o >> 3) & 7, o & 7, org, h, tris + 9 * at));
   }
+}
+
+// Cubes of the tiles' boundary faces (marching_cubes.rs:969-994): for tile
+// t of size s, cube c in [cbase[t], cbase[t + 1]) is face f = r / s^2 of
+// (left, right, top, bottom, front, back) at (i, j) = ((r % s^2) / s, r % s).
+__global__ void k_mc_tiles(McVol V, McTiles T, const int4* __restrict__ tiles, const uint64_t* __restrict__ cbase,
+                           int n_tiles, uint64_t n_cubes, float h, uint32_t* __restrict__ count,
+                           const uint64_t* __restrict__ off, float* __restrict__ tris) {
+  const uint64_t c = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (c >= n_cubes) return;
+  int lo = 0, hi = n_tiles - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (cbase[mid] <= c) lo = mid;
+    else hi = mid - 1;
+  }
+  const int4 t = tiles[lo];
+  const int s = t.w;
+  const uint64_t r = c - cbase[lo], s2 = uint64_t(s) * s;
+  const int f = int(r / s2);
+  const int i = int((r % s2) / s), j = int(r % s);
+  int x, y, z;
+  switch (f) {
+    case 0: x = 0; y = i; z = j; break;          // left
+    case 1: x = s - 1; y = i; z = j; break;      // right
+    case 2: x = i; y = j; z = s - 1; break;      // top
+    case 3: x = i; y = j; z = 0; break;          // bottom
+    case 4: x = i; y = s - 1; z = j; break;      // front
+    default: x = i; y = 0; z = j; break;         // back
+  }
+  x += t.x;
+  y += t.y;
+  z += t.z;
+  float raw[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) raw[k] = value_at(V, T, x + c_corner[k][0], y + c_corner[k][1], z + c_corner[k][2]);
+  if (!tris) {
+    count[c] = uint32_t(cube_tris(raw, x, y, z, h, nullptr));
+  } else if (off[c + 1] > off[c]) {
+    cube_tris(raw, x, y, z, h, tris + 9 * off[c]);
+  }
+}
+
+__global__ void k_tile_cube_counts(const int4* __restrict__ tiles, int n, uint64_t* __restrict__ cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) cnt[i] = 6ull * uint64_t(tiles[i].w) * uint64_t(tiles[i].w);
+  if (i == n) cnt[n] = 0;
+}
+
+__global__ void k_widen(const uint32_t* __restrict__ in, uint64_t n, uint64_t* __restrict__ out) {
+  const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i < n) out[i] = in[i];
+  if (i == n) out[n] = 0;
 }
 
 }  // namespace
@@ -208,37 +320,82 @@ __global__ void __launch_bounds__(32 * MC_WARPS) k_mc(McVol V, uint64_t n, float
 // triangles stay cached on the volume until it changes.
 void marching_cubes_impl(bs_ctx* ctx, bs_volume* v, float voxel_size) {
   if (v->mc_valid && v->mc_h == voxel_size) return;
-  if (v->n_tiles) fail(BS_ERR_UNSUPPORTED, "marching cubes: volumes with active tiles are not supported");
   cudaStream_t s = ctx->stream;
   dfree(ctx, v->d_mc_tris);
   v->d_mc_tris = nullptr;
   v->n_mc_tris = 0;
-  const uint64_t n = v->n_leaves;
-  if (n == 0) {
+  const uint64_t n = v->n_leaves, ntl = v->n_tiles;
+  if (n == 0 && ntl == 0) {
     v->mc_valid = true;
     v->mc_h = voxel_size;
     return;
   }
-  LeafHashBuf hb;
+  LeafHashBuf hb, h1, h2;
   hb.build(ctx, v->d_origins, n, n);
   McVol V{v->d_origins, v->d_values, v->d_masks, hb.h};
-  DBuf<uint32_t> cnt(ctx, n + 1), off(ctx, n + 1);
-  BS_CUDA(cudaMemsetAsync(cnt.p + n, 0, sizeof(uint32_t), s));
+  McTiles T{};
+  T.any = 0;
+  if (ntl) {
+    const Upper* u = v->upper;
+    if (!u) fail(BS_ERR_UNSUPPORTED, "marching cubes: tiles without internal levels");
+    h1.build(ctx, u->l1.d_key, u->l1.n, u->l1.n);
+    h2.build(ctx, u->l2.d_key, u->l2.n, u->l2.n);
+    T = McTiles{h1.h, h2.h, u->l1.d_state, u->l1.d_tile, u->l2.d_state, u->l2.d_tile, 1};
+  }
+  // leaves: count, scan, (write below)
+  uint32_t nt_leaf = 0;
+  DBuf<uint32_t> cnt, off;
   const unsigned grid = unsigned((n + MC_WARPS - 1) / MC_WARPS);
-  BS_KERNEL(ctx, "k_mc_count", (k_mc<<<grid, 32 * MC_WARPS, 0, s>>>(V, n, voxel_size, cnt.p, nullptr, nullptr)));
-  size_t tmp = 0;
-  BS_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, cnt.p, off.p, n + 1, s));
-  {
+  if (n) {
+    cnt = DBuf<uint32_t>(ctx, n + 1);
+    off = DBuf<uint32_t>(ctx, n + 1);
+    BS_CUDA(cudaMemsetAsync(cnt.p + n, 0, sizeof(uint32_t), s));
+    BS_KERNEL(ctx, "k_mc_count", (k_mc<<<grid, 32 * MC_WARPS, 0, s>>>(V, T, n, voxel_size, cnt.p, nullptr, nullptr)));
+    size_t tmp = 0;
+    BS_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, cnt.p, off.p, n + 1, s));
     DBuf<uint8_t> t(ctx, tmp);
     BS_CUDA(cub::DeviceScan::ExclusiveSum(t.p, tmp, cnt.p, off.p, n + 1, s));
+    read_back(ctx, &nt_leaf, off.p + n, sizeof nt_leaf);
   }
-  uint32_t nt = 0;
-  read_back(ctx, &nt, off.p + n, sizeof nt);
-  if (nt) {
-    v->d_mc_tris = dalloc<float>(ctx, uint64_t(nt) * 9);
-    BS_KERNEL(ctx, "k_mc_write", (k_mc<<<grid, 32 * MC_WARPS, 0, s>>>(V, n, voxel_size, nullptr, off.p, v->d_mc_tris)));
+  // tile boundary cubes: count, scan
+  uint64_t n_cubes = 0, nt_tile = 0;
+  DBuf<uint64_t> cbase, toff;
+  if (ntl) {
+    DBuf<uint64_t> tc(ctx, ntl + 1);
+    cbase = DBuf<uint64_t>(ctx, ntl + 1);
+    BS_KERNEL(ctx, "k_tile_cube_counts", (k_tile_cube_counts<<<unsigned((ntl + 256) / 256), 256, 0, s>>>(v->d_tiles, int(ntl), tc.p)));
+    size_t tmp = 0;
+    BS_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, tc.p, cbase.p, ntl + 1, s));
+    {
+      DBuf<uint8_t> t(ctx, tmp);
+      BS_CUDA(cub::DeviceScan::ExclusiveSum(t.p, tmp, tc.p, cbase.p, ntl + 1, s));
+    }
+    read_back(ctx, &n_cubes, cbase.p + ntl, sizeof n_cubes);
+    if (n_cubes) {
+      DBuf<uint32_t> cc(ctx, n_cubes);
+      DBuf<uint64_t> c64(ctx, n_cubes + 1);
+      toff = DBuf<uint64_t>(ctx, n_cubes + 1);
+      BS_KERNEL(ctx, "k_mc_tiles_count", (k_mc_tiles<<<unsigned((n_cubes + 255) / 256), 256, 0, s>>>(V, T, v->d_tiles, cbase.p, int(ntl), n_cubes,
+                                                                                        voxel_size, cc.p, nullptr, nullptr)));
+      BS_KERNEL(ctx, "k_widen", (k_widen<<<unsigned((n_cubes + 256) / 256), 256, 0, s>>>(cc.p, n_cubes, c64.p)));
+      tmp = 0;
+      BS_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, c64.p, toff.p, n_cubes + 1, s));
+      DBuf<uint8_t> t(ctx, tmp);
+      BS_CUDA(cub::DeviceScan::ExclusiveSum(t.p, tmp, c64.p, toff.p, n_cubes + 1, s));
+      read_back(ctx, &nt_tile, toff.p + n_cubes, sizeof nt_tile);
+    }
   }
-  v->n_mc_tris = nt;
+  const uint64_t total = uint64_t(nt_leaf) + nt_tile;
+  if (total) {
+    v->d_mc_tris = dalloc<float>(ctx, total * 9);
+    if (nt_leaf)
+      BS_KERNEL(ctx, "k_mc_write", (k_mc<<<grid, 32 * MC_WARPS, 0, s>>>(V, T, n, voxel_size, nullptr, off.p, v->d_mc_tris)));
+    if (nt_tile)
+      BS_KERNEL(ctx, "k_mc_tiles_write", (k_mc_tiles<<<unsigned((n_cubes + 255) / 256), 256, 0, s>>>(V, T, v->d_tiles, cbase.p, int(ntl), n_cubes,
+                                                                                        voxel_size, nullptr, toff.p,
+                                                                                        v->d_mc_tris + 9 * uint64_t(nt_leaf))));
+  }
+  v->n_mc_tris = total;
   v->mc_valid = true;
   v->mc_h = voxel_size;
 }

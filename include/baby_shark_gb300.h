@@ -179,8 +179,8 @@ bs_status bs_volume_iwp(bs_ctx* ctx, float voxel_size, const float* min3, const 
                         bs_volume** out);
 
 /* --------------------------------------------------- marching cubes ---- */
-/* MarchingCubesMesher::with_voxel_size(..).mesh(&volume) (marching_cubes.rs:30-63)
- * for a volume without active tiles (BS_ERR_UNSUPPORTED otherwise).  Same
+/* MarchingCubesMesher::with_voxel_size(..).mesh(&volume) (marching_cubes.rs:30-63,
+ * 969-1011), active tiles included (the cubes on their boundary faces).  Same
  * calling convention as bs_dual_contour: capacity 0 sizes the buffer, the
  * result is cached on the volume.  Cubes, corner values and edge
  * intersections are the reference's; the tiling inside a cube is this

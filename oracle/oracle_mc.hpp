@@ -1,6 +1,6 @@
 // ORACLE — test infrastructure only (see oracle_core.hpp).
 //
-// Marching-cubes surface of a leaf-only volume, as the GPU mesher builds it:
+// Marching-cubes surface of a volume, as the GPU mesher builds it:
 // the reference's cube enumeration, corner values and edge intersections
 // (voxel/meshing/marching_cubes.rs:967-1181), polygons from face segments
 // directed around each face's outward normal, the bilinear asymptotic
@@ -111,7 +111,9 @@ inline void mc_cube_tris(const Grid& g, const I3& vox, float voxel_size, std::ve
   }
 }
 
-// MarchingCubesMesher::mesh for a volume without tiles (marching_cubes.rs:43-63).
+// MarchingCubesMesher::mesh (marching_cubes.rs:43-63, 969-1011): every cube of
+// every leaf, then the cubes on the six faces of every active tile, in the
+// reference's visiting order (a cube on a tile's edge is visited once per face).
 inline std::vector<float> mc_mesh(const Grid& g, float voxel_size) {
   std::vector<float> out;
   g.visit_leafs(
@@ -120,7 +122,17 @@ inline std::vector<float> mc_mesh(const Grid& g, float voxel_size) {
           for (int b = 0; b < 8; ++b)
             for (int c = 0; c < 8; ++c) mc_cube_tris(g, i3(l.origin.x + a, l.origin.y + b, l.origin.z + c), voxel_size, out);
       },
-      [](I3, int, float) {});
+      [&](I3 o, int s, float) {
+        for (int i = 0; i < s; ++i)
+          for (int j = 0; j < s; ++j) {
+            mc_cube_tris(g, i3(o.x, o.y + i, o.z + j), voxel_size, out);          // left
+            mc_cube_tris(g, i3(o.x + s - 1, o.y + i, o.z + j), voxel_size, out);  // right
+            mc_cube_tris(g, i3(o.x + i, o.y + j, o.z + s - 1), voxel_size, out);  // top
+            mc_cube_tris(g, i3(o.x + i, o.y + j, o.z), voxel_size, out);          // bottom
+            mc_cube_tris(g, i3(o.x + i, o.y + s - 1, o.z + j), voxel_size, out);  // front
+            mc_cube_tris(g, i3(o.x + i, o.y, o.z + j), voxel_size, out);          // back
+          }
+      });
   return out;
 }
 

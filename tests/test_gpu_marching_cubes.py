@@ -76,7 +76,9 @@ def test_builder_sphere_and_cache():
     assert_same(g, o, h)
 
 
-def test_tiles_unsupported():
+def test_union_with_tiles():
+    """A union with active inside tiles: the tiles' boundary cubes are meshed
+    (marching_cubes.rs:969-994) and the result equals the oracle's."""
     va, fa = synthetic.icosphere(3, 0.6, 0.02, seed=11)
     vb, fb = synthetic.icosphere(3, 0.5, 0.02, seed=12)
     vb = vb + np.array([0.45, 0.1, -0.05], np.float32)
@@ -85,9 +87,11 @@ def test_tiles_unsupported():
     b = bs.MeshToVolume(ctx).with_voxel_size(0.02).with_narrow_band_width(3).convert((vb, fb))
     u = a.union(b)
     assert u.counts()["tiles"] > 0
-    with pytest.raises(bs.BsError) as e:
-        bs.MarchingCubesMesher().with_voxel_size(0.02).mesh(u)
-    assert e.value.status == 7
+    oa, _, _ = ob.mesh_to_volume(va, fa, 0.02, 3)
+    obb, _, _ = ob.mesh_to_volume(vb, fb, 0.02, 3)
+    ou = oa.union(obb)
+    gt = assert_same(u, ou, 0.02)
+    assert len(gt) > 1000
 
 
 def test_voxel_remesher_manifold_default():
