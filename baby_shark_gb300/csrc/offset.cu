@@ -92,16 +92,21 @@ __global__ void k_remove_far(const float* __restrict__ values, uint32_t* __restr
   if (b == n - 1 && lane == 0) keep[n] = 0u;
 }
 
-__global__ void k_gather_leaves(const uint32_t* __restrict__ keep, const uint32_t* __restrict__ pos, uint64_t n,
-                                const int4* __restrict__ oi, const float* __restrict__ vi, const uint32_t* __restrict__ mi,
-                                int4* __restrict__ oo, float* __restrict__ vo, uint32_t* __restrict__ mo) {
-  const uint64_t b = blockIdx.x;
+// Leaf copies: LEAVES_PER_BLOCK leaves per block of 128 threads each, one
+// float4 of a leaf's values per thread (one leaf per block measured fastest).
+constexpr int LEAVES_PER_BLOCK = 1;
+
+__global__ void __launch_bounds__(128 * LEAVES_PER_BLOCK) k_gather_leaves(
+    const uint32_t* __restrict__ keep, const uint32_t* __restrict__ pos, uint64_t n, const int4* __restrict__ oi,
+    const float* __restrict__ vi, const uint32_t* __restrict__ mi, int4* __restrict__ oo, float* __restrict__ vo,
+    uint32_t* __restrict__ mo) {
+  const uint64_t b = blockIdx.x * uint64_t(LEAVES_PER_BLOCK) + (threadIdx.x >> 7);
+  const int t = threadIdx.x & 127;
   if (b >= n || !keep[b]) return;
   const uint64_t d = pos[b];
-  for (int t = threadIdx.x; t < 128; t += blockDim.x)
-    reinterpret_cast<float4*>(vo + d * 512)[t] = reinterpret_cast<const float4*>(vi + b * 512)[t];
-  if (threadIdx.x < 16) mo[d * 16 + threadIdx.x] = mi[b * 16 + threadIdx.x];
-  if (threadIdx.x == 0) oo[d] = oi[b];
+  reinterpret_cast<float4*>(vo + d * 512)[t] = reinterpret_cast<const float4*>(vi + b * 512)[t];
+  if (t < 16) mo[d * 16 + t] = mi[b * 16 + t];
+  if (t == 0) oo[d] = oi[b];
 }
 
 // --------------------------------------------------------------- sweeps ----
@@ -445,7 +450,8 @@ __global__ void __launch_bounds__(128) k_sweep_init(Sweep S, int n, int* list, i
   if (l >= n) return;
   const float* iv = S.in_val + uint64_t(l) * 512;
   const uint32_t* im = S.in_msk + uint64_t(l) * 16;
-  for (int k = lane; k < 512; k += 32) S.out_val[uint64_t(l) * 512 + k] = iv[k];
+  for (int k = lane; k < 128; k += 32)
+    reinterpret_cast<float4*>(S.out_val + uint64_t(l) * 512)[k] = reinterpret_cast<const float4*>(iv)[k];
   if (lane < 16) S.out_msk[uint64_t(l) * 16 + lane] = im[lane];
   const int sdir[3] = {S.sx, S.sy, S.sz};
   for (int ax = 0; ax < 3; ++ax) {
@@ -545,16 +551,16 @@ __global__ void k_leaf_keys(const int4* __restrict__ org, uint64_t n, unsigned l
   idx[i] = uint32_t(i);
 }
 
-__global__ void k_permute_leaves(const uint32_t* __restrict__ perm, uint64_t n, const int4* __restrict__ oi,
-                                 const float* __restrict__ vi, const uint32_t* __restrict__ mi, int4* __restrict__ oo,
-                                 float* __restrict__ vo, uint32_t* __restrict__ mo) {
-  const uint64_t d = blockIdx.x;
+__global__ void __launch_bounds__(128 * LEAVES_PER_BLOCK) k_permute_leaves(
+    const uint32_t* __restrict__ perm, uint64_t n, const int4* __restrict__ oi, const float* __restrict__ vi,
+    const uint32_t* __restrict__ mi, int4* __restrict__ oo, float* __restrict__ vo, uint32_t* __restrict__ mo) {
+  const uint64_t d = blockIdx.x * uint64_t(LEAVES_PER_BLOCK) + (threadIdx.x >> 7);
+  const int t = threadIdx.x & 127;
   if (d >= n) return;
   const uint64_t s = perm[d];
-  for (int t = threadIdx.x; t < 128; t += blockDim.x)
-    reinterpret_cast<float4*>(vo + d * 512)[t] = reinterpret_cast<const float4*>(vi + s * 512)[t];
-  if (threadIdx.x < 16) mo[d * 16 + threadIdx.x] = mi[s * 16 + threadIdx.x];
-  if (threadIdx.x == 0) oo[d] = oi[s];
+  reinterpret_cast<float4*>(vo + d * 512)[t] = reinterpret_cast<const float4*>(vi + s * 512)[t];
+  if (t < 16) mo[d * 16 + t] = mi[s * 16 + t];
+  if (t == 0) oo[d] = oi[s];
 }
 
 __global__ void k_count_bits(const uint32_t* __restrict__ m, uint64_t n_words, unsigned long long* out) {
@@ -578,7 +584,7 @@ static uint64_t compact_nonempty(bs_ctx* ctx, bs_volume* v, float remove_above) 
   int4* o2 = dalloc<int4>(ctx, m);
   float* v2 = dalloc<float>(ctx, uint64_t(m) * 512);
   uint32_t* m2 = dalloc<uint32_t>(ctx, uint64_t(m) * 16);
-  BS_KERNEL(ctx, "k_gather_leaves", (k_gather_leaves<<<unsigned(n), 128, 0, s>>>(keep.p, pos.p, n, v->d_origins, v->d_values, v->d_masks, o2, v2, m2)));
+  BS_KERNEL(ctx, "k_gather_leaves", (k_gather_leaves<<<nb_(n, LEAVES_PER_BLOCK), 128 * LEAVES_PER_BLOCK, 0, s>>>(keep.p, pos.p, n, v->d_origins, v->d_values, v->d_masks, o2, v2, m2)));
   dfree(ctx, v->d_origins);
   dfree(ctx, v->d_values);
   dfree(ctx, v->d_masks);
@@ -758,7 +764,7 @@ void volume_offset_impl(bs_ctx* ctx, bs_volume* v, float distance) {
     int4* o2 = dalloc<int4>(ctx, n);
     float* v2 = dalloc<float>(ctx, n * 512);
     uint32_t* m2 = dalloc<uint32_t>(ctx, n * 16);
-    BS_KERNEL(ctx, "k_permute_leaves", (k_permute_leaves<<<unsigned(n), 128, 0, s>>>(perm.p, n, v->d_origins, v->d_values, v->d_masks, o2, v2, m2)));
+    BS_KERNEL(ctx, "k_permute_leaves", (k_permute_leaves<<<nb_(n, LEAVES_PER_BLOCK), 128 * LEAVES_PER_BLOCK, 0, s>>>(perm.p, n, v->d_origins, v->d_values, v->d_masks, o2, v2, m2)));
     dfree(ctx, v->d_origins);
     dfree(ctx, v->d_values);
     dfree(ctx, v->d_masks);
