@@ -337,23 +337,32 @@ def winding_numbers_exact(vertices, triangles, points, ctx=None):
 
 
 class DualContouringMesher:
-    """DualContouringMesher (voxel/meshing/dual_contouring.rs:12-91)."""
+    """DualContouringMesher (voxel/meshing/dual_contouring.rs:12-91).
+
+    with_qef_vertices() switches the cell vertices from the reference's
+    particle solver to a float64 quadratic-error solve (bs_dual_contour_qef),
+    an extension without a reference counterpart."""
 
     def __init__(self):
         self.voxel_size = 1.0
+        self.qef = False
 
     def with_voxel_size(self, size):
         self.voxel_size = float(size)
         return self
 
+    def with_qef_vertices(self, on=True):
+        self.qef = bool(on)
+        return self
+
     def mesh(self, volume):
         """Triangle soup as float32[n, 3, 3] in world units."""
         L = N.load()
+        fn = L.bs_dual_contour_qef if self.qef else L.bs_dual_contour
         n = C.c_uint64()
-        N.check(L.bs_dual_contour(volume.ctx.h, volume.h, self.voxel_size, None, 0, C.byref(n)), volume.ctx.h)
+        N.check(fn(volume.ctx.h, volume.h, self.voxel_size, None, 0, C.byref(n)), volume.ctx.h)
         out = np.zeros((max(n.value, 1), 3, 3), np.float32)
-        N.check(L.bs_dual_contour(volume.ctx.h, volume.h, self.voxel_size, out.ctypes.data, n.value, C.byref(n)),
-                volume.ctx.h)
+        N.check(fn(volume.ctx.h, volume.h, self.voxel_size, out.ctypes.data, n.value, C.byref(n)), volume.ctx.h)
         return out[: n.value]
 
 

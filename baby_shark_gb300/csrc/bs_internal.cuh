@@ -165,6 +165,7 @@ struct bs_volume {
   uint64_t n_dc_tris = 0;
   bool dc_valid = false;
   float dc_h = 0.0f;
+  int dc_mode = 0;
   // cached marching-cubes output (world-unit triangles)
   float* d_mc_tris = nullptr;
   uint64_t n_mc_tris = 0;
@@ -329,5 +330,6 @@ bs_volume* volume_from_samples_impl(bs_ctx* ctx, float h, long long band_width, 
                                     const unsigned long long dims[3], const float* d_values);
 bs_volume* volume_csg_impl(bs_ctx* ctx, bs_volume* a, bs_volume* b, int op);
 void volume_offset_impl(bs_ctx* ctx, bs_volume* v, float distance);
-void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size);
+// mode 0: the reference's particle solver; 1: the float64 QEF vertex
+void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size, int mode = 0);
 }  // namespace bs

@@ -424,6 +424,20 @@ bs_status bs_dual_contour(bs_ctx* ctx, bs_volume* v, float voxel_size, float* h_
   });
 }
 
+bs_status bs_dual_contour_qef(bs_ctx* ctx, bs_volume* v, float voxel_size, float* h_tris, uint64_t capacity,
+                              uint64_t* n_tris) {
+  if (!ctx || !v || !n_tris || v->ctx != ctx || (capacity && !h_tris)) return BS_ERR_INVALID_ARG;
+  return guarded(ctx, [&] {
+    bs::dual_contour_impl(ctx, v, voxel_size, 1);
+    *n_tris = v->n_dc_tris;
+    if (capacity >= v->n_dc_tris && v->n_dc_tris) {
+      BS_CUDA(cudaMemcpyAsync(h_tris, v->d_dc_tris, v->n_dc_tris * 9 * sizeof(float), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+      BS_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+  });
+}
+
 bs_status bs_marching_cubes(bs_ctx* ctx, bs_volume* v, float voxel_size, float* h_tris, uint64_t capacity,
                             uint64_t* n_tris) {
   if (!ctx || !v || !n_tris || v->ctx != ctx || (capacity && !h_tris)) return BS_ERR_INVALID_ARG;

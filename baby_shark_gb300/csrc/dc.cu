@@ -279,6 +279,99 @@ __global__ void __launch_bounds__(128) k_dc_cell_points(DcVol V, uint64_t n, con
   }
 }
 
+// Eigen-decomposition of a symmetric 3x3 matrix by cyclic Jacobi rotations
+// (Jacobi 1846; Rutishauser's update): a is overwritten, w = eigenvalues,
+// columns of V = eigenvectors.
+__device__ __forceinline__ void sym3_jacobi(double a[3][3], double V[3][3], double w[3]) {
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) V[r][c] = r == c ? 1.0 : 0.0;
+  const int P[3] = {0, 0, 1}, Q[3] = {1, 2, 2};
+  for (int sweep = 0; sweep < 24; ++sweep) {
+    const double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+    const double dia = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+    if (off <= 1e-30 * dia || off == 0.0) break;
+    for (int k = 0; k < 3; ++k) {
+      const int p = P[k], q = Q[k];
+      const double apq = a[p][q];
+      if (apq == 0.0) continue;
+      const double theta = (a[q][q] - a[p][p]) / (2.0 * apq);
+      const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+      const double c = 1.0 / sqrt(t * t + 1.0), s = t * c, tau = s / (1.0 + c);
+      a[p][p] -= t * apq;
+      a[q][q] += t * apq;
+      a[p][q] = a[q][p] = 0.0;
+      for (int r = 0; r < 3; ++r) {
+        if (r != p && r != q) {
+          const double arp = a[r][p], arq = a[r][q];
+          a[r][p] = a[p][r] = arp - s * (arq + tau * arp);
+          a[r][q] = a[q][r] = arq + s * (arp - tau * arq);
+        }
+        const double vrp = V[r][p], vrq = V[r][q];
+        V[r][p] = vrp - s * (vrq + tau * vrp);
+        V[r][q] = vrq + s * (vrp - tau * vrq);
+      }
+    }
+  }
+  for (int k = 0; k < 3; ++k) w[k] = a[k][k];
+}
+
+// Pass 2b, QEF mode (no reference counterpart): the point minimising
+// sum_i (n_i . (x - p_i))^2 over the cell's crossings p_i with normals n_i,
+// taken as m + pinv(A^T A) (A^T b - A^T A m) around the crossings' mass
+// point m, with eigenvalues below QEF_TRUNC of the largest dropped; all in
+// double.
+constexpr double QEF_TRUNC = 0.1;
+
+__global__ void __launch_bounds__(128) k_dc_cell_qef(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
+                                                     const uint32_t* __restrict__ coff, const float* __restrict__ pts,
+                                                     const uint32_t* __restrict__ cellm,
+                                                     const uint32_t* __restrict__ celloff, float* __restrict__ cells) {
+  __shared__ int nb[27];
+  const uint64_t l = blockIdx.x;
+  if (l >= n) return;
+  const int4 org = V.org[l];
+  load_neighbours(V, org, nb);
+  __syncthreads();
+  const uint32_t* m = cellm + l * 16;
+  for (int o = threadIdx.x; o < 512; o += blockDim.x) {
+    if (!((m[o >> 5] >> (o & 31)) & 1u)) continue;
+    const int x = o >> 6, y = (o >> 3) & 7, z = o & 7;
+    double mp[3] = {0.0, 0.0, 0.0}, ata[3][3] = {{0.0}}, atb[3] = {0.0, 0.0, 0.0};
+    int np = 0;
+    for (int e = 0; e < 12; ++e) {
+      const float* q = edge_point(nb, cm, coff, pts, x + c_edges[e][0], y + c_edges[e][1], z + c_edges[e][2],
+                                  c_edges[e][3]);
+      if (!q) continue;
+      ++np;
+      const double p[3] = {q[0], q[1], q[2]}, nn[3] = {q[3], q[4], q[5]};
+      const double d = nn[0] * p[0] + nn[1] * p[1] + nn[2] * p[2];
+      for (int r = 0; r < 3; ++r) {
+        mp[r] += p[r];
+        atb[r] += nn[r] * d;
+        for (int c = 0; c < 3; ++c) ata[r][c] += nn[r] * nn[c];
+      }
+    }
+    for (int r = 0; r < 3; ++r) mp[r] /= double(np);
+    double rhs[3];
+    for (int r = 0; r < 3; ++r) rhs[r] = atb[r] - (ata[r][0] * mp[0] + ata[r][1] * mp[1] + ata[r][2] * mp[2]);
+    double a[3][3], Vm[3][3], w[3];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) a[r][c] = ata[r][c];
+    sym3_jacobi(a, Vm, w);
+    const double wmax = fmax(fabs(w[0]), fmax(fabs(w[1]), fabs(w[2])));
+    double xs[3] = {mp[0], mp[1], mp[2]};
+    for (int k = 0; k < 3; ++k) {
+      if (!(fabs(w[k]) > QEF_TRUNC * wmax)) continue;
+      const double proj = (Vm[0][k] * rhs[0] + Vm[1][k] * rhs[1] + Vm[2][k] * rhs[2]) / w[k];
+      for (int r = 0; r < 3; ++r) xs[r] += proj * Vm[r][k];
+    }
+    float* out = cells + (celloff[l] + rank512(m, o)) * 3;
+    out[0] = float(xs[0]);
+    out[1] = float(xs[1]);
+    out[2] = float(xs[2]);
+  }
+}
+
 __device__ __forceinline__ const float* cell_point(const int* nb, const uint32_t* cellm, const uint32_t* celloff,
                                                    const float* cells, int x, int y, int z) {
   const int k = ((x >> 3) + 1) * 9 + ((y >> 3) + 1) * 3 + ((z >> 3) + 1);
@@ -378,8 +471,8 @@ __global__ void __launch_bounds__(128) k_dc_quads(DcVol V, uint64_t n, const uin
 
 static bool has_active_tiles(const bs_volume* v) { return v->n_tiles != 0; }
 
-void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size) {
-  if (v->dc_valid && v->dc_h == voxel_size) return;
+void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size, int mode) {
+  if (v->dc_valid && v->dc_h == voxel_size && v->dc_mode == mode) return;
   if (has_active_tiles(v)) fail(BS_ERR_UNSUPPORTED, "dual contouring of a volume with active tiles (the reference stops with todo!())");
   cudaStream_t s = ctx->stream;
   dfree(ctx, v->d_dc_tris);
@@ -389,6 +482,7 @@ void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size) {
   if (n == 0) {
     v->dc_valid = true;
     v->dc_h = voxel_size;
+    v->dc_mode = mode;
     return;
   }
   LeafHashBuf hb;
@@ -411,7 +505,10 @@ void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size) {
   uint32_t nc = 0;
   read_back(ctx, &nc, celloff.p + n, sizeof(uint32_t));
   DBuf<float> cells(ctx, uint64_t(nc) * 3);
-  BS_KERNEL(ctx, "k_dc_cell_points", (k_dc_cell_points<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, coff.p, pts.p, cellm.p, celloff.p, cells.p)));
+  if (mode == 1)
+    BS_KERNEL(ctx, "k_dc_cell_qef", (k_dc_cell_qef<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, coff.p, pts.p, cellm.p, celloff.p, cells.p)));
+  else
+    BS_KERNEL(ctx, "k_dc_cell_points", (k_dc_cell_points<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, coff.p, pts.p, cellm.p, celloff.p, cells.p)));
   // 3. quads
   DBuf<uint32_t> vcnt(ctx, n * 512 + 1), voff(ctx, n * 512 + 1);
   BS_KERNEL(ctx, "k_dc_quads", (k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, cellm.p, celloff.p, cells.p, voxel_size, vcnt.p, nullptr, nullptr)));
@@ -428,6 +525,7 @@ void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size) {
   v->n_dc_tris = nt;
   v->dc_valid = true;
   v->dc_h = voxel_size;
+  v->dc_mode = mode;
   ctx->last_stats[6] = ne;
   ctx->last_stats[7] = nc;
 }

@@ -178,6 +178,16 @@ bs_status bs_volume_cuboid(bs_ctx* ctx, float voxel_size, const float* min3, con
 bs_status bs_volume_iwp(bs_ctx* ctx, float voxel_size, const float* min3, const float* max3, float cell_size,
                         bs_volume** out);
 
+/* Dual contouring with the vertex of every cell placed by a quadratic error
+ * function instead of the reference's particle solver: the point minimising
+ * sum_i (n_i . (x - p_i))^2 over the cell's edge crossings p_i and normals n_i,
+ * solved in double by a 3x3 symmetric eigen-decomposition and pseudo-inverse
+ * (eigenvalues below 0.1 of the largest dropped) around the crossings' mass
+ * point.  Crossings, normals, cells and quads are those of bs_dual_contour, so
+ * the triangles connect the same cells.  No reference counterpart. */
+bs_status bs_dual_contour_qef(bs_ctx* ctx, bs_volume* v, float voxel_size, float* h_tris, uint64_t capacity,
+                              uint64_t* n_tris);
+
 /* --------------------------------------------------- marching cubes ---- */
 /* MarchingCubesMesher::with_voxel_size(..).mesh(&volume) (marching_cubes.rs:30-63,
  * 969-1011), active tiles included (the cubes on their boundary faces).  Same

@@ -64,6 +64,7 @@ def lib():
                 "orc_dual_contour": (i64, [vp, f32, vp, i64, vp, vp, vp]),
                 "orc_mc_count": (i64, [vp, vp, vp]),
                 "orc_marching_cubes": (i64, [vp, f32, vp, i64]),
+                "orc_subtriangles": (i64, [f32p, i64, u32p, i64, f32, i64, vp, vp, i64]),
                 "orc_corner_table_from_soup": (C.c_int, [f32p, i64, vp, vp]),
                 "orc_corner_table_from_indexed": (C.c_int, [f32p, i64, i64p, i64, vp, vp, vp, vp, vp, vp, vp, vp]),
                 "orc_fast_wn": (None, [f32p, i64, u32p, i64, f32p, i64, f32, f32p, vp]),
@@ -222,6 +223,17 @@ def volume_from_samples(h, band, idx_min, values):
     lo = np.ascontiguousarray(idx_min, np.int64)
     dims = np.array(v.shape, np.int64)
     return OracleVolume(lib().orc_volume_from_samples(float(h), int(band), lo, dims, v), float(h))
+
+
+def subtriangles(verts, tris, voxel_size, band):
+    """The reference's sub-triangles (n, 3, 3) float32 and widened boxes (n, 6) int64."""
+    v = np.ascontiguousarray(verts, np.float32)
+    t = np.ascontiguousarray(tris, np.uint32)
+    n = lib().orc_subtriangles(v, len(v), t, len(t), float(voxel_size), int(band), None, None, 0)
+    out = np.zeros((max(n, 1), 9), np.float32)
+    box = np.zeros((max(n, 1), 6), np.int64)
+    lib().orc_subtriangles(v, len(v), t, len(t), float(voxel_size), int(band), _ptr(out), _ptr(box), n)
+    return out[:n].reshape(n, 3, 3), box[:n]
 
 
 def fast_wn(verts, tris, points, beta=2.0):

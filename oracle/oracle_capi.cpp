@@ -230,6 +230,32 @@ int64_t orc_mc_count(void* v, int64_t* ambiguous_faces, int64_t* cubes) {
   return int64_t(mc.triangles);
 }
 
+// Sub-triangles of MeshToVolume (mesh_to_volume.rs:75-116) with their widened
+// integer boxes (124-143): returns the count, fills up to `capacity` records
+// of 9 floats and 6 int64 (box min, box max).
+int64_t orc_subtriangles(const float* xyz, int64_t nv, const uint32_t* tri, int64_t nt, float voxel_size,
+                         int64_t band, float* out_tris, int64_t* out_boxes, int64_t capacity) {
+  auto tris = tris_from_indexed(xyz, nv, tri, nt);
+  std::vector<Tri> sub;
+  for (const Tri& t : tris) subdivide_triangle(t, voxel_size, sub);
+  const float inv_h = 1.0f / voxel_size;
+  const int64_t n = int64_t(sub.size());
+  for (int64_t i = 0; i < std::min(n, capacity); ++i) {
+    const Tri& t = sub[size_t(i)];
+    const V3 p[3] = {t.a, t.b, t.c};
+    for (int k = 0; k < 3; ++k) {
+      out_tris[9 * i + 3 * k] = p[k].x;
+      out_tris[9 * i + 3 * k + 1] = p[k].y;
+      out_tris[9 * i + 3 * k + 2] = p[k].z;
+    }
+    I3 mn, mx;
+    widened_box(t, inv_h, band, mn, mx);
+    const int64_t b[6] = {mn.x, mn.y, mn.z, mx.x, mx.y, mx.z};
+    for (int k = 0; k < 6; ++k) out_boxes[6 * i + k] = b[k];
+  }
+  return n;
+}
+
 // Marching-cubes triangles of a volume without tiles (oracle_mc.hpp); returns
 // the triangle count, copies up to `capacity` triangles.
 int64_t orc_marching_cubes(void* v, float voxel_size, float* out, int64_t capacity) {

@@ -116,3 +116,26 @@ def test_voxel_remesher_feature_preserving():
         .with_meshing_method(bs.VoxelRemesher.FEATURE_PRESERVING)
     ct = r.remesh((v, f))
     assert ct.faces_count() > 10000 and ct.vertices_count() > 5000
+
+
+def test_qef_vertices_sphere_and_cuboid():
+    """bs_dual_contour_qef: the same cells and quads as the particle solver
+    (same triangle count), vertices on a sphere's surface, and on a cuboid's
+    flat faces (rank-1 systems) every vertex exactly on its face plane."""
+    h = 0.02
+    sph = bs.VolumeBuilder(context()).with_voxel_size(h).sphere(0.5, (0.013, -0.007, 0.004))
+    part = bs.DualContouringMesher().with_voxel_size(h).mesh(sph)
+    qef = bs.DualContouringMesher().with_voxel_size(h).with_qef_vertices().mesh(sph)
+    assert abs(len(qef) - len(part)) <= len(part) // 1000
+    r = np.linalg.norm(qef.reshape(-1, 3) - np.array([0.013, -0.007, 0.004], np.float32), axis=1)
+    assert np.abs(r - 0.5).max() < 0.25 * h and np.abs(r - 0.5).mean() < 0.05 * h
+    mn, mx = np.array([-0.301, -0.203, -0.105]), np.array([0.307, 0.252, 0.196])
+    cub = bs.VolumeBuilder(context()).with_voxel_size(h).cuboid(mn, mx)
+    q = np.unique(bs.DualContouringMesher().with_voxel_size(h).with_qef_vertices().mesh(cub).reshape(-1, 3), axis=0)
+    # distance of each vertex to the six face planes; vertices 3 voxels away
+    # from every edge of the box sit on exactly one face
+    dp = np.abs(np.concatenate([q - mn, q - mx], axis=1)).astype(np.float64)
+    near = np.sort(dp, axis=1)
+    interior = near[:, 1] > 3 * h
+    assert interior.sum() > 500
+    assert near[interior, 0].max() < 1e-3 * h

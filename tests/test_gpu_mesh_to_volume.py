@@ -196,3 +196,47 @@ def test_fast_sign_agrees_with_exact_on_watertight():
     wn = bs.winding_numbers_exact(v, f, pts, ctx=context()).cpu().numpy()
     inside_gpu = np.signbit(val[idx])
     assert np.array_equal(inside_gpu, wn >= 0.2)
+
+
+def test_distance_error_vs_float64():
+    """The float32 distances (bit-identical to the reference's) against a
+    float64 evaluation of the same candidate minimum, in voxel units: the
+    error stays at the float32 rounding of the inputs (about 1e-5 voxel here)."""
+    from tests.f64_distance import min_distance_f64
+    v, f = synthetic.config1()
+    h = 0.02
+    vol = bs.MeshToVolume(context()).with_voxel_size(h).with_narrow_band_width(3).convert((v, f))
+    o, val, m = vol.export()
+    act = np.unpackbits(m.view(np.uint8), bitorder="little").reshape(len(o), 512).astype(bool)
+    li, vi = np.nonzero(act)
+    pick = np.random.default_rng(3).choice(len(li), 1500, replace=False)
+    li, vi = li[pick], vi[pick]
+    vox = o[li].astype(np.int64) + np.stack([vi >> 6, (vi >> 3) & 7, vi & 7], 1)
+    sub, box = ob.subtriangles(v, f, h, 3)
+    d64 = min_distance_f64(vox, h, sub, box)
+    err = np.abs(np.abs(val[li, vi]).astype(np.float64) - d64) / h
+    assert np.all(np.isfinite(d64))
+    assert err.max() < 1e-5
+
+
+def test_distance_error_vs_float64_fine_voxel():
+    """The same on a patch of the boolean workload's torus at its voxel size
+    0.002: the float32 inputs themselves (ulp 1.2e-7 at coordinates ~1.3 =
+    6e-5 voxel) bound the error; it stays within 2e-4 voxel."""
+    from tests.f64_distance import min_distance_f64
+    (v, f), _ = synthetic.config2(nu=1024, nv=512)
+    c = (v[f[:, 0]] + v[f[:, 1]] + v[f[:, 2]]) / 3
+    keep = np.linalg.norm(c - v[0], axis=1) < 0.02
+    v2, f2 = v, f[keep]
+    h = 0.002
+    vol = bs.MeshToVolume(context()).with_voxel_size(h).with_narrow_band_width(3).convert((v2, f2))
+    o, val, m = vol.export()
+    act = np.unpackbits(m.view(np.uint8), bitorder="little").reshape(len(o), 512).astype(bool)
+    li, vi = np.nonzero(act)
+    pick = np.random.default_rng(4).choice(len(li), 800, replace=False)
+    li, vi = li[pick], vi[pick]
+    vox = o[li].astype(np.int64) + np.stack([vi >> 6, (vi >> 3) & 7, vi & 7], 1)
+    sub, box = ob.subtriangles(v2, f2, h, 3)
+    d64 = min_distance_f64(vox, h, sub, box)
+    err = np.abs(np.abs(val[li, vi]).astype(np.float64) - d64) / h
+    assert err.max() < 2e-4
