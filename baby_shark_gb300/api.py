@@ -274,6 +274,11 @@ class MeshToVolume:
     def set_narrow_band_width(self, width):
         return self.with_narrow_band_width(width)
 
+    def with_winding_number_order(self, order):
+        """Far-field order of the sign pass: 2 as the reference, or 3 (extension)."""
+        self.params.wn_order = int(order)
+        return self
+
     def convert(self, mesh):
         """Returns a Volume, or None for an empty mesh (as the reference)."""
         v, f = _mesh_arrays(mesh)
@@ -311,6 +316,48 @@ def convert_batch(meshes, params, ctx=None):
     N.check(N.load().bs_mesh_to_volume_batch(ctx.h, K, xyz.ctypes.data, nv.ctypes.data, tri.ctypes.data,
                                              nt.ctypes.data, P, out), ctx.h)
     return [Volume(C.c_void_p(out[k]), ctx) if out[k] else None for k in range(K)]
+
+
+class WindingNumbers:
+    """WindingNumbers (spatial_partitioning/aabb_tree.rs:622-691) on the GPU:
+    from_mesh builds the tree and far-field records, approximate evaluates the
+    fast winding number at points.  order=3 adds the third-order far-field
+    term (an extension; the reference stops at order 2)."""
+
+    def __init__(self, handle, ctx):
+        self.h = handle
+        self.ctx = ctx
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            try:
+                N.load().bs_winding_numbers_free(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+    @staticmethod
+    def from_mesh(mesh, order=2, ctx=None):
+        import torch
+        ctx = ctx or default_context()
+        v, f = _mesh_arrays(mesh)
+        dv = torch.from_numpy(v).cuda()
+        df = torch.from_numpy(f.astype(np.int32)).cuda()
+        torch.cuda.synchronize()
+        out = C.c_void_p()
+        N.check(N.load().bs_winding_numbers_build(ctx.h, dv.data_ptr(), len(v), df.data_ptr(), len(f), int(order),
+                                                  C.byref(out)), ctx.h)
+        return WindingNumbers(out, ctx)
+
+    def approximate(self, points, accuracy_scale=2.0):
+        """Winding numbers (float32) of an (n, 3) array of points."""
+        import torch
+        p = torch.from_numpy(np.ascontiguousarray(points, np.float32).reshape(-1, 3)).cuda()
+        out = torch.empty(p.shape[0], dtype=torch.float32, device=p.device)
+        torch.cuda.synchronize()
+        N.check(N.load().bs_winding_numbers_approximate(self.ctx.h, self.h, p.data_ptr(), p.shape[0],
+                                                        float(accuracy_scale), out.data_ptr()), self.ctx.h)
+        return out.cpu().numpy()
 
 
 def winding_numbers_exact(vertices, triangles, points, ctx=None):

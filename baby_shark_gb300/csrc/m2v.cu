@@ -69,7 +69,7 @@ struct M2VStats {
 // to the mesh's vertices [vtx_base, vtx_base + n_vtx).
 struct MeshInfo {
   float h, inv_h, beta, thresh;
-  int band, pad;
+  int band, order;  // order: far-field expansion order, 2 or 3
   uint32_t tri_base, n_tri;
   uint64_t vtx_base, n_vtx;
 };
@@ -566,8 +566,31 @@ __global__ void k_mesh_keys(const uint32_t* __restrict__ order, uint64_t nt, con
   const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (i < nt) mk[i] = uint32_t(find_seg(tri_base, K, order[i]));
 }
+// Order-3 far-field record of a node (6 float4): C_i,jk = sum over its
+// triangles of n_i * integral (x - p)_j (x - p)_k dA about the dipole centre
+// p (18 floats: for i = x, y, z the symmetric jk block xx xy xz yy yz zz),
+// then u_k = sum_i C_i,ik and v_i = sum_j C_i,jj.
+__device__ __forceinline__ void store_c3(float4* o, const float C[3][6]) {
+  const float u0 = C[0][0] + C[1][1] + C[2][2];  // C_x,xx + C_y,yx + C_z,zx
+  const float u1 = C[0][1] + C[1][3] + C[2][4];  // C_x,xy + C_y,yy + C_z,zy
+  const float u2 = C[0][2] + C[1][4] + C[2][5];  // C_x,xz + C_y,yz + C_z,zz
+  const float v0 = C[0][0] + C[0][3] + C[0][5], v1 = C[1][0] + C[1][3] + C[1][5], v2 = C[2][0] + C[2][3] + C[2][5];
+  o[0] = make_float4(C[0][0], C[0][1], C[0][2], C[0][3]);
+  o[1] = make_float4(C[0][4], C[0][5], C[1][0], C[1][1]);
+  o[2] = make_float4(C[1][2], C[1][3], C[1][4], C[1][5]);
+  o[3] = make_float4(C[2][0], C[2][1], C[2][2], C[2][3]);
+  o[4] = make_float4(C[2][4], C[2][5], u0, u1);
+  o[5] = make_float4(u2, v0, v1, v2);
+}
+__device__ __forceinline__ void load_c3(const float4* o, float C[3][6]) {
+  const float4 a = o[0], b = o[1], c = o[2], d = o[3], e = o[4];
+  C[0][0] = a.x; C[0][1] = a.y; C[0][2] = a.z; C[0][3] = a.w; C[0][4] = b.x; C[0][5] = b.y;
+  C[1][0] = b.z; C[1][1] = b.w; C[1][2] = c.x; C[1][3] = c.y; C[1][4] = c.z; C[1][5] = c.w;
+  C[2][0] = d.x; C[2][1] = d.y; C[2][2] = d.z; C[2][3] = d.w; C[2][4] = e.x; C[2][5] = e.y;
+}
+
 __global__ void k_leaves(const float4* __restrict__ T, const uint32_t* __restrict__ order, uint64_t nt,
-                         float4* __restrict__ leaf, Sums* __restrict__ lsum) {
+                         float4* __restrict__ leaf, Sums* __restrict__ lsum, float4* __restrict__ leaf3) {
   uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (i >= nt) return;
   uint32_t t = order[i];
@@ -602,6 +625,21 @@ __global__ void k_leaves(const float4* __restrict__ T, const uint32_t* __restric
   leaf[5 * i + 2] = A;
   leaf[5 * i + 3] = B;
   leaf[5 * i + 4] = C;
+  if (leaf3) {
+    // a triangle's second moment about its centroid: (area / 12) sum_v (v - c)(v - c)^T,
+    // so C_i,jk = (area n)_i / 12 * sum_v (v - c)_j (v - c)_k
+    const float e[3][3] = {{A.x - cx, A.y - cy, A.z - cz}, {B.x - cx, B.y - cy, B.z - cz}, {C.x - cx, C.y - cy, C.z - cz}};
+    const int J[6] = {0, 0, 0, 1, 1, 2}, Kk[6] = {0, 1, 2, 1, 2, 2};
+    float S[6];
+    for (int q = 0; q < 6; ++q) S[q] = (e[0][J[q]] * e[0][Kk[q]] + e[1][J[q]] * e[1][Kk[q]] + e[2][J[q]] * e[2][Kk[q]]) * (1.0f / 12.0f);
+    float Cc[3][6];
+    for (int q = 0; q < 6; ++q) {
+      Cc[0][q] = s.ax * S[q];
+      Cc[1][q] = s.ay * S[q];
+      Cc[2][q] = s.az * S[q];
+    }
+    store_c3(leaf3 + 6 * i, Cc);
+  }
 }
 
 // ---- PLOC: Meister & Bittner, "Parallel Locally-Ordered Clustering for
@@ -877,10 +915,24 @@ __device__ __forceinline__ Sums load_sums_cg(const Sums* p) {
 // Bottom-up: the second thread to reach a node combines both children.
 __device__ __forceinline__ float4 ld_cg4(const float4* p) { return __ldcg(p); }
 
+// Adds a child's order-3 coefficients, moved from its dipole centre to the
+// parent's (d = child centre - parent centre):
+// C_i,jk += B_child[j][i] d_k + d_j B_child[k][i] + a_i d_j d_k.
+__device__ __forceinline__ void add_shifted_c3(float C[3][6], const float Cc[3][6], const float Bc[3][3],
+                                               const float a[3], const float d[3]) {
+  const int J[6] = {0, 0, 0, 1, 1, 2}, Kk[6] = {0, 1, 2, 1, 2, 2};
+  for (int i = 0; i < 3; ++i)
+    for (int q = 0; q < 6; ++q) {
+      const int j = J[q], k = Kk[q];
+      C[i][q] += Cc[i][q] + Bc[j][i] * d[k] + d[j] * Bc[k][i] + a[i] * d[j] * d[k];
+    }
+}
+
 __global__ void k_refit(uint64_t nt, const uint32_t* __restrict__ tri_base, const uint32_t* __restrict__ inode_base,
                         int K, const int2* __restrict__ child, const int* __restrict__ parent_i,
                         const int* __restrict__ parent_l, const Sums* __restrict__ lsum, Sums* __restrict__ isum,
-                        int* __restrict__ flags, float4* __restrict__ inode, const float4* __restrict__ leaf_rec) {
+                        int* __restrict__ flags, float4* __restrict__ inode, const float4* __restrict__ leaf_rec,
+                        float4* __restrict__ inode3, const float4* __restrict__ leaf3) {
   const uint64_t gl = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (gl >= nt) return;
   const int mesh = find_seg(tri_base, K, gl);
@@ -917,6 +969,37 @@ __global__ void k_refit(uint64_t nt, const uint32_t* __restrict__ tri_base, cons
     inode[5 * gn + 2] = make_float4(B[0], B[1], B[2], B[3]);
     inode[5 * gn + 3] = make_float4(B[4], B[5], B[6], B[7]);
     inode[5 * gn + 4] = make_float4(B[8], __int_as_float(c.x), __int_as_float(c.y), 0.f);
+    if (inode3) {
+      float C[3][6] = {{0.f}};
+      const int kids[2] = {c.x, c.y};
+      for (int h = 0; h < 2; ++h) {
+        const int k = kids[h];
+        float Cc[3][6], Bc[3][3], a[3], d[3];
+        float4 P, A1;
+        if (k >= 0) {
+          const float4* rec = inode + 5 * (ib + uint64_t(k));
+          P = ld_cg4(rec);
+          A1 = ld_cg4(rec + 1);
+          const float4 b0 = ld_cg4(rec + 2), b1 = ld_cg4(rec + 3), b2 = ld_cg4(rec + 4);
+          Bc[0][0] = b0.x; Bc[0][1] = b0.y; Bc[0][2] = b0.z; Bc[1][0] = b0.w; Bc[1][1] = b1.x; Bc[1][2] = b1.y;
+          Bc[2][0] = b1.z; Bc[2][1] = b1.w; Bc[2][2] = b2.x;
+          float4 t[5];
+          for (int q = 0; q < 5; ++q) t[q] = ld_cg4(inode3 + 6 * (ib + uint64_t(k)) + q);
+          load_c3(t, Cc);
+        } else {
+          const float4* rec = leaf_rec + 5 * (lb + uint64_t(~k));
+          P = rec[0];
+          A1 = rec[1];
+          for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) Bc[r][q] = 0.f;
+          load_c3(leaf3 + 6 * (lb + uint64_t(~k)), Cc);
+        }
+        a[0] = A1.x; a[1] = A1.y; a[2] = A1.z;
+        d[0] = P.x - px; d[1] = P.y - py; d[2] = P.z - pz;
+        add_shifted_c3(C, Cc, Bc, a, d);
+      }
+      store_c3(inode3 + 6 * gn, C);
+    }
     node = parent_i[gn];
   }
 }
@@ -984,18 +1067,34 @@ __device__ __forceinline__ void kahan(float& sum, float& comp, float w) {
 
 // Warps are numbered per mesh (warp_base[m] .. warp_base[m+1]) so that a warp
 // never holds voxels of two meshes.
-// Traversal of one warp's 32 voxels (act[i] for the lanes with valid) in one
-// mesh's tree, then the sign of each voxel's distance.
-__device__ __forceinline__ void wn_warp(const uint32_t* __restrict__ act, uint64_t i, bool valid, uint64_t last,
-                                        const int4* __restrict__ origins, float* __restrict__ values,
-                                        const float4* __restrict__ inode, const float4* __restrict__ leaf, int n,
-                                        float h, float beta, float thresh, M2VStats* st, int (*stk)[WN_STACK]) {
+// Order-3 far-field term (1 / 8 pi) [-3 |r|^-5 (2 u.r + v.r) + 15 |r|^-7
+// sum_i r_i r^T C_i r] with inv = 1 / (4 pi |r|^3) and ri2 = 1 / |r|^2.
+__device__ __forceinline__ float far3(const float4* __restrict__ c3, float rx, float ry, float rz, float inv,
+                                      float ri2) {
+  const float4 a = __ldg(c3), b = __ldg(c3 + 1), c = __ldg(c3 + 2), d = __ldg(c3 + 3), e = __ldg(c3 + 4),
+               f = __ldg(c3 + 5);
+  const float xx = rx * rx, yy = ry * ry, zz = rz * rz, xy = 2.f * rx * ry, xz = 2.f * rx * rz, yz = 2.f * ry * rz;
+  const float q0 = a.x * xx + a.y * xy + a.z * xz + a.w * yy + b.x * yz + b.y * zz;
+  const float q1 = b.z * xx + b.w * xy + c.x * xz + c.y * yy + c.z * yz + c.w * zz;
+  const float q2 = d.x * xx + d.y * xy + d.z * xz + d.w * yy + e.x * yz + e.y * zz;
+  const float cubic = rx * q0 + ry * q1 + rz * q2;
+  const float ur = e.z * rx + e.w * ry + f.x * rz, vr = f.y * rx + f.z * ry + f.w * rz;
+  return 0.5f * inv * ri2 * (-3.0f * (2.0f * ur + vr) + 15.0f * ri2 * cubic);
+}
+
+// Traversal of one warp's 32 query points in one mesh's tree; returns each
+// lane's winding number.  The 32 lanes hold nearby points (Morton order inside
+// a brick for band voxels) and walk the tree together: a node is summed
+// through its far field only when it is far (|q - p| > beta r,
+// aabb_tree.rs:666) for every lane; otherwise the warp opens it, and at a leaf
+// every lane takes the exact solid angle.  Node loads are warp-uniform, control
+// flow never diverges, and each lane's sum is at least as accurate as its own
+// traversal would be.  ORDER 3 adds the third-order far-field term.
+template <int ORDER>
+__device__ __forceinline__ float wn_traverse(F3 q, const float4* __restrict__ inode, const float4* __restrict__ leaf,
+                                             const float4* __restrict__ inode3, const float4* __restrict__ leaf3, int n,
+                                             float beta, M2VStats* st, int (*stk)[WN_STACK]) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const uint32_t v = valid ? act[i] : act[last];
-  const uint32_t b = v >> 9, o = v & 511;
-  const int4 org = origins[b];
-  const F3 q = f3(fmul(__int2float_rn(org.x + int(o >> 6)), h), fmul(__int2float_rn(org.y + int((o >> 3) & 7)), h),
-                  fmul(__int2float_rn(org.z + int(o & 7)), h));
   const float beta2 = beta * beta;
   float sum = 0.f, comp = 0.f;  // Kahan-compensated accumulation
   int sp = 0;
@@ -1024,6 +1123,7 @@ __device__ __forceinline__ void wn_warp(const uint32_t* __restrict__ act, uint64
         const float brz = B1.z * rx + B1.w * ry + B2.x * rz;
         const float rbr = rx * brx + ry * bry + rz * brz;
         wv = inv * ((ar + A.w) - 3.0f * ri2 * rbr);
+        if (ORDER >= 3) wv += far3(inode3 + 6 * node, rx, ry, rz, inv, ri2);
       } else {
         const float4 E = inode[5 * node + 4];
         if (sp < WN_STACK) {
@@ -1044,7 +1144,9 @@ __device__ __forceinline__ void wn_warp(const uint32_t* __restrict__ act, uint64
         ++c_far;
         const float4 A = leaf[5 * li + 1];
         const float ri = rsqrtf(r2);
-        wv = (A.x * rx + A.y * ry + A.z * rz) * (ri * ri * ri * (1.0f / FOUR_PI));
+        const float inv = ri * ri * ri * (1.0f / FOUR_PI);
+        wv = (A.x * rx + A.y * ry + A.z * rz) * inv;
+        if (ORDER >= 3) wv += far3(leaf3 + 6 * li, rx, ry, rz, inv, ri * ri);
       } else {
         ++c_exact;
         wv = tri_wn(leaf[5 * li + 2], leaf[5 * li + 3], leaf[5 * li + 4], q);
@@ -1065,26 +1167,47 @@ __device__ __forceinline__ void wn_warp(const uint32_t* __restrict__ act, uint64
     atomicAdd(&st->wn_far, (unsigned long long)c_far);
     atomicAdd(&st->wn_exact, (unsigned long long)c_exact);
   }
+  return sum;
+}
+
+// Band voxel act[i] of the warp: its grid point and, after the traversal, the
+// sign of its distance (mesh_to_volume.rs:264-271).
+template <int ORDER>
+__device__ __forceinline__ void wn_warp(const uint32_t* __restrict__ act, uint64_t i, bool valid, uint64_t last,
+                                        const int4* __restrict__ origins, float* __restrict__ values,
+                                        const float4* __restrict__ inode, const float4* __restrict__ leaf,
+                                        const float4* __restrict__ inode3, const float4* __restrict__ leaf3, int n,
+                                        float h, float beta, float thresh, M2VStats* st, int (*stk)[WN_STACK]) {
+  const uint32_t v = valid ? act[i] : act[last];
+  const uint32_t b = v >> 9, o = v & 511;
+  const int4 org = origins[b];
+  const F3 q = f3(fmul(__int2float_rn(org.x + int(o >> 6)), h), fmul(__int2float_rn(org.y + int((o >> 3) & 7)), h),
+                  fmul(__int2float_rn(org.z + int(o & 7)), h));
+  const float sum = wn_traverse<ORDER>(q, inode, leaf, inode3, leaf3, n, beta, st, stk);
   if (valid) {
     const float d = values[uint64_t(b) * 512 + o];
     values[uint64_t(b) * 512 + o] = (sum < thresh) ? copysignf(d, 1.0f) : copysignf(d, -1.0f);
   }
 }
 
+template <int ORDER>
 __global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restrict__ act, uint64_t na,
                                                         const int4* __restrict__ origins, float* __restrict__ values,
                                                         const float4* __restrict__ inode,
-                                                        const float4* __restrict__ leaf, int n, float h, float beta,
+                                                        const float4* __restrict__ leaf,
+                                                        const float4* __restrict__ inode3,
+                                                        const float4* __restrict__ leaf3, int n, float h, float beta,
                                                         float thresh, M2VStats* st) {
   __shared__ int stk[WN_WARPS][WN_STACK];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint64_t i = (blockIdx.x * uint64_t(WN_WARPS) + w) * 32 + lane;
   if ((blockIdx.x * uint64_t(WN_WARPS) + w) * 32 >= na) return;  // whole warp out of range
-  wn_warp(act, i, i < na, na - 1, origins, values, inode, leaf, n, h, beta, thresh, st, stk);
+  wn_warp<ORDER>(act, i, i < na, na - 1, origins, values, inode, leaf, inode3, leaf3, n, h, beta, thresh, st, stk);
 }
 
 // Batches: warps are numbered per mesh (warp_base[m] .. warp_base[m+1]) so
 // that a warp never holds voxels of two meshes.
+template <int ORDER>
 __global__ void __launch_bounds__(WN_THREADS) k_wn_sign_batch(const uint32_t* __restrict__ act,
                                                               const uint32_t* __restrict__ act_base,
                                                               const uint32_t* __restrict__ warp_base, int K,
@@ -1094,7 +1217,9 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign_batch(const uint32_t* __
                                                               const int4* __restrict__ origins,
                                                               float* __restrict__ values,
                                                               const float4* __restrict__ inodes,
-                                                              const float4* __restrict__ leaves, M2VStats* stats) {
+                                                              const float4* __restrict__ leaves,
+                                                              const float4* __restrict__ inodes3,
+                                                              const float4* __restrict__ leaves3, M2VStats* stats) {
   __shared__ int stk[WN_WARPS][WN_STACK];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint64_t gw = blockIdx.x * uint64_t(WN_WARPS) + w;
@@ -1103,8 +1228,32 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_sign_batch(const uint32_t* __
   const uint64_t a1 = act_base[mesh + 1];
   const uint64_t i = act_base[mesh] + (gw - warp_base[mesh]) * 32 + lane;
   const MeshInfo M = mi[mesh];
-  wn_warp(act, i, i < a1, a1 - 1, origins, values, inodes + 5 * uint64_t(inode_base[mesh]),
-          leaves + 5 * uint64_t(tri_base[mesh]), int(M.n_tri), M.h, M.beta, M.thresh, stats + mesh, stk);
+  const uint64_t ib = inode_base[mesh], lb = tri_base[mesh];
+  if (ORDER >= 3 && M.order >= 3)
+    wn_warp<3>(act, i, i < a1, a1 - 1, origins, values, inodes + 5 * ib, leaves + 5 * lb, inodes3 + 6 * ib,
+               leaves3 + 6 * lb, int(M.n_tri), M.h, M.beta, M.thresh, stats + mesh, stk);
+  else
+    wn_warp<2>(act, i, i < a1, a1 - 1, origins, values, inodes + 5 * ib, leaves + 5 * lb, nullptr, nullptr,
+               int(M.n_tri), M.h, M.beta, M.thresh, stats + mesh, stk);
+}
+
+// WindingNumbers::approximate (aabb_tree.rs:654-660) at arbitrary points: a
+// warp takes 32 consecutive points of the caller's order.
+template <int ORDER>
+__global__ void __launch_bounds__(WN_THREADS) k_wn_points(const float* __restrict__ pts, uint64_t np,
+                                                          const float4* __restrict__ inode,
+                                                          const float4* __restrict__ leaf,
+                                                          const float4* __restrict__ inode3,
+                                                          const float4* __restrict__ leaf3, int n, float beta,
+                                                          float* __restrict__ out, M2VStats* st) {
+  __shared__ int stk[WN_WARPS][WN_STACK];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint64_t wbase = (blockIdx.x * uint64_t(WN_WARPS) + w) * 32;
+  if (wbase >= np) return;
+  const uint64_t i = wbase + lane, j = i < np ? i : np - 1;
+  const F3 q = f3(pts[3 * j], pts[3 * j + 1], pts[3 * j + 2]);
+  const float sum = wn_traverse<ORDER>(q, inode, leaf, inode3, leaf3, n, beta, st, stk);
+  if (i < np) out[i] = sum;
 }
 
 // ------------------------------------------------ exact winding numbers ---
@@ -1182,6 +1331,100 @@ __global__ void k_split(const uint32_t* __restrict__ leaf_base, int K, const Spl
   reinterpret_cast<float4*>(D.v + d * 512)[threadIdx.x] = reinterpret_cast<const float4*>(vi + b * 512)[threadIdx.x];
   if (threadIdx.x < 16) D.m[d * 16 + threadIdx.x] = mi_[b * 16 + threadIdx.x];
   if (threadIdx.x == 0) D.o[d] = oi[b];
+}
+
+// One BVH per mesh over the triangles T (3 float4 per triangle, meshes in
+// [tri_base[m], tri_base[m+1])), from Morton order and PLOC, with the
+// far-field records of every node (and the order-3 ones when order3).
+// st[m] holds each mesh's centroid bounds.
+static void build_trees(bs_ctx* ctx, const float4* T, uint64_t nt, int K, const uint32_t* d_tb, const uint32_t* d_ib,
+                        const M2VStats* st, bool order3, DBuf<float4>& leaf, DBuf<float4>& inode,
+                        DBuf<float4>& leaf3, DBuf<float4>& inode3) {
+  cudaStream_t s = ctx->stream;
+  DBuf<uint64_t> keys(ctx, nt), keys2(ctx, nt);
+  DBuf<uint32_t> vals(ctx, nt), order(ctx, nt);
+  BS_KERNEL(ctx, "k_morton", (k_morton<<<blocks(nt, 256), 256, 0, s>>>(T, nt, st, d_tb, K, keys.p, vals.p)));
+  {
+    size_t tmp = 0;
+    BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, keys.p, keys2.p, vals.p, order.p, int(nt), 0, 64, s));
+    DBuf<uint8_t> t(ctx, tmp);
+    BS_CUDA(cub::DeviceRadixSort::SortPairs(t.p, tmp, keys.p, keys2.p, vals.p, order.p, int(nt), 0, 64, s));
+  }
+  if (K > 1) {
+    // stable second pass by mesh: every mesh keeps its full-precision Morton
+    // order, so its tree is the one a call for that mesh alone builds
+    int mesh_bits = 1;
+    while ((1 << mesh_bits) < K) ++mesh_bits;
+    DBuf<uint32_t> mk(ctx, nt), mk2(ctx, nt), order2(ctx, nt);
+    BS_KERNEL(ctx, "k_mesh_keys", (k_mesh_keys<<<blocks(nt, 256), 256, 0, s>>>(order.p, nt, d_tb, K, mk.p)));
+    size_t tmp = 0;
+    BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, mk.p, mk2.p, order.p, order2.p, int(nt), 0, mesh_bits, s));
+    DBuf<uint8_t> t(ctx, tmp);
+    BS_CUDA(cub::DeviceRadixSort::SortPairs(t.p, tmp, mk.p, mk2.p, order.p, order2.p, int(nt), 0, mesh_bits, s));
+    std::swap(order.p, order2.p);
+  }
+  keys.reset();
+  vals.reset();
+  const uint64_t n_int = nt - uint64_t(K);
+  leaf = DBuf<float4>(ctx, 5 * nt);
+  inode = DBuf<float4>(ctx, 5 * std::max<uint64_t>(n_int, 1));
+  if (order3) {
+    leaf3 = DBuf<float4>(ctx, 6 * nt);
+    inode3 = DBuf<float4>(ctx, 6 * std::max<uint64_t>(n_int, 1));
+  }
+  DBuf<Sums> lsum(ctx, nt), isum(ctx, std::max<uint64_t>(n_int, 1));
+  BS_KERNEL(ctx, "k_leaves", (k_leaves<<<blocks(nt, 256), 256, 0, s>>>(T, order.p, nt, leaf.p, lsum.p, leaf3.p)));
+  {
+    DBuf<int2> child(ctx, std::max<uint64_t>(n_int, 1));
+    DBuf<int> parent_i(ctx, std::max<uint64_t>(n_int, 1)), parent_l(ctx, nt), flags(ctx, std::max<uint64_t>(n_int, 1));
+    BS_CUDA(cudaMemsetAsync(parent_l.p, 0xff, nt * sizeof(int), s));  // single-triangle meshes: no parent
+    if (n_int) {
+      BS_CUDA(cudaMemsetAsync(flags.p, 0, n_int * sizeof(int), s));
+      BS_CUDA(cudaMemsetAsync(parent_i.p, 0xff, n_int * sizeof(int), s));  // roots keep -1
+      // topology by PLOC over the Morton-ordered triangles, one tree per mesh
+      DBuf<Cluster> ca(ctx, nt), cb(ctx, nt);
+      DBuf<int> nn(ctx, nt), next_id(ctx, K);
+      DBuf<uint32_t> keep(ctx, nt + 1), pos(ctx, nt + 1);
+      BS_CUDA(cudaMemsetAsync(next_id.p, 0, K * sizeof(int), s));
+      BS_KERNEL(ctx, "k_ploc_init", (k_ploc_init<<<blocks(nt, 256), 256, 0, s>>>(lsum.p, nt, d_tb, K, ca.p)));
+      uint32_t nc = uint32_t(nt);
+      DBuf<uint32_t> mcnt(ctx, K + 1);
+      DBuf<int> ferr(ctx, 1);
+      for (int round = 0; nc > uint32_t(K); ++round) {
+        if (nc <= uint32_t(PLOC_FIN) * uint32_t(K)) {
+          // every mesh small enough: finish each in one block
+          BS_CUDA(cudaMemsetAsync(mcnt.p, 0, (K + 1) * sizeof(uint32_t), s));
+          BS_KERNEL(ctx, "k_ploc_counts", (k_ploc_counts<<<blocks(nc, 256), 256, 0, s>>>(ca.p, nc, mcnt.p, mcnt.p + K, K)));
+          uint32_t mx = 0;
+          read_back(ctx, &mx, mcnt.p + K, sizeof mx);
+          if (mx <= uint32_t(PLOC_FIN)) {
+            const size_t smem = 2 * PLOC_FIN * sizeof(Cluster) + 2 * PLOC_FIN * sizeof(int);
+            BS_CUDA(cudaFuncSetAttribute(k_ploc_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+            BS_CUDA(cudaMemsetAsync(ferr.p, 0, sizeof(int), s));
+            BS_KERNEL(ctx, "k_ploc_finish", (k_ploc_finish<<<unsigned(K), PLOC_FIN_T, smem, s>>>(ca.p, nc, d_tb, d_ib, next_id.p, child.p,
+                                                                                     parent_i.p, parent_l.p, ferr.p)));
+            int fe = 0;
+            read_back(ctx, &fe, ferr.p, sizeof fe);
+            if (fe) fail(BS_ERR_CAPACITY, "tree build did not converge");
+            break;
+          }
+        }
+        if (round >= 4096) fail(BS_ERR_CAPACITY, "tree build did not converge");
+        BS_KERNEL(ctx, "k_ploc_nn", (k_ploc_nn<<<blocks(nc, PLOC_T), PLOC_T, 0, s>>>(ca.p, nc, nn.p)));
+        BS_KERNEL(ctx, "k_ploc_merge", (k_ploc_merge<<<blocks(nc + 1, 256), 256, 0, s>>>(ca.p, nc, nn.p, d_tb, d_ib, next_id.p, child.p,
+                                                                                   parent_i.p, parent_l.p, keep.p)));
+        exclusive_scan(ctx, keep.p, pos.p, uint64_t(nc) + 1);
+        BS_KERNEL(ctx, "k_ploc_compact", (k_ploc_compact<<<blocks(nc, 256), 256, 0, s>>>(ca.p, nc, keep.p, pos.p, cb.p)));
+        std::swap(ca.p, cb.p);
+        uint32_t next = 0;
+        read_back(ctx, &next, pos.p + nc, sizeof next);
+        if (next >= nc) fail(BS_ERR_CAPACITY, "tree build made no progress");
+        nc = next;
+      }
+      BS_KERNEL(ctx, "k_refit", (k_refit<<<blocks(nt, 256), 256, 0, s>>>(nt, d_tb, d_ib, K, child.p, parent_i.p, parent_l.p, lsum.p, isum.p,
+                                                                      flags.p, inode.p, leaf.p, inode3.p, leaf3.p)));
+    }
+  }
 }
 
 // A batch over one of the per-call limits: each mesh's share of the limit.
@@ -1267,6 +1510,7 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
     const bs_m2v_params& p = params[m];
     if (!(p.voxel_size > 0.f) || !std::isfinite(p.voxel_size)) fail(BS_ERR_INVALID_ARG, "voxel_size must be > 0");
     if (p.band_width < 0 || p.band_width > 1000000) fail(BS_ERR_INVALID_ARG, "band_width out of range");
+    if (p.wn_order != 2 && p.wn_order != 3) fail(BS_ERR_INVALID_ARG, "wn_order must be 2 or 3");
     if (n_tri[m]) {
       MeshInfo q{};
       q.h = p.voxel_size;
@@ -1274,6 +1518,7 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
       q.beta = p.wn_beta;
       q.thresh = p.wn_threshold;
       q.band = p.band_width;
+      q.order = p.wn_order;
       q.tri_base = uint32_t(tri_at);
       q.n_tri = uint32_t(n_tri[m]);
       q.vtx_base = vtx_at;
@@ -1418,100 +1663,30 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   vc.reset();
   voff.reset();
 
-  // LBVH per mesh over its original triangles
-  DBuf<uint64_t> keys(ctx, nt), keys2(ctx, nt);
-  DBuf<uint32_t> vals(ctx, nt), order(ctx, nt);
-  BS_KERNEL(ctx, "k_morton", (k_morton<<<blocks(nt, 256), 256, 0, s>>>(T.p, nt, st.p, d_tb.p, K, keys.p, vals.p)));
-  {
-    size_t tmp = 0;
-    BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, keys.p, keys2.p, vals.p, order.p, int(nt), 0, 64, s));
-    DBuf<uint8_t> t(ctx, tmp);
-    BS_CUDA(cub::DeviceRadixSort::SortPairs(t.p, tmp, keys.p, keys2.p, vals.p, order.p, int(nt), 0, 64, s));
-  }
-  if (K > 1) {
-    // stable second pass by mesh: every mesh keeps its full-precision Morton
-    // order, so its tree is the one a call for that mesh alone builds
-    int mesh_bits = 1;
-    while ((1 << mesh_bits) < K) ++mesh_bits;
-    DBuf<uint32_t> mk(ctx, nt), mk2(ctx, nt), order2(ctx, nt);
-    BS_KERNEL(ctx, "k_mesh_keys", (k_mesh_keys<<<blocks(nt, 256), 256, 0, s>>>(order.p, nt, d_tb.p, K, mk.p)));
-    size_t tmp = 0;
-    BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, mk.p, mk2.p, order.p, order2.p, int(nt), 0, mesh_bits, s));
-    DBuf<uint8_t> t(ctx, tmp);
-    BS_CUDA(cub::DeviceRadixSort::SortPairs(t.p, tmp, mk.p, mk2.p, order.p, order2.p, int(nt), 0, mesh_bits, s));
-    std::swap(order.p, order2.p);
-  }
-  keys.reset();
-  vals.reset();
+  // one tree per mesh over its original triangles
+  const bool any3 = std::any_of(mi.begin(), mi.end(), [](const MeshInfo& q) { return q.order >= 3; });
   const uint64_t n_int = nt - uint64_t(K);
-  DBuf<float4> leaf(ctx, 5 * nt), inode(ctx, 5 * std::max<uint64_t>(n_int, 1));
-  DBuf<Sums> lsum(ctx, nt), isum(ctx, std::max<uint64_t>(n_int, 1));
-  BS_KERNEL(ctx, "k_leaves", (k_leaves<<<blocks(nt, 256), 256, 0, s>>>(T.p, order.p, nt, leaf.p, lsum.p)));
-  {
-    DBuf<int2> child(ctx, std::max<uint64_t>(n_int, 1));
-    DBuf<int> parent_i(ctx, std::max<uint64_t>(n_int, 1)), parent_l(ctx, nt), flags(ctx, std::max<uint64_t>(n_int, 1));
-    BS_CUDA(cudaMemsetAsync(parent_l.p, 0xff, nt * sizeof(int), s));  // single-triangle meshes: no parent
-    if (n_int) {
-      BS_CUDA(cudaMemsetAsync(flags.p, 0, n_int * sizeof(int), s));
-      BS_CUDA(cudaMemsetAsync(parent_i.p, 0xff, n_int * sizeof(int), s));  // roots keep -1
-      // topology by PLOC over the Morton-ordered triangles, one tree per mesh
-      DBuf<Cluster> ca(ctx, nt), cb(ctx, nt);
-      DBuf<int> nn(ctx, nt), next_id(ctx, K);
-      DBuf<uint32_t> keep(ctx, nt + 1), pos(ctx, nt + 1);
-      BS_CUDA(cudaMemsetAsync(next_id.p, 0, K * sizeof(int), s));
-      BS_KERNEL(ctx, "k_ploc_init", (k_ploc_init<<<blocks(nt, 256), 256, 0, s>>>(lsum.p, nt, d_tb.p, K, ca.p)));
-      uint32_t nc = uint32_t(nt);
-      DBuf<uint32_t> mcnt(ctx, K + 1);
-      DBuf<int> ferr(ctx, 1);
-      for (int round = 0; nc > uint32_t(K); ++round) {
-        if (nc <= uint32_t(PLOC_FIN) * uint32_t(K)) {
-          // every mesh small enough: finish each in one block
-          BS_CUDA(cudaMemsetAsync(mcnt.p, 0, (K + 1) * sizeof(uint32_t), s));
-          BS_KERNEL(ctx, "k_ploc_counts", (k_ploc_counts<<<blocks(nc, 256), 256, 0, s>>>(ca.p, nc, mcnt.p, mcnt.p + K, K)));
-          uint32_t mx = 0;
-          read_back(ctx, &mx, mcnt.p + K, sizeof mx);
-          if (mx <= uint32_t(PLOC_FIN)) {
-            const size_t smem = 2 * PLOC_FIN * sizeof(Cluster) + 2 * PLOC_FIN * sizeof(int);
-            BS_CUDA(cudaFuncSetAttribute(k_ploc_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-            BS_CUDA(cudaMemsetAsync(ferr.p, 0, sizeof(int), s));
-            BS_KERNEL(ctx, "k_ploc_finish", (k_ploc_finish<<<unsigned(K), PLOC_FIN_T, smem, s>>>(ca.p, nc, d_tb.p, d_ib.p, next_id.p, child.p,
-                                                                                     parent_i.p, parent_l.p, ferr.p)));
-            int fe = 0;
-            read_back(ctx, &fe, ferr.p, sizeof fe);
-            if (fe) fail(BS_ERR_CAPACITY, "tree build did not converge");
-            break;
-          }
-        }
-        if (round >= 4096) fail(BS_ERR_CAPACITY, "tree build did not converge");
-        BS_KERNEL(ctx, "k_ploc_nn", (k_ploc_nn<<<blocks(nc, PLOC_T), PLOC_T, 0, s>>>(ca.p, nc, nn.p)));
-        BS_KERNEL(ctx, "k_ploc_merge", (k_ploc_merge<<<blocks(nc + 1, 256), 256, 0, s>>>(ca.p, nc, nn.p, d_tb.p, d_ib.p, next_id.p, child.p,
-                                                                                   parent_i.p, parent_l.p, keep.p)));
-        exclusive_scan(ctx, keep.p, pos.p, uint64_t(nc) + 1);
-        BS_KERNEL(ctx, "k_ploc_compact", (k_ploc_compact<<<blocks(nc, 256), 256, 0, s>>>(ca.p, nc, keep.p, pos.p, cb.p)));
-        std::swap(ca.p, cb.p);
-        uint32_t next = 0;
-        read_back(ctx, &next, pos.p + nc, sizeof next);
-        if (next >= nc) fail(BS_ERR_CAPACITY, "tree build made no progress");
-        nc = next;
-      }
-      BS_KERNEL(ctx, "k_refit", (k_refit<<<blocks(nt, 256), 256, 0, s>>>(nt, d_tb.p, d_ib.p, K, child.p, parent_i.p, parent_l.p, lsum.p, isum.p,
-                                                                      flags.p, inode.p, leaf.p)));
-    }
-  }
-  keys2.reset();
-  order.reset();
-  lsum.reset();
-  isum.reset();
+  DBuf<float4> leaf, inode, leaf3, inode3;
+  build_trees(ctx, T.p, nt, K, d_tb.p, d_ib.p, st.p, any3, leaf, inode, leaf3, inode3);
   T.reset();
   if (na > 0) {
     const uint64_t n_warps = warp_base[K];
-    if (K == 1)
-      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<<<blocks(na, WN_THREADS), WN_THREADS, 0, s>>>(act.p, na, origins.p, values.p, inode.p, leaf.p,
-                                                                                 int(nt), mi[0].h, mi[0].beta,
-                                                                                 mi[0].thresh, st.p)));
+    if (K == 1 && mi[0].order < 3)
+      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<2><<<blocks(na, WN_THREADS), WN_THREADS, 0, s>>>(act.p, na, origins.p, values.p, inode.p, leaf.p,
+                                                                                    nullptr, nullptr, int(nt), mi[0].h,
+                                                                                    mi[0].beta, mi[0].thresh, st.p)));
+    else if (K == 1)
+      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<3><<<blocks(na, WN_THREADS), WN_THREADS, 0, s>>>(act.p, na, origins.p, values.p, inode.p, leaf.p,
+                                                                                    inode3.p, leaf3.p, int(nt), mi[0].h,
+                                                                                    mi[0].beta, mi[0].thresh, st.p)));
+    else if (!any3)
+      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign_batch<2><<<blocks(n_warps, WN_WARPS), WN_THREADS, 0, s>>>(act.p, act_base.p, d_wb.p, K, d_mi.p, d_tb.p,
+                                                                                       d_ib.p, origins.p, values.p, inode.p, leaf.p,
+                                                                                       nullptr, nullptr, st.p)));
     else
-      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign_batch<<<blocks(n_warps, WN_WARPS), WN_THREADS, 0, s>>>(act.p, act_base.p, d_wb.p, K, d_mi.p, d_tb.p,
-                                                                                    d_ib.p, origins.p, values.p, inode.p, leaf.p, st.p)));
+      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign_batch<3><<<blocks(n_warps, WN_WARPS), WN_THREADS, 0, s>>>(act.p, act_base.p, d_wb.p, K, d_mi.p, d_tb.p,
+                                                                                       d_ib.p, origins.p, values.p, inode.p, leaf.p,
+                                                                                       inode3.p, leaf3.p, st.p)));
   }
   read_back(ctx, hst.data(), st.p, K * sizeof(M2VStats));
   uint64_t n_vp = 0, n_p = 0, visits = 0, far = 0, exact = 0;
@@ -1568,6 +1743,155 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   for (int m = 0; m < K; ++m) result[size_t(which[m])] = vols[m];
   return result;
 }
+
+// ---------------------------------------------------- WindingNumbers ------
+// Triangles of one mesh as float4 triples, and their centroid bounds.
+__global__ void k_tri_gather(const float* __restrict__ xyz, uint64_t nv, const uint32_t* __restrict__ tri, uint64_t nt,
+                             float4* __restrict__ T, M2VStats* st) {
+  const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= nt) return;
+  const uint32_t ia = tri[3 * i], ib = tri[3 * i + 1], ic = tri[3 * i + 2];
+  float4 a = make_float4(0, 0, 0, 0), b = a, c = a;
+  if (ia >= nv || ib >= nv || ic >= nv) {
+    atomicExch(&st->error, 1);
+  } else {
+    a = make_float4(xyz[3 * ia], xyz[3 * ia + 1], xyz[3 * ia + 2], 0.f);
+    b = make_float4(xyz[3 * ib], xyz[3 * ib + 1], xyz[3 * ib + 2], 0.f);
+    c = make_float4(xyz[3 * ic], xyz[3 * ic + 1], xyz[3 * ic + 2], 0.f);
+  }
+  T[3 * i] = a;
+  T[3 * i + 1] = b;
+  T[3 * i + 2] = c;
+  const float cc[3] = {(a.x + b.x + c.x) * (1.0f / 3.0f), (a.y + b.y + c.y) * (1.0f / 3.0f),
+                       (a.z + b.z + c.z) * (1.0f / 3.0f)};
+  const unsigned mask = __activemask();
+  for (int k = 0; k < 3; ++k) {
+    warp_min(&st->cmin[k], f2ord(cc[k]), true, mask);
+    warp_max(&st->cmax[k], f2ord(cc[k]), true, mask);
+  }
+}
+
+}  // namespace bs
+
+// WindingNumbers (spatial_partitioning/aabb_tree.rs:622-691): a mesh's tree
+// with its far-field records, evaluated at arbitrary points.
+struct bs_wn_tree {
+  explicit bs_wn_tree(bs_ctx* c) : ctx(c) { ctx->refs++; }
+  bs_wn_tree(const bs_wn_tree&) = delete;
+  bs_wn_tree& operator=(const bs_wn_tree&) = delete;
+  ~bs_wn_tree() {
+    cudaSetDevice(ctx->device);
+    bs::dfree(ctx, leaf);
+    bs::dfree(ctx, inode);
+    bs::dfree(ctx, leaf3);
+    bs::dfree(ctx, inode3);
+    bs_ctx_release(ctx);
+  }
+  bs_ctx* ctx;
+  uint64_t nt = 0;
+  int order = 2;
+  float4 *leaf = nullptr, *inode = nullptr, *leaf3 = nullptr, *inode3 = nullptr;
+};
+
+namespace bs {
+
+static bs_wn_tree* wn_tree_build(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
+                                 int order) {
+  if (nt == 0) fail(BS_ERR_EMPTY, "mesh has no triangles");
+  if (nt >= (1ull << 31)) fail(BS_ERR_CAPACITY, "more than 2^31 triangles");
+  if (order != 2 && order != 3) fail(BS_ERR_INVALID_ARG, "order must be 2 or 3");
+  cudaStream_t s = ctx->stream;
+  DBuf<float4> T(ctx, 3 * nt);
+  DBuf<M2VStats> st(ctx, 1);
+  M2VStats init{};
+  for (int k = 0; k < 3; ++k) {
+    init.cmin[k] = 0xffffffffu;
+    init.cmax[k] = 0u;
+  }
+  BS_CUDA(cudaMemcpyAsync(st.p, &init, sizeof init, cudaMemcpyHostToDevice, s));
+  BS_KERNEL(ctx, "k_tri_gather", (k_tri_gather<<<blocks(nt, 256), 256, 0, s>>>(d_xyz, nv, d_tri, nt, T.p, st.p)));
+  const uint32_t tb[2] = {0, uint32_t(nt)}, ibase[2] = {0, uint32_t(nt - 1)};
+  DBuf<uint32_t> d_tb(ctx, 2), d_ib(ctx, 2);
+  BS_CUDA(cudaMemcpyAsync(d_tb.p, tb, sizeof tb, cudaMemcpyHostToDevice, s));
+  BS_CUDA(cudaMemcpyAsync(d_ib.p, ibase, sizeof ibase, cudaMemcpyHostToDevice, s));
+  DBuf<float4> leaf, inode, leaf3, inode3;
+  build_trees(ctx, T.p, nt, 1, d_tb.p, d_ib.p, st.p, order >= 3, leaf, inode, leaf3, inode3);
+  M2VStats hs;
+  read_back(ctx, &hs, st.p, sizeof hs);
+  if (hs.error == 1) fail(BS_ERR_INVALID_ARG, "triangle vertex index out of range");
+  bs_wn_tree* t = new bs_wn_tree(ctx);
+  t->nt = nt;
+  t->order = order;
+  t->leaf = leaf.release();
+  t->inode = inode.release();
+  t->leaf3 = leaf3.release();
+  t->inode3 = inode3.release();
+  return t;
+}
+
+static void wn_tree_approximate(bs_ctx* ctx, const bs_wn_tree* t, const float* d_pts, uint64_t np, float beta,
+                                float* d_out) {
+  if (np == 0) return;
+  cudaStream_t s = ctx->stream;
+  DBuf<M2VStats> st(ctx, 1);
+  BS_CUDA(cudaMemsetAsync(st.p, 0, sizeof(M2VStats), s));
+  if (t->order >= 3)
+    BS_KERNEL(ctx, "k_wn_points", (k_wn_points<3><<<blocks(np, WN_THREADS), WN_THREADS, 0, s>>>(d_pts, np, t->inode, t->leaf, t->inode3,
+                                                                                         t->leaf3, int(t->nt), beta, d_out, st.p)));
+  else
+    BS_KERNEL(ctx, "k_wn_points", (k_wn_points<2><<<blocks(np, WN_THREADS), WN_THREADS, 0, s>>>(d_pts, np, t->inode, t->leaf, nullptr,
+                                                                                         nullptr, int(t->nt), beta, d_out, st.p)));
+  M2VStats hs;
+  read_back(ctx, &hs, st.p, sizeof hs);
+  if (hs.error == 3) fail(BS_ERR_CAPACITY, "winding-number traversal stack overflow");
+  ctx->last_stats[6] = hs.wn_visits;
+  ctx->last_stats[7] = (hs.wn_far & 0xffffffffull) | (hs.wn_exact << 32);
+}
+
+}  // namespace bs
+
+extern "C" {
+
+bs_status bs_winding_numbers_build(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
+                                   int order, bs_wn_tree** out) {
+  if (!ctx || !out || (nt && (!d_xyz || !d_tri))) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  try {
+    BS_CUDA(cudaSetDevice(ctx->device));
+    *out = bs::wn_tree_build(ctx, d_xyz, nv, d_tri, nt, order);
+    return BS_OK;
+  } catch (const bs::Error& e) {
+    ctx->last_error = e.msg;
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    return BS_ERR_OOM;
+  }
+}
+
+bs_status bs_winding_numbers_approximate(bs_ctx* ctx, const bs_wn_tree* t, const float* d_points, uint64_t n_points,
+                                         float beta, float* d_out) {
+  if (!ctx || !t || t->ctx != ctx || (n_points && (!d_points || !d_out)) || !(beta > 0.f)) return BS_ERR_INVALID_ARG;
+  try {
+    BS_CUDA(cudaSetDevice(ctx->device));
+    bs::wn_tree_approximate(ctx, t, d_points, n_points, beta, d_out);
+    return BS_OK;
+  } catch (const bs::Error& e) {
+    ctx->last_error = e.msg;
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    return BS_ERR_OOM;
+  }
+}
+
+bs_status bs_winding_numbers_free(bs_wn_tree* t) {
+  if (!t) return BS_ERR_INVALID_ARG;
+  delete t;
+  return BS_OK;
+}
+
+}  // extern "C"
+
+namespace bs {
 
 bs_volume* mesh_to_volume_impl(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
                                const bs_m2v_params& p) {

@@ -418,6 +418,7 @@ def run_open(args):
     L.bs_m2v_params_default(C.byref(params))
     params.voxel_size = h
     params.band_width = BAND
+    params.wn_order = args.wn_order
     stream = torch.cuda.ExternalStream(ctx.stream)
 
     def step():
@@ -459,7 +460,8 @@ def run_open(args):
             "warmup": args.warmup, "ms_per_step": min(ms), "higher_is_better": True, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": "open icosphere: subdivision 9, 4-octave radial noise 0.1, 10%% of faces "
-                                   "removed (%d triangles), voxel 0.001, band 3" % len(f),
+                                   "removed (%d triangles), voxel 0.001, band 3, far field order %d"
+                                   % (len(f), args.wn_order),
                        "band_voxels_per_step": int(band), "generation_s": t_gen},
             "sign_vs_exact": {"sample": int(len(li)), "mismatches": int(mism.sum()),
                               "mismatches_within_0.01_of_threshold": int((mism & (np.abs(wn - 0.2) < 0.01)).sum()),
@@ -627,6 +629,8 @@ def main():
     ap.add_argument("--workload", default="tori", choices=["tori", "open-icosphere"],
                     help="tori: the boolean workload's two tori (the headline line); open-icosphere: the "
                          "non-watertight subdivision-9 icosphere with an exact-sign check")
+    ap.add_argument("--wn-order", type=int, default=2, choices=[2, 3],
+                    help="far-field order of the sign pass for --workload open-icosphere (2 = the reference's)")
     ap.add_argument("--validation", type=int, default=200000,
                     help="band voxels checked against exact winding numbers (open-icosphere)")
     ap.add_argument("--pipeline-only", action="store_true",

@@ -98,6 +98,8 @@ typedef struct bs_m2v_params {
   int32_t band_width;  /* MeshToVolume::with_narrow_band_width (mesh_to_volume.rs:28-37) */
   float wn_beta;       /* far-field accuracy scale; the reference uses 2.0 (mesh_to_volume.rs:264) */
   float wn_threshold;  /* wn < threshold => outside; the reference uses 0.2 (mesh_to_volume.rs:266) */
+  int32_t wn_order;    /* far-field expansion order: 2 as the reference (aabb_tree.rs:662-691), or 3
+                          (the third-order term the reference leaves undone, aabb_tree.rs:706) */
 } bs_m2v_params;
 
 /* Fills `p` with the reference's defaults (voxel 1, band 0, beta 2, threshold 0.2). */
@@ -155,6 +157,22 @@ bs_status bs_volume_subtract(bs_ctx* ctx, bs_volume* a, bs_volume* b, bs_volume*
 bs_status bs_volume_intersect(bs_ctx* ctx, bs_volume* a, bs_volume* b, bs_volume** out);
 /* Volume::offset (volume/mod.rs:95-108), in place. */
 bs_status bs_volume_offset(bs_ctx* ctx, bs_volume* v, float distance);
+
+/* ------------------------------------------------- winding numbers ---- */
+typedef struct bs_wn_tree bs_wn_tree;
+/* WindingNumbers::from_mesh (spatial_partitioning/aabb_tree.rs:636-644): the
+ * mesh's tree with the far-field records of every node (device arrays: 3
+ * floats per vertex, 3 uint32 per triangle).  order 2 is the reference's
+ * expansion; 3 adds the third-order term the reference leaves undone
+ * (aabb_tree.rs:706).  The tree topology is this library's (PLOC), not the
+ * reference's SAH split. */
+bs_status bs_winding_numbers_build(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
+                                   int order, bs_wn_tree** out);
+/* WindingNumbers::approximate(point, accuracy_scale) (aabb_tree.rs:654-660) at
+ * n_points device points (3 floats each) into d_out; beta = accuracy_scale. */
+bs_status bs_winding_numbers_approximate(bs_ctx* ctx, const bs_wn_tree* tree, const float* d_points, uint64_t n_points,
+                                         float beta, float* d_out);
+bs_status bs_winding_numbers_free(bs_wn_tree* tree);
 
 /* ------------------------------------------- from_fn / VolumeBuilder ---- */
 /* Volume::from_fn (volume/mod.rs:40-72) over values the caller sampled: the
