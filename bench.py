@@ -363,6 +363,7 @@ def run_ours(args):
     roof["launch_ms"] = tot_ms / nl
 
     pipe = pipeline_secondary(ctx, params, dev, L, N, bs, C) if args.pipeline else None
+    fast3 = order3_secondary(ctx, params, dev, L, N, bs, C, args) if args.order3 else None
     batch = batch_secondary(ctx, L, N, bs, C, args.batch_meshes) if args.batch_meshes else None
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -380,7 +381,8 @@ def run_ours(args):
             "stages_ms_per_step": {k: v[0] / args.steps for k, v in sorted(stages.items(), key=lambda kv: -kv[1][0])},
             "last_stats": stats,
             "pipeline": pipe,
-            "batched": batch}
+            "batched": batch,
+            "order3_beta1.5": fast3}
     if rank == 0:
         if world == 1:
             line["cpu_baseline"] = cpu_baseline()
@@ -419,6 +421,7 @@ def run_open(args):
     params.voxel_size = h
     params.band_width = BAND
     params.wn_order = args.wn_order
+    params.wn_beta = args.wn_beta
     stream = torch.cuda.ExternalStream(ctx.stream)
 
     def step():
@@ -460,14 +463,56 @@ def run_open(args):
             "warmup": args.warmup, "ms_per_step": min(ms), "higher_is_better": True, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": "open icosphere: subdivision 9, 4-octave radial noise 0.1, 10%% of faces "
-                                   "removed (%d triangles), voxel 0.001, band 3, far field order %d"
-                                   % (len(f), args.wn_order),
+                                   "removed (%d triangles), voxel 0.001, band 3, far field order %d, "
+                                   "beta %g" % (len(f), args.wn_order, args.wn_beta),
                        "band_voxels_per_step": int(band), "generation_s": t_gen},
             "sign_vs_exact": {"sample": int(len(li)), "mismatches": int(mism.sum()),
                               "mismatches_within_0.01_of_threshold": int((mism & (np.abs(wn - 0.2) < 0.01)).sum()),
                               "exact_pass_s": t_exact},
             "last_stats": stats}
     print(json.dumps(line))
+
+
+def order3_secondary(ctx, params, dev, L, N, bs, C, args):
+    """The same conversion with the order-3 far field at accuracy scale 1.5
+    (not the reference's order 2 / scale 2): band voxels/s, and how many band
+    voxel signs differ from the reference-parameter result."""
+    import copy
+
+    import torch
+    p3 = copy.copy(params)
+    p3.wn_order = 3
+    p3.wn_beta = 1.5
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def conv(p):
+        vols = []
+        for x, t in dev:
+            out = C.c_void_p()
+            N.check(L.bs_mesh_to_volume_device(ctx.h, x.data_ptr(), x.shape[0], t.data_ptr(), t.shape[0],
+                                               C.byref(p), C.byref(out)), ctx.h)
+            vols.append(bs.Volume(out, ctx))
+        return vols
+
+    for _ in range(max(1, args.warmup // 2)):
+        conv(p3)
+    ms = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        v3 = conv(p3)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    band = sum(v.counts()["active_voxels"] for v in v3)
+    v2 = conv(params)
+    diff = 0
+    for a, b in zip(v2, v3):
+        (_, va, ma), (_, vb, mb) = a.export(), b.export()
+        act = np.unpackbits(ma.view(np.uint8), bitorder="little").reshape(len(ma), 512).astype(bool)
+        diff += int(np.sum(np.signbit(va[act]) != np.signbit(vb[act])))
+    return {"value": band / (min(ms) / 1000.0), "unit": UNIT, "ms_per_step": min(ms),
+            "sign_differences_vs_reference_parameters": diff, "band_voxels": int(band)}
 
 
 def batch_secondary(ctx, L, N, bs, C, n_meshes, reps=3):
@@ -624,6 +669,8 @@ def main():
                     help="skip the secondary boolean / offset / dual-contouring timings")
     ap.add_argument("--tris-fraction", type=float, default=1.0,
                     help="use only the first part of each torus ring (smaller case for profiling)")
+    ap.add_argument("--no-order3", dest="order3", action="store_false",
+                    help="skip the order-3 / accuracy-scale-1.5 sign-pass comparison")
     ap.add_argument("--batch-meshes", type=int, default=256,
                     help="meshes of the uneven-batch comparison (0 skips it)")
     ap.add_argument("--workload", default="tori", choices=["tori", "open-icosphere"],
@@ -631,6 +678,8 @@ def main():
                          "non-watertight subdivision-9 icosphere with an exact-sign check")
     ap.add_argument("--wn-order", type=int, default=2, choices=[2, 3],
                     help="far-field order of the sign pass for --workload open-icosphere (2 = the reference's)")
+    ap.add_argument("--wn-beta", type=float, default=2.0,
+                    help="accuracy scale of the sign pass for --workload open-icosphere (2 = the reference's)")
     ap.add_argument("--validation", type=int, default=200000,
                     help="band voxels checked against exact winding numbers (open-icosphere)")
     ap.add_argument("--pipeline-only", action="store_true",
