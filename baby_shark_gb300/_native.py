@@ -39,6 +39,7 @@ SIGNATURES = {
     "bs_ctx_stage_info": (i32, [vp, i32, C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.POINTER(u64)]),
     "bs_ctx_stage_reset": (i32, [vp]),
     "bs_ctx_last_stats": (i32, [vp, C.POINTER(u64)]),
+    "bs_ctx_last_counters": (i32, [vp, C.POINTER(u64)]),
     "bs_diag_fp32_peak": (i32, [vp, C.POINTER(C.c_double)]),
     "bs_winding_numbers_exact": (i32, [vp, vp, u64, vp, u64, vp, u64, vp]),
     "bs_winding_numbers_build": (i32, [vp, vp, u64, vp, u64, i32, PP]),

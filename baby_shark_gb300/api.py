@@ -69,17 +69,24 @@ class Context:
         return out
 
     def last_stats(self):
-        """Counters of the last mesh -> volume conversion (see bs_ctx_last_stats)."""
-        a = (C.c_uint64 * 8)()
-        N.check(self._lib.bs_ctx_last_stats(self.h, a), self.h)
-        keys = ["triangles", "subtris", "brick_pairs", "voxel_pairs", "leaves", "active_voxels"]
-        out = dict(zip(keys, [int(x) for x in a]))
-        out["wn_warp_visits"] = int(a[6])
-        out["wn_warp_far"] = int(a[7]) & 0xffffffff
-        out["wn_warp_exact"] = int(a[7]) >> 32
-        # after an offset: relaxation passes and leaf sweeps of its 8 sweeps
-        out["offset_passes"] = int(a[6])
-        out["offset_leaf_sweeps"] = int(a[7])
+        """Counters of the last mesh -> volume, offset, dual contouring or
+        winding-number call (bs_ctx_last_counters), named for that call."""
+        a = (C.c_uint64 * 16)()
+        N.check(self._lib.bs_ctx_last_counters(self.h, a), self.h)
+        a = [int(x) for x in a]
+        kind = a[8]
+        if kind == 2:
+            return {"call": "offset", "offset_passes": a[6], "offset_leaf_sweeps": a[7]}
+        if kind == 3:
+            return {"call": "dual_contouring", "crossings": a[6], "cells": a[7]}
+        out = {"call": "winding_numbers" if kind == 4 else "mesh_to_volume"}
+        if kind != 4:
+            keys = ["triangles", "subtris", "brick_pairs", "voxel_pairs", "leaves", "active_voxels"]
+            out.update(zip(keys, a[:6]))
+            out["voxel_pairs_evaluated"] = a[9]
+        out["wn_warp_visits"] = a[6]
+        out["wn_warp_far"] = a[7] & 0xffffffff
+        out["wn_warp_exact"] = a[7] >> 32
         return out
 
 

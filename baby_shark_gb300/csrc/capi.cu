@@ -201,6 +201,12 @@ bs_status bs_ctx_last_stats(const bs_ctx* ctx, uint64_t* out8) {
   return BS_OK;
 }
 
+bs_status bs_ctx_last_counters(const bs_ctx* ctx, uint64_t* out16) {
+  if (!ctx || !out16) return BS_ERR_INVALID_ARG;
+  for (int k = 0; k < 16; ++k) out16[k] = ctx->last_stats[k];
+  return BS_OK;
+}
+
 void bs_m2v_params_default(bs_m2v_params* p) {
   if (!p) return;
   p->voxel_size = 1.0f;   // MeshToVolume::default (mesh_to_volume.rs:223-236)

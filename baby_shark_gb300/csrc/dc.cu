@@ -528,6 +528,7 @@ void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size, int mode) {
   v->dc_mode = mode;
   ctx->last_stats[6] = ne;
   ctx->last_stats[7] = nc;
+  ctx->last_stats[8] = BS_STATS_DUAL_CONTOURING;
 }
 
 }  // namespace bs

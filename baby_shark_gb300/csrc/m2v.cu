@@ -62,6 +62,7 @@ struct M2VStats {
   unsigned long long wn_visits;      // warp-level node visits of the winding-number pass
   unsigned long long wn_far;         // warp-level far-field evaluations (internal + leaf dipoles)
   unsigned long long wn_exact;       // warp-level exact solid angles
+  unsigned long long n_eval;         // (voxel, sub-triangle) pairs left after culling
 };
 
 // Per-mesh parameters of a batch.  Triangles of mesh m are [tri_base,
@@ -366,62 +367,162 @@ __global__ void k_act_starts(const uint32_t* __restrict__ voff, const uint32_t* 
 }
 
 // ----------------------------------------------- 3. per-brick distances ----
-// One CTA of 128 threads per brick.  Each warp takes sub-triangles of the
-// brick's list in turn and its lanes walk only the voxels of (widened box of
-// the sub-triangle) x (brick); the per-voxel minimum is kept in shared memory
-// with atomicMin on the float bits (distances are >= 0, so unsigned order is
-// float order; NaN distances are skipped, as `dist < cur` never holds for NaN
-// in the reference).
+// One CTA of 128 threads per brick.  Each warp stages DIST_BATCH sub-triangles
+// of the brick's list and its lanes walk the (voxel, sub-triangle) pairs of
+// (widened box of the sub-triangle) x (brick); the per-voxel minimum is kept
+// in shared memory with atomicMin on the float bits (distances are >= 0, so
+// unsigned order is float order; NaN distances are skipped, as `dist < cur`
+// never holds for NaN in the reference).
+//
+// Pairs that cannot lower the voxel's minimum are culled before the exact
+// point-triangle distance is evaluated: a pair is dropped when the distance
+// from the voxel to the sub-triangle's bounding box, less a per-triangle
+// bound rho on how far the float32 closest point of the reference's formula
+// can stray from the triangle, already exceeds the voxel's running minimum.
+// The running minimum is a value some evaluated pair produced, so the
+// minimum over the surviving pairs equals the minimum over all pairs, bit
+// for bit, whatever the order; a voxel whose minimum is still +inf keeps all
+// its pairs, so the active set is unchanged too.  Lanes take (sub-triangle,
+// y, z) columns of the staged sub-triangles and step along x (the x part of
+// the bound comes from a per-sub-triangle table, the y and z parts once per
+// column); survivors go through a per-warp queue and are evaluated 32 at a
+// time with all lanes busy.
 constexpr int DIST_THREADS = 128;
-constexpr int DIST_BATCH = 8;  // sub-triangles a warp packs into one stream of (voxel, sub-triangle) pairs
+constexpr int DIST_BATCH = 16;  // sub-triangles a warp stages at a time
+constexpr int DIST_QUEUE = 32 + 8 * 32;  // < 32 left over + one column walk of 8 steps x 32 lanes
 
-struct BatchTri {
-  float a[3], b[3], c[3], ab[3], ac[3], cb[3];
-  int x0, y0, z0, ny, nz, nyz;
-  float rnyz, rnz;
+struct __align__(16) BatchTri {
+  float4 v0;   // a.x a.y a.z ab.x
+  float4 v1;   // ab.y ab.z ac.x ac.y
+  float4 v2;   // ac.z b.x b.y b.z
+  float4 v3;   // c.x c.y c.z cb.x
+  float4 v4;   // cb.y cb.z rho2 1/nz
+  float4 dxa;  // (1 - 2^-20) dx^2 of the first voxels in x: distance to the bounding box in x
+  float4 dxb;  //   ... voxels 4..7
+  float4 yz;   // bounding box lo.y lo.z hi.y hi.z
+  int4 box;    // x0 y0 z0 nx: first voxel of (widened box) x (brick) and its x extent
+  int4 box1;   // nz - - -
 };
 
-__global__ void __launch_bounds__(DIST_THREADS, 9) k_brick_distance(
+// Squared cull margin 17 rho^2 of one sub-triangle (+inf: never cull).
+// In the reference's closest-point formula (Ericson, point_triangle_dist2)
+// the vertex cases return a vertex exactly and the edge cases a parameter in
+// [0, 1] (their denominators add two numbers of one sign), so there the
+// float32 closest point leaves the triangle only by rounding: 16 u (e + R)
+// + 4 u M with u = 2^-24, e the longest edge, R a bound on |p - vertex| and M
+// on |coordinates|.  The face case divides by va + vb + vc, whose exact value
+// is |ab x ac|^2 and whose float32 error is at most about 70 u e^2 R^2 (the
+// six dot products carry 5 u e R each); the parameters then move by at most
+// about 93 u e^2 R^2 / (|ab x ac|^2 / 4) and the point by 188 u e^3 R^2 /
+// |ab x ac|^2, bounded here by 1024 u e^3 R^2 / |ab x ac|^2 =: eps_face.
+// Sub-triangles where that perturbation is not small (eps_face > e) are never
+// culled.  rho = 2 eps also covers the rounding of the final |q - p|^2.  The
+// cull test lb' > cur * 17/16 + 17 rho^2, with lb' the float32 sum of the
+// squared box distances each scaled by 1 - 2^-20 (so lb' < lb (1 - 8 u)),
+// implies sqrt(lb) > sqrt(cur) + rho (2 rho sqrt(cur) <= cur / 16 + 16 rho^2),
+// so a culled pair's float32 distance is above cur.
+__device__ __forceinline__ float cull_margin2(F3 ab, F3 ac, F3 cb, float R, float M) {
+  const float u = 5.9604645e-8f;
+  const float e2 = fmaxf(dot3(ab, ab), fmaxf(dot3(ac, ac), dot3(cb, cb)));
+  const float e = sqrtf(e2);
+  const F3 n = cross3(ab, ac);
+  const float a2sq = dot3(n, n);
+  const float face = 1024.0f * u * (e2 * e * R * R / a2sq);  // +inf or NaN for a degenerate triangle
+  if (!(face <= e)) return __int_as_float(0x7f800000);
+  const float eps = face + 16.0f * u * (e + R) + 4.0f * u * M;
+  const float rho = 2.0f * eps;
+  const float r2 = 17.0f * rho * rho;
+  return r2 == r2 ? r2 : __int_as_float(0x7f800000);
+}
+
+constexpr float CULL_SCALE = 1.0f - 0x1p-20f;
+
+__device__ __forceinline__ float box_d(float lo, float hi, float g) { return fmaxf(fmaxf(lo - g, g - hi), 0.0f); }
+
+__global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
     const int4* __restrict__ origins, const uint32_t* __restrict__ list_off, const uint32_t* __restrict__ list,
     const SubTri* __restrict__ S, const MeshInfo* __restrict__ mi, const uint32_t* __restrict__ leaf_base, int K,
-    float* __restrict__ values, uint32_t* __restrict__ masks) {
+    float* __restrict__ values, uint32_t* __restrict__ masks, M2VStats* st) {
   __shared__ uint32_t dmin[512];
   __shared__ BatchTri bt[DIST_THREADS / 32][DIST_BATCH];
   __shared__ int pre[DIST_THREADS / 32][DIST_BATCH + 1];
+  __shared__ uint32_t queue[DIST_THREADS / 32][DIST_QUEUE];
+  __shared__ float gtab[3][8];  // grid coordinates x * h of the brick's voxels, per axis
+  __shared__ uint32_t evaluated;
   const int b = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int4 org = origins[b];
-  const float h = mi[find_seg(leaf_base, K, uint64_t(b))].h;
+  const int mesh = find_seg(leaf_base, K, uint64_t(b));
+  const float h = mi[mesh].h;
   for (int o = t; o < 512; o += DIST_THREADS) dmin[o] = 0x7f800000u;  // +inf
+  if (t < 24) {
+    const int ax = t >> 3, i = t & 7;
+    gtab[ax][i] = fmul(__int2float_rn((ax == 0 ? org.x : ax == 1 ? org.y : org.z) + i), h);
+  }
+  if (t == 0) evaluated = 0;
   __syncthreads();
   const uint32_t beg = list_off[b], end = list_off[b + 1];
   BatchTri* W = bt[warp];
   int* P = pre[warp];
+  uint32_t* Q = queue[warp];
+  const uint32_t lt = (1u << lane) - 1u;
+  uint32_t n_eval = 0;
+
+  // exact distance of one queued pair (entry = j << 9 | voxel offset)
+  auto eval = [&](uint32_t ent) {
+    const BatchTri& q = W[ent >> 9];
+    const int o = int(ent & 511u);
+    const F3 g = f3(gtab[0][o >> 6], gtab[1][(o >> 3) & 7], gtab[2][o & 7]);
+    const float4 v0 = q.v0, v1 = q.v1, v2 = q.v2, v3 = q.v3, v4 = q.v4;
+    const float d2 = point_triangle_dist2_flat(f3(v0.x, v0.y, v0.z), f3(v2.y, v2.z, v2.w), f3(v3.x, v3.y, v3.z),
+                                               f3(v0.w, v1.x, v1.y), f3(v1.z, v1.w, v2.x), f3(v3.w, v4.x, v4.y), g);
+    if (d2 < __int_as_float(0x7f800000))  // false for NaN and +inf
+      atomicMin(&dmin[o], __float_as_uint(d2));
+  };
+
   for (uint32_t e0 = beg + warp * DIST_BATCH; e0 < end; e0 += (DIST_THREADS / 32) * DIST_BATCH) {
-    // lanes 0..BATCH-1: stage one sub-triangle each and count its voxels in this brick
-    int cnt = 0;
+    // lanes 0..BATCH-1: stage one sub-triangle each and count its (y, z)
+    // columns of voxels in this brick
+    int cols = 0;
     if (lane < DIST_BATCH && e0 + lane < end) {
-      const SubTri st = S[list[e0 + lane]];
-      const F3 a = f3(st.p0.x, st.p0.y, st.p0.z), bb = f3(st.p0.w, st.p1.x, st.p1.y), c = f3(st.p1.z, st.p1.w, st.p2.x);
-      const int x0 = max(st.lo.x, org.x), y0 = max(st.lo.y, org.y), z0 = max(st.lo.z, org.z);
-      const int nx = min(st.hi.x, org.x + 7) - x0 + 1, ny = min(st.hi.y, org.y + 7) - y0 + 1,
-                nz = min(st.hi.z, org.z + 7) - z0 + 1;
+      const SubTri sb = S[list[e0 + lane]];
+      const F3 a = f3(sb.p0.x, sb.p0.y, sb.p0.z), bb = f3(sb.p0.w, sb.p1.x, sb.p1.y), c = f3(sb.p1.z, sb.p1.w, sb.p2.x);
+      const int x0 = max(sb.lo.x, org.x), y0 = max(sb.lo.y, org.y), z0 = max(sb.lo.z, org.z);
+      const int nx = min(sb.hi.x, org.x + 7) - x0 + 1, ny = min(sb.hi.y, org.y + 7) - y0 + 1,
+                nz = min(sb.hi.z, org.z + 7) - z0 + 1;
       if (nx > 0 && ny > 0 && nz > 0) {
         BatchTri& q = W[lane];
         const F3 ab = sub3(bb, a), ac = sub3(c, a), cb = sub3(c, bb);
-        q.a[0] = a.x; q.a[1] = a.y; q.a[2] = a.z;
-        q.b[0] = bb.x; q.b[1] = bb.y; q.b[2] = bb.z;
-        q.c[0] = c.x; q.c[1] = c.y; q.c[2] = c.z;
-        q.ab[0] = ab.x; q.ab[1] = ab.y; q.ab[2] = ab.z;
-        q.ac[0] = ac.x; q.ac[1] = ac.y; q.ac[2] = ac.z;
-        q.cb[0] = cb.x; q.cb[1] = cb.y; q.cb[2] = cb.z;
-        q.x0 = x0; q.y0 = y0; q.z0 = z0; q.ny = ny; q.nz = nz; q.nyz = ny * nz;
-        q.rnyz = 1.0f / float(ny * nz);
-        q.rnz = 1.0f / float(nz);
-        cnt = nx * ny * nz;
+        // R: the widened box holds the vertices and every voxel it covers
+        const float ex = float(sb.hi.x - sb.lo.x), ey = float(sb.hi.y - sb.lo.y), ez = float(sb.hi.z - sb.lo.z);
+        const float R = h * (sqrtf(ex * ex + ey * ey + ez * ez) + 2.0f);
+        const float gm = h * float(max(max(max(abs(sb.lo.x), abs(sb.hi.x)), max(abs(sb.lo.y), abs(sb.hi.y))),
+                                       max(abs(sb.lo.z), abs(sb.hi.z))) + 1);
+        const float M = fmaxf(gm, fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(bb.x))),
+                                        fmaxf(fmaxf(fabsf(bb.y), fabsf(bb.z)),
+                                              fmaxf(fmaxf(fabsf(c.x), fabsf(c.y)), fabsf(c.z)))));
+        const float lox = fminf(fminf(a.x, bb.x), c.x), hix = fmaxf(fmaxf(a.x, bb.x), c.x);
+        float dx[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const float d = box_d(lox, hix, gtab[0][min(x0 - org.x + i, 7)]);
+          dx[i] = fmul(fmul(d, d), CULL_SCALE);
+        }
+        q.v0 = make_float4(a.x, a.y, a.z, ab.x);
+        q.v1 = make_float4(ab.y, ab.z, ac.x, ac.y);
+        q.v2 = make_float4(ac.z, bb.x, bb.y, bb.z);
+        q.v3 = make_float4(c.x, c.y, c.z, cb.x);
+        q.v4 = make_float4(cb.y, cb.z, cull_margin2(ab, ac, cb, R, M), 1.0f / float(nz));
+        q.dxa = make_float4(dx[0], dx[1], dx[2], dx[3]);
+        q.dxb = make_float4(dx[4], dx[5], dx[6], dx[7]);
+        q.yz = make_float4(fminf(fminf(a.y, bb.y), c.y), fminf(fminf(a.z, bb.z), c.z),
+                           fmaxf(fmaxf(a.y, bb.y), c.y), fmaxf(fmaxf(a.z, bb.z), c.z));
+        q.box = make_int4(x0, y0, z0, nx);
+        q.box1 = make_int4(nz, 0, 0, 0);
+        cols = ny * nz;
       }
     }
-    // inclusive prefix over the batch lanes
-    int inc = cnt;
+    // inclusive prefix of the column counts over the batch lanes
+    int inc = cols;
 #pragma unroll
     for (int d = 1; d < DIST_BATCH; d <<= 1) {
       const int v = __shfl_up_sync(0xffffffffu, inc, d);
@@ -431,29 +532,64 @@ __global__ void __launch_bounds__(DIST_THREADS, 9) k_brick_distance(
     if (lane == 0) P[0] = 0;
     const int total = __shfl_sync(0xffffffffu, inc, DIST_BATCH - 1);
     __syncwarp();
-    for (int k = lane; k < total; k += 32) {
-      int j = 0;
-#pragma unroll
-      for (int q = 1; q < DIST_BATCH; ++q) j = (k >= P[q]) ? q : j;
-      const BatchTri& q = W[j];
-      const int r0 = k - P[j];
-      // r0 -> (ix, iy, iz) by reciprocal multiply: r0 < 512 and nyz <= 64 keep
-      // the product at least 0.5/64 away from the next integer
-      const int ix = int((float(r0) + 0.5f) * q.rnyz), r = r0 - ix * q.nyz;
-      const int iy = int((float(r) + 0.5f) * q.rnz), iz = r - iy * q.nz;
-      const int x = q.x0 + ix, y = q.y0 + iy, z = q.z0 + iz;
-      const F3 g = f3(fmul(__int2float_rn(x), h), fmul(__int2float_rn(y), h), fmul(__int2float_rn(z), h));
-      const float d2 = point_triangle_dist2_e(f3(q.a[0], q.a[1], q.a[2]), f3(q.b[0], q.b[1], q.b[2]),
-                                              f3(q.c[0], q.c[1], q.c[2]), f3(q.ab[0], q.ab[1], q.ab[2]),
-                                              f3(q.ac[0], q.ac[1], q.ac[2]), f3(q.cb[0], q.cb[1], q.cb[2]), g);
-      if (d2 < __int_as_float(0x7f800000)) {  // false for NaN and +inf
-        const int o = ((x - org.x) << 6) | ((y - org.y) << 3) | (z - org.z);
-        atomicMin(&dmin[o], __float_as_uint(d2));
+    int j = 0, qn = 0;
+    for (int base = 0; base < total; base += 32) {
+      // one lane per (sub-triangle, y, z) column; the column's voxels follow in x
+      const int k = base + lane;
+      int nx = 0, o = 0;
+      float dyz = 0.0f, rho2 = 0.0f;
+      float4 dxa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), dxb = dxa;
+      if (k < total) {
+        while (k >= P[j + 1]) ++j;  // P[DIST_BATCH] = total > k
+        const BatchTri& q = W[j];
+        const int4 bx = q.box;
+        const float4 v4 = q.v4, yz = q.yz;
+        const int c = k - P[j];
+        // c -> (iy, iz) by reciprocal multiply: c < 64 and nz <= 8 keep the
+        // product at least 0.5/8 away from the next integer
+        const int iy = int((float(c) + 0.5f) * v4.w), iz = c - iy * q.box1.x;
+        const int oy = bx.y - org.y + iy, oz = bx.z - org.z + iz;
+        const float dy = box_d(yz.x, yz.z, gtab[1][oy]), dz = box_d(yz.y, yz.w, gtab[2][oz]);
+        dyz = fadd(fmul(fmul(dy, dy), CULL_SCALE), fmul(fmul(dz, dz), CULL_SCALE));
+        rho2 = v4.z;
+        dxa = q.dxa;
+        dxb = q.dxb;
+        nx = bx.w;
+        o = ((bx.x - org.x) << 6) | (oy << 3) | oz;
       }
+      const int steps = __reduce_max_sync(0xffffffffu, nx);
+      const uint32_t jj = uint32_t(j) << 9;
+      const float dxs[8] = {dxa.x, dxa.y, dxa.z, dxa.w, dxb.x, dxb.y, dxb.z, dxb.w};
+#pragma unroll
+      for (int ix = 0; ix < 8; ++ix) {
+        if (ix < steps) {
+          bool keep = false;
+          if (ix < nx) {
+            const float cur = __uint_as_float(dmin[o + 64 * ix]);
+            keep = !(fadd(dxs[ix], dyz) > fmaf(cur, 1.0625f, rho2));
+          }
+          const uint32_t m = __ballot_sync(0xffffffffu, keep);
+          if (keep) Q[qn + __popc(m & lt)] = jj | uint32_t(o + 64 * ix);
+          qn += __popc(m);
+        }
+      }
+      while (qn >= 32) {
+        __syncwarp();
+        qn -= 32;
+        eval(Q[qn + lane]);
+        n_eval += 32;
+      }
+      __syncwarp();
+    }
+    if (qn > 0) {
+      if (lane < qn) eval(Q[lane]);
+      n_eval += qn;
     }
     __syncwarp();
   }
+  if (lane == 0 && n_eval) atomicAdd(&evaluated, n_eval);
   __syncthreads();
+  if (t == 0 && evaluated) atomicAdd(&st[mesh].n_eval, (unsigned long long)evaluated);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int o = t + DIST_THREADS * k;
@@ -1012,10 +1148,6 @@ constexpr int WN_STACK = 96;
 // for query points on a triangle's plane the numerator is then the
 // reference's exact value (often exactly 0, which the reference treats as
 // "on the surface"), so such voxels take the reference's sign.
-__device__ __forceinline__ F3 cross3(F3 a, F3 b) {
-  return {fsub(fmul(a.y, b.z), fmul(a.z, b.y)), fsub(fmul(a.z, b.x), fmul(a.x, b.z)),
-          fsub(fmul(a.x, b.y), fmul(a.y, b.x))};
-}
 __device__ __forceinline__ float tri_wn_exact(float4 A, float4 B, float4 C, F3 q) {
   F3 qa = sub3(f3(A.x, A.y, A.z), q), qb = sub3(f3(B.x, B.y, B.z), q), qc = sub3(f3(C.x, C.y, C.z), q);
   const float la = fsqrt(dot3(qa, qa)), lb = fsqrt(dot3(qb, qb)), lc = fsqrt(dot3(qc, qc));
@@ -1641,7 +1773,7 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
     BS_KERNEL(ctx, "k_fill_pairs", (k_fill_pairs<<<blocks(ns, 256), 256, 0, s>>>(S.p, ns, d_dirs.p, d_db.p, cnt.p, list.p)));
     cnt.reset();
     BS_KERNEL(ctx, "k_brick_distance", (k_brick_distance<<<unsigned(nb), DIST_THREADS, 0, s>>>(origins.p, list_off.p, list.p, S.p, d_mi.p,
-                                                          leaf_base.p, K, values.p, masks.p)));
+                                                          leaf_base.p, K, values.p, masks.p, st.p)));
   }
   S.reset();
 
@@ -1689,10 +1821,11 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
                                                                                        inode3.p, leaf3.p, st.p)));
   }
   read_back(ctx, hst.data(), st.p, K * sizeof(M2VStats));
-  uint64_t n_vp = 0, n_p = 0, visits = 0, far = 0, exact = 0;
+  uint64_t n_vp = 0, n_p = 0, visits = 0, far = 0, exact = 0, n_ev = 0;
   for (int m = 0; m < K; ++m) {
     if (hst[m].error == 3) fail(BS_ERR_CAPACITY, "winding-number traversal stack overflow");
     n_vp += hst[m].n_vpairs;
+    n_ev += hst[m].n_eval;
     n_p += hst[m].n_pairs;
     visits += hst[m].wn_visits;
     far += hst[m].wn_far;
@@ -1706,6 +1839,8 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   ctx->last_stats[5] = na;
   ctx->last_stats[6] = visits;
   ctx->last_stats[7] = (far & 0xffffffffull) | (exact << 32);
+  ctx->last_stats[8] = BS_STATS_MESH_TO_VOLUME;
+  ctx->last_stats[9] = n_ev;
 
   // hand out the volumes
   std::vector<bs_volume*> vols(K, nullptr);
@@ -1846,6 +1981,7 @@ static void wn_tree_approximate(bs_ctx* ctx, const bs_wn_tree* t, const float* d
   if (hs.error == 3) fail(BS_ERR_CAPACITY, "winding-number traversal stack overflow");
   ctx->last_stats[6] = hs.wn_visits;
   ctx->last_stats[7] = (hs.wn_far & 0xffffffffull) | (hs.wn_exact << 32);
+  ctx->last_stats[8] = BS_STATS_WINDING_NUMBERS;
 }
 
 }  // namespace bs

@@ -709,6 +709,7 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   read_back(ctx, &n, S.n_slots, sizeof(int));
   ctx->last_stats[6] = total_passes;
   ctx->last_stats[7] = total_sweeps;
+  ctx->last_stats[8] = BS_STATS_OFFSET;
   // adopt the swept arrays (dead and empty slots go with the next compaction)
   dfree(ctx, v->d_origins);
   dfree(ctx, v->d_values);

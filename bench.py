@@ -40,6 +40,7 @@ H = 0.002
 BAND = 3
 # Algorithmic work per unit, counted from the reference's operations.
 FLOP_PER_PAIR = 84          # closest point + norm, triangle3.rs:317-382 (face-region path)
+CULL_FLOP_PER_PAIR = 20     # voxel to bounding box distance and the cull comparison
 WN_FLOP_FAR = 31            # far test + order-1/2 terms, aabb_tree.rs:662-671, 803-816
 WN_FLOP_EXACT = 70          # Van Oosterom-Strackee solid angle, aabb_tree.rs:582-615 (atan2 as 20)
 WN_FAR_PER_VOXEL = 110.1    # the oracle's traversal of the reference's SAH tree on this workload's
@@ -337,9 +338,14 @@ def run_ours(args):
     fp32_peak = fp32_peak_tflops(ctx)
     per_launch_s = tot_ms / nl / 1000.0
     # stats are of the last conversion (torus B); both tori are the same size class
+    extra = {}
     if name == "k_brick_distance":
-        flops = FLOP_PER_PAIR * stats["voxel_pairs"]
-        algo = "%d FLOP x (voxel, sub-triangle) pairs = %d per launch" % (FLOP_PER_PAIR, stats["voxel_pairs"])
+        ev = stats["voxel_pairs_evaluated"]
+        flops = FLOP_PER_PAIR * ev + CULL_FLOP_PER_PAIR * stats["voxel_pairs"]
+        algo = ("%d FLOP x %d evaluated (voxel, sub-triangle) pairs + %d FLOP cull test x %d pairs per launch"
+                % (FLOP_PER_PAIR, ev, CULL_FLOP_PER_PAIR, stats["voxel_pairs"]))
+        extra["reference_equivalent_tflops"] = FLOP_PER_PAIR * stats["voxel_pairs"] / per_launch_s / 1e12
+        extra["pairs_evaluated_fraction"] = ev / max(1, stats["voxel_pairs"])
     elif name == "k_wn_sign":
         flops = WN_FLOP_PER_VOXEL * stats["active_voxels"]
         algo = ("%d FLOP per band voxel (the reference's own traversal: %.0f far-field nodes x %d FLOP + "
@@ -355,7 +361,7 @@ def run_ours(args):
                 "frac": achieved / fp32_peak if fp32_peak else None, "traffic": TRAFFIC_PER_LAUNCH.get(name),
                 "peak_source": "measured on this GPU by bs_diag_fp32_peak (FFMA loop); MEASURED_PEAKS.json "
                                "holds no FP32 figure",
-                "algorithmic": algo}
+                "algorithmic": algo, **extra}
     else:
         roof = {"kernel": name, "bound": "hbm", "achieved": None, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                 "frac": None, "traffic": None, "peak_source": src}
@@ -623,7 +629,7 @@ def pipeline_secondary(ctx, params, dev, L, N, bs, C):
             cc = c.clone()
             _, t_off = timed(lambda: cc.offset(dist))
             st = ctx.last_stats()
-            d["offset_%s_relax_passes" % sign] = st["offset_passes"]
+            d["offset_%s_relax_passes" % sign] = st.get("offset_passes")
             d["offset_%s_leaf_sweeps" % sign] = st["offset_leaf_sweeps"]
             n = C.c_uint64()
             _, t_dc = timed(lambda: N.check(L.bs_dual_contour(ctx.h, cc.h, params.voxel_size, None, 0, C.byref(n)),

@@ -81,6 +81,18 @@ bs_status bs_ctx_stage_reset(bs_ctx* ctx);
  * [6] and [7] with its crossing and cell counts, an offset call with its
  * relaxation passes and leaf sweeps over the 8 sweep directions. */
 bs_status bs_ctx_last_stats(const bs_ctx* ctx, uint64_t* out8);
+/* The same counters and more: [0..7] as above, [8] which call wrote them
+ * (bs_stats_kind), [9] (voxel, sub-triangle) pairs whose exact distance a
+ * mesh -> volume call evaluated after culling (the rest provably could not
+ * lower their voxel's minimum), [10..15] zero. */
+enum bs_stats_kind {
+  BS_STATS_NONE = 0,
+  BS_STATS_MESH_TO_VOLUME = 1,
+  BS_STATS_OFFSET = 2,
+  BS_STATS_DUAL_CONTOURING = 3,
+  BS_STATS_WINDING_NUMBERS = 4
+};
+bs_status bs_ctx_last_counters(const bs_ctx* ctx, uint64_t* out16);
 /* Measured FP32 FMA throughput of the context's device in TFLOP/s (a timed
  * FFMA loop over all SMs); the denominator of FP32-bound roofline fractions. */
 bs_status bs_diag_fp32_peak(bs_ctx* ctx, double* tflops);

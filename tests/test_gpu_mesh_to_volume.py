@@ -120,6 +120,65 @@ def test_degenerate_triangles():
     assert_parity_open(v, f, 0.1, 1)
 
 
+def cull_stress_soup(h, seed):
+    """Random soup for the pair culling of the distance pass: well-shaped
+    triangles of 0.3-2 voxels, needles (two vertices within 1e-4 voxel),
+    near-collinear slivers, exactly degenerate triangles and large
+    triangles of ~10 voxels, randomly oriented, far from the origin."""
+    rng = np.random.default_rng(seed)
+    centre = np.array([37.3, -51.9, 12.1], np.float64)
+    tris = []
+
+    def rnd_dir(n):
+        d = rng.normal(size=(n, 3))
+        return d / np.linalg.norm(d, axis=1, keepdims=True)
+
+    n = 300
+    c = centre + rng.uniform(-8 * h, 8 * h, size=(n, 3))
+    s = rng.uniform(0.3, 2.0, size=(n, 1)) * h
+    tris.append(np.stack([c + s * rnd_dir(n), c + s * rnd_dir(n), c + s * rnd_dir(n)], axis=1))
+    n = 120  # needles
+    c = centre + rng.uniform(-8 * h, 8 * h, size=(n, 3))
+    far = c + 1.5 * h * rnd_dir(n)
+    tris.append(np.stack([c, c + 1e-4 * h * rnd_dir(n), far], axis=1))
+    n = 120  # slivers: the third vertex within 1e-5..1e-2 voxel of the line of the others
+    a = centre + rng.uniform(-8 * h, 8 * h, size=(n, 3))
+    b = a + 2.0 * h * rnd_dir(n)
+    t = rng.uniform(0.1, 0.9, size=(n, 1))
+    off = 10.0 ** rng.uniform(-5, -2, size=(n, 1)) * h
+    tris.append(np.stack([a, b, a + t * (b - a) + off * rnd_dir(n)], axis=1))
+    n = 30  # exactly degenerate
+    a = centre + rng.uniform(-8 * h, 8 * h, size=(n, 3))
+    tris.append(np.stack([a, a, a + h * rnd_dir(n)], axis=1))
+    n = 40  # large
+    c = centre + rng.uniform(-6 * h, 6 * h, size=(n, 3))
+    tris.append(np.stack([c + 10 * h * rnd_dir(n), c + 10 * h * rnd_dir(n), c + 10 * h * rnd_dir(n)], axis=1))
+    tri = np.concatenate(tris).astype(np.float32)
+    v = tri.reshape(-1, 3)
+    return v, np.arange(len(v), dtype=np.uint32).reshape(-1, 3)
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_culled_distances_on_slivers_and_needles(seed):
+    """The distance pass skips pairs whose lower bound exceeds the voxel's
+    running minimum; on triangles of every conditioning the distances and
+    the active set stay bit-identical to the oracle's full evaluation."""
+    h, band = 0.05, 2
+    v, f = cull_stress_soup(h, seed)
+    ctx = context()
+    vol = bs.MeshToVolume(ctx).with_voxel_size(h).with_narrow_band_width(band).convert((v, f))
+    st = ctx.last_stats()
+    ov, _, _ = ob.mesh_to_volume(v, f, h, band)
+    go, gv, gm = vol.export()
+    oo, ovv, om = ov.export()
+    perm = np.lexsort((oo[:, 2], oo[:, 1], oo[:, 0]))
+    oo, ovv, om = oo[perm], ovv[perm], om[perm]
+    assert np.array_equal(go, oo) and np.array_equal(gm, om)
+    act = np.stack([unpack_mask(m) for m in om])
+    assert np.array_equal(np.abs(gv[act]).view(np.uint32), np.abs(ovv[act]).view(np.uint32))
+    assert 0 < st["voxel_pairs_evaluated"] < st["voxel_pairs"]
+
+
 def test_empty_mesh_is_none():
     ctx = context()
     v = np.zeros((0, 3), np.float32)
