@@ -286,6 +286,25 @@ __device__ __forceinline__ bool brick_range(const SubTri& s, const Dir& d, int l
   return lo[0] >= 0 && lo[1] >= 0 && lo[2] >= 0 && hi[0] < d.dx && hi[1] < d.dy && hi[2] < d.dz;
 }
 
+// Lists are grouped by the class of each (sub-triangle, brick) pair: the
+// distance from the centre of the sub-triangle's widened box to the brick's
+// centre in steps of 1.25 voxels, capped at LIST_CLASSES - 1.  Each brick's
+// list holds class 0 first, so the distance pass meets the sub-triangles
+// nearest to most of its voxels early and culls more of the rest (the result
+// does not depend on the order).  Integer arithmetic: count and fill agree.
+constexpr int LIST_CLASSES = 8;
+__device__ __forceinline__ int pair_class(const SubTri& s, int bx, int by, int bz) {
+  // twice the centre offset per axis, in voxels
+  const long long dx = (long long)s.lo.x + s.hi.x - (16LL * bx + 7);
+  const long long dy = (long long)s.lo.y + s.hi.y - (16LL * by + 7);
+  const long long dz = (long long)s.lo.z + s.hi.z - (16LL * bz + 7);
+  const long long q = 4 * (dx * dx + dy * dy + dz * dz);  // d >= 1.25 k  <=>  q >= 25 k^2
+  int c = 0;
+#pragma unroll
+  for (int k = 1; k < LIST_CLASSES; ++k) c += q >= 25LL * k * k ? 1 : 0;
+  return c;
+}
+
 __global__ void k_count_pairs(const SubTri* __restrict__ S, uint64_t ns, const Dir* __restrict__ dirs,
                               const uint64_t* __restrict__ dir_base, uint32_t* __restrict__ cnt, M2VStats* st) {
   uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
@@ -293,7 +312,7 @@ __global__ void k_count_pairs(const SubTri* __restrict__ S, uint64_t ns, const D
   SubTri s = S[i];
   const int mesh = s.lo.w;
   const Dir d = dirs[mesh];
-  uint32_t* C = cnt + dir_base[mesh];
+  uint32_t* C = cnt + dir_base[mesh] * LIST_CLASSES;
   int lo[3], hi[3];
   if (!brick_range(s, d, lo, hi)) {
     atomicExch(&st[mesh].error, 2);
@@ -302,37 +321,41 @@ __global__ void k_count_pairs(const SubTri* __restrict__ S, uint64_t ns, const D
   for (int x = lo[0]; x <= hi[0]; ++x)
     for (int y = lo[1]; y <= hi[1]; ++y)
       for (int z = lo[2]; z <= hi[2]; ++z)
-        atomicAdd(&C[(uint64_t(x) * d.dy + y) * d.dz + z], 1u);
+        atomicAdd(&C[((uint64_t(x) * d.dy + y) * d.dz + z) * LIST_CLASSES +
+                     pair_class(s, x + d.bx0, y + d.by0, z + d.bz0)], 1u);
   unsigned long long np = uint64_t(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
   unsigned long long vp = uint64_t(s.hi.x - s.lo.x + 1) * (s.hi.y - s.lo.y + 1) * (s.hi.z - s.lo.z + 1);
   warp_add(&st[mesh].n_pairs, np, mesh);
   warp_add(&st[mesh].n_vpairs, vp, mesh);
 }
 
-__global__ void k_dir_flags(const uint32_t* __restrict__ cnt, uint64_t n, uint32_t* __restrict__ flag) {
+// flag[e] = 1 for directory entries with pairs (pair_off: scan over entries x classes)
+__global__ void k_dir_flags(const uint32_t* __restrict__ pair_off, uint64_t n, uint32_t* __restrict__ flag) {
   uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
-  if (i < n) flag[i] = cnt[i] ? 1u : 0u;
+  if (i < n) flag[i] = pair_off[(i + 1) * LIST_CLASSES] != pair_off[i * LIST_CLASSES] ? 1u : 0u;
   if (i == n) flag[n] = 0u;
 }
 
 // Compacts non-empty directory entries into bricks in (mesh, x, y, z) order
-// and turns cnt[] into per-entry fill cursors.
+// and turns cnt[] into per-(entry, class) fill cursors.
 __global__ void k_dir_compact(uint32_t* __restrict__ cnt, const uint32_t* __restrict__ pair_off,
                               const uint32_t* __restrict__ bidx, uint64_t n, const Dir* __restrict__ dirs,
                               const uint64_t* __restrict__ dir_base, int K, int4* __restrict__ origins,
                               uint32_t* __restrict__ list_off) {
   uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (e >= n) return;
-  if (cnt[e]) {
+  const uint64_t e0 = e * LIST_CLASSES;
+  if (pair_off[e0 + LIST_CLASSES] != pair_off[e0]) {
     const int mesh = find_seg(dir_base, K, e);
     const Dir d = dirs[mesh];
     const uint64_t l = e - dir_base[mesh];
     uint32_t b = bidx[e];
     int z = int(l % d.dz), y = int((l / d.dz) % d.dy), x = int(l / (uint64_t(d.dz) * d.dy));
     origins[b] = make_int4((x + d.bx0) * 8, (y + d.by0) * 8, (z + d.bz0) * 8, 0);
-    list_off[b] = pair_off[e];
+    list_off[b] = pair_off[e0];
   }
-  cnt[e] = pair_off[e];
+#pragma unroll
+  for (int c = 0; c < LIST_CLASSES; ++c) cnt[e0 + c] = pair_off[e0 + c];
 }
 
 __global__ void k_fill_pairs(const SubTri* __restrict__ S, uint64_t ns, const Dir* __restrict__ dirs,
@@ -343,13 +366,14 @@ __global__ void k_fill_pairs(const SubTri* __restrict__ S, uint64_t ns, const Di
   SubTri s = S[i];
   const int mesh = s.lo.w;
   const Dir d = dirs[mesh];
-  uint32_t* C = cursor + dir_base[mesh];
+  uint32_t* C = cursor + dir_base[mesh] * LIST_CLASSES;
   int lo[3], hi[3];
   if (!brick_range(s, d, lo, hi)) return;
   for (int x = lo[0]; x <= hi[0]; ++x)
     for (int y = lo[1]; y <= hi[1]; ++y)
       for (int z = lo[2]; z <= hi[2]; ++z) {
-        uint32_t p = atomicAdd(&C[(uint64_t(x) * d.dy + y) * d.dz + z], 1u);
+        uint32_t p = atomicAdd(&C[((uint64_t(x) * d.dy + y) * d.dz + z) * LIST_CLASSES +
+                                  pair_class(s, x + d.bx0, y + d.by0, z + d.bz0)], 1u);
         list[p] = uint32_t(i);
       }
 }
@@ -1719,7 +1743,7 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   }
   // count of sub-triangles in 64 bit: nsub sums can wrap in uint32
   check_limit(q_sub, which, K_all, 4294967296.0, "more than 2^32 sub-triangles");
-  check_limit(q_dir, which, K_all, 4294967294.0, "brick directory exceeds 2^32 entries");
+  check_limit(q_dir, which, K_all, 4294967294.0 / LIST_CLASSES, "brick directory exceeds 2^29 entries");
   const uint64_t ns = total;
   if (ns == 0) fail(BS_ERR_EMPTY, "no sub-triangles");
   const uint64_t D = dir_base[K];
@@ -1733,17 +1757,18 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   nsub.reset();
   soff.reset();
 
-  DBuf<uint32_t> cnt(ctx, D + 1), pair_off(ctx, D + 1), flag(ctx, D + 1), bidx(ctx, D + 1);
-  BS_CUDA(cudaMemsetAsync(cnt.p, 0, (D + 1) * sizeof(uint32_t), s));
+  const uint64_t DC = D * LIST_CLASSES;
+  DBuf<uint32_t> cnt(ctx, DC + 1), pair_off(ctx, DC + 1), flag(ctx, D + 1), bidx(ctx, D + 1);
+  BS_CUDA(cudaMemsetAsync(cnt.p, 0, (DC + 1) * sizeof(uint32_t), s));
   BS_KERNEL(ctx, "k_count_pairs", (k_count_pairs<<<blocks(ns, 256), 256, 0, s>>>(S.p, ns, d_dirs.p, d_db.p, cnt.p, st.p)));
-  exclusive_scan(ctx, cnt.p, pair_off.p, D + 1);
-  BS_KERNEL(ctx, "k_dir_flags", (k_dir_flags<<<blocks(D + 1, 256), 256, 0, s>>>(cnt.p, D, flag.p)));
+  exclusive_scan(ctx, cnt.p, pair_off.p, DC + 1);
+  BS_KERNEL(ctx, "k_dir_flags", (k_dir_flags<<<blocks(D + 1, 256), 256, 0, s>>>(pair_off.p, D, flag.p)));
   exclusive_scan(ctx, flag.p, bidx.p, D + 1);
   DBuf<uint32_t> leaf_base(ctx, K + 1), act_base(ctx, K + 1);
   BS_KERNEL(ctx, "k_seg_starts", (k_seg_starts<<<blocks(K + 1, 128), 128, 0, s>>>(bidx.p, d_db.p, K, leaf_base.p)));
   uint32_t nb_np[2];
   read_back(ctx, &nb_np[0], bidx.p + D, sizeof(uint32_t));
-  read_back(ctx, &nb_np[1], pair_off.p + D, sizeof(uint32_t));
+  read_back(ctx, &nb_np[1], pair_off.p + DC, sizeof(uint32_t));
   read_back(ctx, hst.data(), st.p, K * sizeof(M2VStats));
   std::vector<uint64_t> q_pairs(K);
   for (int m = 0; m < K; ++m) {
@@ -1767,7 +1792,7 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   {
     DBuf<uint32_t> list_off(ctx, nb + 1), list(ctx, np);
     BS_KERNEL(ctx, "k_dir_compact", (k_dir_compact<<<blocks(D, 256), 256, 0, s>>>(cnt.p, pair_off.p, bidx.p, D, d_dirs.p, d_db.p, K, origins.p, list_off.p)));
-    BS_CUDA(cudaMemcpyAsync(list_off.p + nb, pair_off.p + D, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+    BS_CUDA(cudaMemcpyAsync(list_off.p + nb, pair_off.p + DC, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
     pair_off.reset();
     bidx.reset();
     BS_KERNEL(ctx, "k_fill_pairs", (k_fill_pairs<<<blocks(ns, 256), 256, 0, s>>>(S.p, ns, d_dirs.p, d_db.p, cnt.p, list.p)));
