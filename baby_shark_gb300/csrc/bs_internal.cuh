@@ -310,50 +310,6 @@ __device__ __forceinline__ float point_triangle_dist2_e(F3 a, F3 b, F3 c, F3 ab,
   return dot3(d, d);
 }
 
-// The same function without branches: every dot product of the chain above
-// is computed, the first region whose test holds (in the chain's order)
-// selects the numerator and denominator of the one division and the base
-// point, edge vectors and parameters of q = (base + e1 s) + e2 t.  Values
-// the chain computes are computed by the same operations in the same order,
-// so the result is bit-identical: vertex and edge regions add e * 0 = +-0,
-// which leaves a coordinate unchanged up to the sign of a zero, and a zero's
-// sign does not survive the square in |q - p|^2.  Lanes of a warp in
-// different regions no longer diverge.
-__device__ __forceinline__ float point_triangle_dist2_flat(F3 a, F3 b, F3 c, F3 ab, F3 ac, F3 cb, F3 p) {
-  const F3 ap = sub3(p, a), bp = sub3(p, b), cp = sub3(p, c);
-  const float d1 = dot3(ab, ap), d2 = dot3(ac, ap);
-  const float d3 = dot3(ab, bp), d4 = dot3(ac, bp);
-  const float d5 = dot3(ab, cp), d6 = dot3(ac, cp);
-  const float vc = fsub(fmul(d1, d4), fmul(d3, d2));
-  const float vb = fsub(fmul(d5, d2), fmul(d1, d6));
-  const float va = fsub(fmul(d3, d6), fmul(d5, d4));
-  const float d43 = fsub(d4, d3), d56 = fsub(d5, d6);
-  const bool r1 = d1 <= 0.0f && d2 <= 0.0f;
-  const bool r2 = !r1 && d3 >= 0.0f && d4 <= d3;
-  const bool n12 = !r1 && !r2;
-  const bool r3 = n12 && vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f;
-  const bool n123 = n12 && !r3;
-  const bool r4 = n123 && d6 >= 0.0f && d5 <= d6;
-  const bool n1234 = n123 && !r4;
-  const bool r5 = n1234 && vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f;
-  const bool r6 = n1234 && !r5 && va <= 0.0f && d43 >= 0.0f && d56 >= 0.0f;
-  const bool r7 = n1234 && !r5 && !r6;
-  // one division: edge parameter or the face's 1 / (va + vb + vc)
-  float num = 0.0f, den = 1.0f;
-  if (r3) { num = d1; den = fsub(d1, d3); }
-  if (r5) { num = d2; den = fsub(d2, d6); }
-  if (r6) { num = d43; den = fadd(d43, d56); }
-  if (r7) { num = 1.0f; den = fadd(fadd(va, vb), vc); }
-  const float t = fdiv(num, den);
-  const F3 base = (r2 || r6) ? b : (r4 ? c : a);
-  const F3 e1 = r5 ? ac : (r6 ? cb : ab);
-  const float s = r7 ? fmul(vb, t) : ((r3 || r5 || r6) ? t : 0.0f);
-  const float w = r7 ? fmul(vc, t) : 0.0f;
-  const F3 q = add3(add3(base, scale3(e1, s)), scale3(ac, w));
-  const F3 d = sub3(q, p);
-  return dot3(d, d);
-}
-
 }  // namespace bs
 
 // Releases the upper-level (internal node) tables of a volume (volume_ops.cu).
