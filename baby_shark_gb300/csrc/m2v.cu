@@ -1254,69 +1254,83 @@ __device__ __forceinline__ float wn_traverse(F3 q, const float4* __restrict__ in
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const float beta2 = beta * beta;
   float sum = 0.f, comp = 0.f;  // Kahan-compensated accumulation
-  int sp = 0;
-  int node = n > 1 ? 0 : ~0;
   bool overflow = false;
   uint32_t c_visit = 0, c_far = 0, c_exact = 0;
-  for (long long guard = 0; guard < 2ll * n + 2; ++guard) {
-    float wv = 0.f;
-    bool have = true;
+
+  // Tests one node (>= 0 internal, < 0 leaf ~index) for the whole warp and
+  // sums its far field or exact solid angle; returns true when the warp has
+  // to open it (an internal node that is near for some lane).
+  auto visit = [&](int node) -> bool {
     ++c_visit;
     if (node >= 0) {
       const float4 P = inode[5 * node];
       const float rx = P.x - q.x, ry = P.y - q.y, rz = P.z - q.z;
       const float r2 = rx * rx + ry * ry + rz * rz;
-      if (__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) {
-        ++c_far;
-        const float4 A = inode[5 * node + 1], B0 = inode[5 * node + 2], B1 = inode[5 * node + 3],
-                     B2 = inode[5 * node + 4];
-        // a.r / (4 pi r^3) + trace(B) / (4 pi r^3) - 3 r^T B r / (4 pi r^5)
-        const float ri = rsqrtf(r2);
-        const float ri2 = ri * ri;
-        const float inv = ri2 * ri * (1.0f / FOUR_PI);
-        const float ar = A.x * rx + A.y * ry + A.z * rz;
-        const float brx = B0.x * rx + B0.y * ry + B0.z * rz;
-        const float bry = B0.w * rx + B1.x * ry + B1.y * rz;
-        const float brz = B1.z * rx + B1.w * ry + B2.x * rz;
-        const float rbr = rx * brx + ry * bry + rz * brz;
-        wv = inv * ((ar + A.w) - 3.0f * ri2 * rbr);
-        if (ORDER >= 3) wv += far3(inode3 + 6 * node, rx, ry, rz, inv, ri2);
-      } else {
-        const float4 E = inode[5 * node + 4];
-        if (sp < WN_STACK) {
-          if (lane == 0) stk[w][sp] = __float_as_int(E.z);
-          ++sp;
-        } else {
-          overflow = true;
-        }
-        node = __float_as_int(E.y);
-        have = false;
-      }
-    } else {
-      const int li = ~node;
-      const float4 P = leaf[5 * li];
-      const float rx = P.x - q.x, ry = P.y - q.y, rz = P.z - q.z;
-      const float r2 = rx * rx + ry * ry + rz * rz;
-      if (__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) {
-        ++c_far;
-        const float4 A = leaf[5 * li + 1];
-        const float ri = rsqrtf(r2);
-        const float inv = ri * ri * ri * (1.0f / FOUR_PI);
-        wv = (A.x * rx + A.y * ry + A.z * rz) * inv;
-        if (ORDER >= 3) wv += far3(leaf3 + 6 * li, rx, ry, rz, inv, ri * ri);
-      } else {
-        ++c_exact;
-        wv = tri_wn(leaf[5 * li + 2], leaf[5 * li + 3], leaf[5 * li + 4], q);
-      }
-    }
-    __syncwarp();
-    if (have) {
+      if (!__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) return true;
+      ++c_far;
+      const float4 A = inode[5 * node + 1], B0 = inode[5 * node + 2], B1 = inode[5 * node + 3],
+                   B2 = inode[5 * node + 4];
+      // a.r / (4 pi r^3) + trace(B) / (4 pi r^3) - 3 r^T B r / (4 pi r^5)
+      const float ri = rsqrtf(r2);
+      const float ri2 = ri * ri;
+      const float inv = ri2 * ri * (1.0f / FOUR_PI);
+      const float ar = A.x * rx + A.y * ry + A.z * rz;
+      const float brx = B0.x * rx + B0.y * ry + B0.z * rz;
+      const float bry = B0.w * rx + B1.x * ry + B1.y * rz;
+      const float brz = B1.z * rx + B1.w * ry + B2.x * rz;
+      const float rbr = rx * brx + ry * bry + rz * brz;
+      float wv = inv * ((ar + A.w) - 3.0f * ri2 * rbr);
+      if (ORDER >= 3) wv += far3(inode3 + 6 * node, rx, ry, rz, inv, ri2);
       kahan(sum, comp, wv);
+      return false;
+    }
+    const int li = ~node;
+    const float4 P = leaf[5 * li];
+    const float rx = P.x - q.x, ry = P.y - q.y, rz = P.z - q.z;
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    float wv;
+    if (__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) {
+      ++c_far;
+      const float4 A = leaf[5 * li + 1];
+      const float ri = rsqrtf(r2);
+      const float inv = ri * ri * ri * (1.0f / FOUR_PI);
+      wv = (A.x * rx + A.y * ry + A.z * rz) * inv;
+      if (ORDER >= 3) wv += far3(leaf3 + 6 * li, rx, ry, rz, inv, ri * ri);
+    } else {
+      ++c_exact;
+      wv = tri_wn(leaf[5 * li + 2], leaf[5 * li + 3], leaf[5 * li + 4], q);
+    }
+    kahan(sum, comp, wv);
+    return false;
+  };
+
+  // Each iteration opens one node: both children are tested and summed in
+  // place; of the children the warp has to open, one is taken next and the
+  // other pushed, so the stack holds at most one pending node per level.
+  int sp = 0;
+  int node = (n > 1) ? (visit(0) ? 0 : -1) : (visit(~0), -1);
+  for (int guard = 0; guard < n + 2; ++guard) {
+    if (node < 0) {
       if (sp == 0) break;
       --sp;
       node = stk[w][sp];
+      __syncwarp();
     }
-    __syncwarp();
+    const float4 E = inode[5 * node + 4];
+    const int c0 = __float_as_int(E.y), c1 = __float_as_int(E.z);
+    const bool o0 = visit(c0), o1 = visit(c1);
+    if (o0 && o1) {
+      if (sp < WN_STACK) {
+        if (lane == 0) stk[w][sp] = c1;
+        ++sp;
+      } else {
+        overflow = true;
+      }
+      __syncwarp();
+      node = c0;
+    } else {
+      node = o0 ? c0 : (o1 ? c1 : -1);
+    }
   }
   if (overflow && lane == 0) atomicExch(&st->error, 3);
   if (lane == 0) {
