@@ -407,10 +407,11 @@ __global__ void k_act_starts(const uint32_t* __restrict__ voff, const uint32_t* 
 // minimum over the surviving pairs equals the minimum over all pairs, bit
 // for bit, whatever the order; a voxel whose minimum is still +inf keeps all
 // its pairs, so the active set is unchanged too.  Lanes take (sub-triangle,
-// y, z) columns of the staged sub-triangles and step along x (the x part of
-// the bound comes from a per-sub-triangle table, the y and z parts once per
-// column); survivors go through a per-warp queue and are evaluated 32 at a
-// time with all lanes busy (the branching closest-point formula measured
+// y, z) columns of the staged sub-triangles and test the column's eight
+// voxels at once (the x part of the bound from a per-sub-triangle table, the
+// y and z parts once per column, the running minima as two float4 loads);
+// survivors go through a per-warp queue and are evaluated 32 at a time with
+// all lanes busy (the branching closest-point formula measured
 // faster here than a branch-free one with a single division).
 constexpr int DIST_THREADS = 128;
 constexpr int DIST_BATCH = 16;  // sub-triangles a warp stages at a time
@@ -422,11 +423,11 @@ struct __align__(16) BatchTri {
   float4 v2;   // ac.z b.x b.y b.z
   float4 v3;   // c.x c.y c.z cb.x
   float4 v4;   // cb.y cb.z rho2 1/nz
-  float4 dxa;  // (1 - 2^-20) dx^2 of the first voxels in x: distance to the bounding box in x
-  float4 dxb;  //   ... voxels 4..7
+  float4 dxa;  // (1 - 2^-20) dx^2 of the brick's voxel columns x = 0..3: distance to the bounding box in x
+  float4 dxb;  //   ... x = 4..7
   float4 yz;   // bounding box lo.y lo.z hi.y hi.z
   int4 box;    // x0 y0 z0 nx: first voxel of (widened box) x (brick) and its x extent
-  int4 box1;   // nz - - -
+  int4 box1;   // nz, mask of the brick x covered by the widened box, - -
 };
 
 // Squared cull margin 17 rho^2 of one sub-triangle (+inf: never cull).
@@ -468,7 +469,9 @@ __global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
     const int4* __restrict__ origins, const uint32_t* __restrict__ list_off, const uint32_t* __restrict__ list,
     const SubTri* __restrict__ S, const MeshInfo* __restrict__ mi, const uint32_t* __restrict__ leaf_base, int K,
     float* __restrict__ values, uint32_t* __restrict__ masks, M2VStats* st) {
-  __shared__ uint32_t dmin[512];
+  // per-voxel running minimum of d^2, x fastest: index (y << 6) | (z << 3) | x,
+  // so a (y, z) column's eight voxels are two float4 loads
+  __shared__ __align__(16) uint32_t dmin[512];
   __shared__ BatchTri bt[DIST_THREADS / 32][DIST_BATCH];
   __shared__ int pre[DIST_THREADS / 32][DIST_BATCH + 1];
   __shared__ uint32_t queue[DIST_THREADS / 32][DIST_QUEUE];
@@ -489,14 +492,13 @@ __global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
   BatchTri* W = bt[warp];
   int* P = pre[warp];
   uint32_t* Q = queue[warp];
-  const uint32_t lt = (1u << lane) - 1u;
   uint32_t n_eval = 0;
 
-  // exact distance of one queued pair (entry = j << 9 | voxel offset)
+  // exact distance of one queued pair (entry = j << 9 | column-major voxel index)
   auto eval = [&](uint32_t ent) {
     const BatchTri& q = W[ent >> 9];
     const int o = int(ent & 511u);
-    const F3 g = f3(gtab[0][o >> 6], gtab[1][(o >> 3) & 7], gtab[2][o & 7]);
+    const F3 g = f3(gtab[0][o & 7], gtab[1][o >> 6], gtab[2][(o >> 3) & 7]);
     const float4 v0 = q.v0, v1 = q.v1, v2 = q.v2, v3 = q.v3, v4 = q.v4;
     const float d2 = point_triangle_dist2_e(f3(v0.x, v0.y, v0.z), f3(v2.y, v2.z, v2.w), f3(v3.x, v3.y, v3.z),
                                             f3(v0.w, v1.x, v1.y), f3(v1.z, v1.w, v2.x), f3(v3.w, v4.x, v4.y), g);
@@ -528,8 +530,8 @@ __global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
         const float lox = fminf(fminf(a.x, bb.x), c.x), hix = fmaxf(fmaxf(a.x, bb.x), c.x);
         float dx[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const float d = box_d(lox, hix, gtab[0][min(x0 - org.x + i, 7)]);
+        for (int i = 0; i < 8; ++i) {  // squared box distance in x of the brick's voxel columns x = org.x + i
+          const float d = box_d(lox, hix, gtab[0][i]);
           dx[i] = fmul(fmul(d, d), CULL_SCALE);
         }
         q.v0 = make_float4(a.x, a.y, a.z, ab.x);
@@ -542,7 +544,7 @@ __global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
         q.yz = make_float4(fminf(fminf(a.y, bb.y), c.y), fminf(fminf(a.z, bb.z), c.z),
                            fmaxf(fmaxf(a.y, bb.y), c.y), fmaxf(fmaxf(a.z, bb.z), c.z));
         q.box = make_int4(x0, y0, z0, nx);
-        q.box1 = make_int4(nz, 0, 0, 0);
+        q.box1 = make_int4(nz, int(((1u << nx) - 1u) << (x0 - org.x)), 0, 0);
         cols = ny * nz;
       }
     }
@@ -559,45 +561,51 @@ __global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
     __syncwarp();
     int j = 0, qn = 0;
     for (int base = 0; base < total; base += 32) {
-      // one lane per (sub-triangle, y, z) column; the column's voxels follow in x
+      // one lane per (sub-triangle, y, z) column: an 8-bit mask of the
+      // column's voxels (x within the brick) that survive the cull test
       const int k = base + lane;
-      int nx = 0, o = 0;
-      float dyz = 0.0f, rho2 = 0.0f;
-      float4 dxa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), dxb = dxa;
+      uint32_t bits = 0, colb = 0;
       if (k < total) {
         while (k >= P[j + 1]) ++j;  // P[DIST_BATCH] = total > k
         const BatchTri& q = W[j];
         const int4 bx = q.box;
+        const int2 b1 = make_int2(q.box1.x, q.box1.y);
         const float4 v4 = q.v4, yz = q.yz;
         const int c = k - P[j];
         // c -> (iy, iz) by reciprocal multiply: c < 64 and nz <= 8 keep the
         // product at least 0.5/8 away from the next integer
-        const int iy = int((float(c) + 0.5f) * v4.w), iz = c - iy * q.box1.x;
+        const int iy = int((float(c) + 0.5f) * v4.w), iz = c - iy * b1.x;
         const int oy = bx.y - org.y + iy, oz = bx.z - org.z + iz;
         const float dy = box_d(yz.x, yz.z, gtab[1][oy]), dz = box_d(yz.y, yz.w, gtab[2][oz]);
-        dyz = fadd(fmul(fmul(dy, dy), CULL_SCALE), fmul(fmul(dz, dz), CULL_SCALE));
-        rho2 = v4.z;
-        dxa = q.dxa;
-        dxb = q.dxb;
-        nx = bx.w;
-        o = ((bx.x - org.x) << 6) | (oy << 3) | oz;
-      }
-      const int steps = __reduce_max_sync(0xffffffffu, nx);
-      const uint32_t jj = uint32_t(j) << 9;
-      const float dxs[8] = {dxa.x, dxa.y, dxa.z, dxa.w, dxb.x, dxb.y, dxb.z, dxb.w};
+        const float dyz = fadd(fmul(fmul(dy, dy), CULL_SCALE), fmul(fmul(dz, dz), CULL_SCALE));
+        const float rho2 = v4.z;
+        const float4 dxa = q.dxa, dxb = q.dxb;
+        colb = uint32_t((oy << 6) | (oz << 3));
+        const float4 ca = *reinterpret_cast<const float4*>(&dmin[colb]);
+        const float4 cc = *reinterpret_cast<const float4*>(&dmin[colb + 4]);
+        const float dxs[8] = {dxa.x, dxa.y, dxa.z, dxa.w, dxb.x, dxb.y, dxb.z, dxb.w};
+        const float cur[8] = {ca.x, ca.y, ca.z, ca.w, cc.x, cc.y, cc.z, cc.w};
 #pragma unroll
-      for (int ix = 0; ix < 8; ++ix) {
-        if (ix < steps) {
-          bool keep = false;
-          if (ix < nx) {
-            const float cur = __uint_as_float(dmin[o + 64 * ix]);
-            keep = !(fadd(dxs[ix], dyz) > fmaf(cur, 1.0625f, rho2));
-          }
-          const uint32_t m = __ballot_sync(0xffffffffu, keep);
-          if (keep) Q[qn + __popc(m & lt)] = jj | uint32_t(o + 64 * ix);
-          qn += __popc(m);
-        }
+        for (int ix = 0; ix < 8; ++ix)
+          bits |= (fadd(dxs[ix], dyz) > fmaf(cur[ix], 1.0625f, rho2)) ? 0u : (1u << ix);
+        bits &= uint32_t(b1.y);  // the voxels of (widened box) x (brick) in this column
       }
+      // survivors to the queue: warp prefix of the per-lane counts
+      const int cnt = __popc(bits);
+      int pos = cnt;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, pos, d);
+        if (lane >= d) pos += v;
+      }
+      const int added = __shfl_sync(0xffffffffu, pos, 31);
+      pos += qn - cnt;
+      while (bits) {
+        const int ix = __ffs(bits) - 1;
+        bits &= bits - 1u;
+        Q[pos++] = (uint32_t(j) << 9) | colb | uint32_t(ix);
+      }
+      qn += added;
       while (qn >= 32) {
         __syncwarp();
         qn -= 32;
@@ -617,8 +625,8 @@ __global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
   if (t == 0 && evaluated) atomicAdd(&st[mesh].n_eval, (unsigned long long)evaluated);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const int o = t + DIST_THREADS * k;
-    const uint32_t u = dmin[o];
+    const int o = t + DIST_THREADS * k;  // (x << 6) | (y << 3) | z
+    const uint32_t u = dmin[((o & 0x38) << 3) | ((o & 7) << 3) | (o >> 6)];
     const float dist = fsqrt(__uint_as_float(u));
     const bool act = dist < __int_as_float(0x7f800000);  // sqrt of a finite square can overflow to inf
     const uint32_t m = __ballot_sync(0xffffffffu, act);
