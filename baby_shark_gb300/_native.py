@@ -40,6 +40,8 @@ SIGNATURES = {
     "bs_ctx_stage_reset": (i32, [vp]),
     "bs_ctx_last_stats": (i32, [vp, C.POINTER(u64)]),
     "bs_ctx_last_counters": (i32, [vp, C.POINTER(u64)]),
+    "bs_ctx_memory": (i32, [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
+    "bs_ctx_memory_reset": (i32, [vp, C.c_int]),
     "bs_diag_fp32_peak": (i32, [vp, C.POINTER(C.c_double)]),
     "bs_winding_numbers_exact": (i32, [vp, vp, u64, vp, u64, vp, u64, vp]),
     "bs_winding_numbers_build": (i32, [vp, vp, u64, vp, u64, i32, PP]),

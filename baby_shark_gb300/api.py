@@ -68,6 +68,15 @@ class Context:
             N.check(self._lib.bs_ctx_stage_reset(self.h), self.h)
         return out
 
+    def memory(self):
+        """Bytes of the context's device pool: in use, peak in use, reserved."""
+        u, hi, r = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        N.check(self._lib.bs_ctx_memory(self.h, C.byref(u), C.byref(hi), C.byref(r)), self.h)
+        return {"used": u.value, "used_high": hi.value, "reserved": r.value}
+
+    def memory_reset(self, trim=False):
+        N.check(self._lib.bs_ctx_memory_reset(self.h, int(bool(trim))), self.h)
+
     def last_stats(self):
         """Counters of the last mesh -> volume, offset, dual contouring or
         winding-number call (bs_ctx_last_counters), named for that call."""

@@ -207,6 +207,31 @@ bs_status bs_ctx_last_counters(const bs_ctx* ctx, uint64_t* out16) {
   return BS_OK;
 }
 
+bs_status bs_ctx_memory(bs_ctx* ctx, uint64_t* used, uint64_t* used_high, uint64_t* reserved) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  return guarded(ctx, [&] {
+    unsigned long long u = 0, hi = 0, r = 0;  // the pool attributes are 64-bit counters
+    BS_CUDA(cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrUsedMemCurrent, &u));
+    BS_CUDA(cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrUsedMemHigh, &hi));
+    BS_CUDA(cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrReservedMemCurrent, &r));
+    if (used) *used = u;
+    if (used_high) *used_high = hi;
+    if (reserved) *reserved = r;
+  });
+}
+
+bs_status bs_ctx_memory_reset(bs_ctx* ctx, int trim) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  return guarded(ctx, [&] {
+    unsigned long long zero = 0;
+    BS_CUDA(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrUsedMemHigh, &zero));
+    if (trim) {
+      BS_CUDA(cudaStreamSynchronize(ctx->stream));
+      BS_CUDA(cudaMemPoolTrimTo(ctx->pool, 0));
+    }
+  });
+}
+
 void bs_m2v_params_default(bs_m2v_params* p) {
   if (!p) return;
   p->voxel_size = 1.0f;   // MeshToVolume::default (mesh_to_volume.rs:223-236)

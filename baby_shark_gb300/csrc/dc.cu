@@ -19,12 +19,11 @@
 #include <cub/device/device_scan.cuh>
 
 #include "bs_internal.cuh"
+#include "dc.cuh"
 #include "leaf_hash.cuh"
 #include "volume_upper.cuh"
 
 namespace bs {
-
-static inline unsigned nbk(uint64_t n, unsigned t) { return unsigned((n + t - 1) / t); }
 
 template <class T>
 static void scan_e(bs_ctx* ctx, const T* in, T* out, size_t n) {
@@ -34,13 +33,6 @@ static void scan_e(bs_ctx* ctx, const T* in, T* out, size_t n) {
   BS_CUDA(cub::DeviceScan::ExclusiveSum(t.p, tmp, in, out, n, ctx->stream));
 }
 
-struct DcVol {
-  const int4* org;
-  const float* val;
-  const uint32_t* msk;
-  LeafHash hash;
-};
-
 // 27 neighbour leaves around a leaf, index (dx+1)*9 + (dy+1)*3 + (dz+1).
 __device__ __forceinline__ void load_neighbours(const DcVol& V, int4 org, int* nb) {
   for (int k = threadIdx.x; k < 27; k += blockDim.x) {
@@ -49,11 +41,14 @@ __device__ __forceinline__ void load_neighbours(const DcVol& V, int4 org, int* n
   }
 }
 
-// Active value at voxel (x, y, z) given relative to the leaf origin, in [-8, 16).
-__device__ __forceinline__ bool at(const DcVol& V, const int* nb, int x, int y, int z, float& v) {
+// Value at voxel (x, y, z) given relative to the leaf origin (in [-8, 16)),
+// as the tree's `at` returns it: an active leaf voxel, or, for a voxel
+// outside every leaf, its active tile's value.  Inactive voxels of a leaf
+// have no value.
+__device__ __forceinline__ bool at(const DcVol& V, const int* nb, int4 org, int x, int y, int z, float& v) {
   const int k = ((x >> 3) + 1) * 9 + ((y >> 3) + 1) * 3 + ((z >> 3) + 1);
   const int l = nb[k];
-  if (l < 0) return false;
+  if (l < 0) return V.tiles.any && tile_value(V.tiles, org.x + x, org.y + y, org.z + z, v);
   const int o = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
   if (!((V.msk[uint64_t(l) * 16 + (o >> 5)] >> (o & 31)) & 1u)) return false;
   v = V.val[uint64_t(l) * 512 + o];
@@ -61,21 +56,18 @@ __device__ __forceinline__ bool at(const DcVol& V, const int* nb, int x, int y, 
 }
 
 // dual_contouring.rs:362-386
-__device__ __forceinline__ bool grad(const DcVol& V, const int* nb, int x, int y, int z, int axis, float& g) {
+__device__ __forceinline__ bool grad(const DcVol& V, const int* nb, int4 org, int x, int y, int z, int axis,
+                                     float& g) {
   const int lx = axis == 0 ? 1 : 0, ly = axis == 1 ? 1 : 0, lz = axis == 2 ? 1 : 0;
   float vp, vl, vr;
-  const bool hp = at(V, nb, x, y, z, vp);
-  const bool hl = at(V, nb, x - lx, y - ly, z - lz, vl);
-  const bool hr = at(V, nb, x + lx, y + ly, z + lz, vr);
+  const bool hp = at(V, nb, org, x, y, z, vp);
+  const bool hl = at(V, nb, org, x - lx, y - ly, z - lz, vl);
+  const bool hr = at(V, nb, org, x + lx, y + ly, z + lz, vr);
   if (hp && hl && hr) { g = fmul(fsub(vr, vl), 0.5f); return true; }
   if (hp && hr) { g = fsub(vr, vp); return true; }
   if (hp && hl) { g = fsub(vp, vl); return true; }
   return false;  // the reference stops with unreachable!() here
 }
-
-struct DcStats {
-  int error;  // 1: gradient with no neighbours, 2: table capacity
-};
 
 // Pass 1a: crossing masks.  cm[l][dir][16]
 __global__ void __launch_bounds__(128) k_dc_edge_mask(DcVol V, uint64_t n, uint32_t* __restrict__ cm,
@@ -93,11 +85,11 @@ __global__ void __launch_bounds__(128) k_dc_edge_mask(DcVol V, uint64_t n, uint3
     const int o = t + 128 * k;
     const int x = o >> 6, y = (o >> 3) & 7, z = o & 7;
     float v1;
-    const bool h1 = at(V, nb, x, y, z, v1);
+    const bool h1 = at(V, nb, org, x, y, z, v1);
 #pragma unroll
     for (int dir = 0; dir < 3; ++dir) {
       float v2;
-      const bool cross = h1 && at(V, nb, x + (dir == 0), y + (dir == 1), z + (dir == 2), v2) &&
+      const bool cross = h1 && at(V, nb, org, x + (dir == 0), y + (dir == 1), z + (dir == 2), v2) &&
                          (signbit(v1) != signbit(v2));
       const uint32_t m = __ballot_sync(0xffffffffu, cross);
       if (lane == 0) {
@@ -139,8 +131,8 @@ __global__ void __launch_bounds__(128) k_dc_edge_points(DcVol V, uint64_t n, con
     const int x = o >> 6, y = (o >> 3) & 7, z = o & 7;
     const int x2 = x + (dir == 0), y2 = y + (dir == 1), z2 = z + (dir == 2);
     float v1, v2;
-    at(V, nb, x, y, z, v1);
-    at(V, nb, x2, y2, z2, v2);
+    at(V, nb, org, x, y, z, v1);
+    at(V, nb, org, x2, y2, z2, v2);
     const float t = (v1 == v2) ? 0.5f : fdiv(v1, fsub(v1, v2));
     float p[3] = {__int2float_rn(org.x + x), __int2float_rn(org.y + y), __int2float_rn(org.z + z)};
     p[dir] = fadd(p[dir], t);
@@ -148,7 +140,7 @@ __global__ void __launch_bounds__(128) k_dc_edge_points(DcVol V, uint64_t n, con
     bool ok = true;
     for (int a = 0; a < 3; ++a) {
       float g1, g2;
-      ok = ok && grad(V, nb, x, y, z, a, g1) && grad(V, nb, x2, y2, z2, a, g2);
+      ok = ok && grad(V, nb, org, x, y, z, a, g1) && grad(V, nb, org, x2, y2, z2, a, g2);
       if (ok) nrm[a] = fadd(fmul(fsub(1.0f, t), g1), fmul(t, g2));
     }
     if (!ok) {
@@ -196,7 +188,7 @@ __global__ void __launch_bounds__(128) k_dc_cell_mask(DcVol V, uint64_t n, uint3
     bool ok = true, any_neg = false, any_pos = false;
     for (int c = 0; c < 8 && ok; ++c) {
       float v;
-      ok = at(V, nb, x + c_cube[c][0], y + c_cube[c][1], z + c_cube[c][2], v);
+      ok = at(V, nb, org, x + c_cube[c][0], y + c_cube[c][1], z + c_cube[c][2], v);
       if (ok) {
         if (signbit(v)) any_neg = true;
         else any_pos = true;
@@ -404,7 +396,7 @@ __device__ __forceinline__ int voxel_tris(const DcVol& V, const int* nb, const u
                         cm[(l * 3 + 2) * 16 + (o >> 5)]) >> (o & 31);
   if (!(any & 1u)) return 0;
   float v1 = 0.f;
-  at(V, nb, x, y, z, v1);
+  v1 = V.val[l * 512 + o];  // active: the voxel has a crossing
   int nt = 0;
   for (int dir = 0; dir < 3; ++dir) {
     if (!((cm[(l * 3 + dir) * 16 + (o >> 5)] >> (o & 31)) & 1u)) continue;
@@ -448,32 +440,60 @@ __device__ __forceinline__ int voxel_tris(const DcVol& V, const int* nb, const u
   return nt;
 }
 
+// Counts (tris == nullptr: vcount[l] = triangles of leaf l) or writes the
+// leaf's triangles from tris + voff[l], voxels in ascending index order.
+// Thread t owns voxels 4t .. 4t+3; a block prefix over the 128 threads
+// places them.
 __global__ void __launch_bounds__(128) k_dc_quads(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
                                                   const uint32_t* __restrict__ cellm, const uint32_t* __restrict__ celloff,
-                                                  const float* __restrict__ cells, float h, uint32_t* __restrict__ vcount,
-                                                  const uint32_t* __restrict__ voff, float* __restrict__ tris) {
+                                                  const float* __restrict__ cells, float h, uint64_t* __restrict__ vcount,
+                                                  const uint64_t* __restrict__ voff, float* __restrict__ tris) {
   __shared__ int nb[27];
+  __shared__ uint32_t wsum[4];
   const uint64_t l = blockIdx.x;
   if (l >= n) return;
   const int4 org = V.org[l];
   load_neighbours(V, org, nb);
   __syncthreads();
-  for (int o = threadIdx.x; o < 512; o += blockDim.x) {
-    const int x = o >> 6, y = (o >> 3) & 7, z = o & 7;
-    if (tris) {
-      voxel_tris(V, nb, cm, cellm, celloff, cells, l, x, y, z, h, tris + uint64_t(voff[l * 512 + o]) * 9);
-    } else {
-      vcount[l * 512 + o] = uint32_t(voxel_tris(V, nb, cm, cellm, celloff, cells, l, x, y, z, h, nullptr));
-    }
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  int c[4];
+  uint32_t mine = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int o = 4 * t + k;
+    c[k] = voxel_tris(V, nb, cm, cellm, celloff, cells, l, o >> 6, (o >> 3) & 7, o & 7, h, nullptr);
+    mine += uint32_t(c[k]);
   }
-  if (!tris && l == n - 1 && threadIdx.x == 0) vcount[n * 512] = 0;
+  // inclusive prefix over the block's threads
+  uint32_t inc = mine;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xffffffffu, inc, d);
+    if (lane >= d) inc += v;
+  }
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  uint32_t before = 0;
+  for (int i = 0; i < w; ++i) before += wsum[i];
+  if (!tris) {
+    if (t == 127) vcount[l] = before + inc;
+    if (l == n - 1 && t == 0) vcount[n] = 0;
+    return;
+  }
+  uint64_t pos = voff[l] + before + inc - mine;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (!c[k]) continue;
+    const int o = 4 * t + k;
+    voxel_tris(V, nb, cm, cellm, celloff, cells, l, o >> 6, (o >> 3) & 7, o & 7, h, tris + pos * 9);
+    pos += uint64_t(c[k]);
+  }
 }
 
 static bool has_active_tiles(const bs_volume* v) { return v->n_tiles != 0; }
 
 void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size, int mode) {
   if (v->dc_valid && v->dc_h == voxel_size && v->dc_mode == mode) return;
-  if (has_active_tiles(v)) fail(BS_ERR_UNSUPPORTED, "dual contouring of a volume with active tiles (the reference stops with todo!())");
   cudaStream_t s = ctx->stream;
   dfree(ctx, v->d_dc_tris);
   v->d_dc_tris = nullptr;
@@ -485,9 +505,20 @@ void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size, int mode) {
     v->dc_mode = mode;
     return;
   }
-  LeafHashBuf hb;
+  LeafHashBuf hb, h1, h2;
   hb.build(ctx, v->d_origins, n, n);
-  DcVol V{v->d_origins, v->d_values, v->d_masks, hb.h};
+  DcVol V{v->d_origins, v->d_values, v->d_masks, hb.h, TileLookup{}};
+  if (has_active_tiles(v)) {
+    // The reference stops at active tiles (todo!(), dual_contouring.rs:139,
+    // 186, 347).  Here the passes still visit the leaves only and read every
+    // neighbour, cell corner and gradient stencil voxel as the tree's `at`
+    // returns it, so a voxel of an active tile has the tile's value.
+    const Upper* u = v->upper;
+    if (!u) fail(BS_ERR_UNSUPPORTED, "dual contouring: tiles without internal levels");
+    h1.build(ctx, u->l1.d_key, u->l1.n, u->l1.n);
+    h2.build(ctx, u->l2.d_key, u->l2.n, u->l2.n);
+    V.tiles = TileLookup{h1.h, h2.h, u->l1.d_state, u->l1.d_tile, u->l2.d_state, u->l2.d_tile, 1};
+  }
   DBuf<DcStats> st(ctx, 1);
   BS_CUDA(cudaMemsetAsync(st.p, 0, sizeof(DcStats), s));
   // 1. crossings
@@ -510,11 +541,11 @@ void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size, int mode) {
   else
     BS_KERNEL(ctx, "k_dc_cell_points", (k_dc_cell_points<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, coff.p, pts.p, cellm.p, celloff.p, cells.p)));
   // 3. quads
-  DBuf<uint32_t> vcnt(ctx, n * 512 + 1), voff(ctx, n * 512 + 1);
+  DBuf<uint64_t> vcnt(ctx, n + 1), voff(ctx, n + 1);
   BS_KERNEL(ctx, "k_dc_quads", (k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, cellm.p, celloff.p, cells.p, voxel_size, vcnt.p, nullptr, nullptr)));
-  scan_e(ctx, vcnt.p, voff.p, n * 512 + 1);
-  uint32_t nt = 0;
-  read_back(ctx, &nt, voff.p + n * 512, sizeof(uint32_t));
+  scan_e(ctx, vcnt.p, voff.p, n + 1);
+  uint64_t nt = 0;
+  read_back(ctx, &nt, voff.p + n, sizeof(uint64_t));
   DcStats hs;
   read_back(ctx, &hs, st.p, sizeof hs);
   if (hs.error == 1)

@@ -24,39 +24,19 @@
 #include <mutex>
 
 #include "bs_internal.cuh"
+#include "dc.cuh"
 #include "leaf_hash.cuh"
 
 namespace bs {
 
-// Declarations of the dual-contouring kernels defined in dc.cu and of the
-// hash fill kernel in offset.cu (same definitions as there).
-struct DcVol {
-  const int4* org;
-  const float* val;
-  const uint32_t* msk;
-  LeafHash hash;
-};
-struct DcStats {
-  int error;
-};
-__global__ void k_dc_edge_mask(DcVol V, uint64_t n, uint32_t* __restrict__ cm, uint32_t* __restrict__ ccount);
-__global__ void k_dc_edge_points(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
-                                 const uint32_t* __restrict__ coff, float* __restrict__ pts, DcStats* st);
-__global__ void k_dc_cell_mask(DcVol V, uint64_t n, uint32_t* __restrict__ cellm, uint32_t* __restrict__ ccount);
-__global__ void k_dc_cell_points(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
-                                 const uint32_t* __restrict__ coff, const float* __restrict__ pts,
-                                 const uint32_t* __restrict__ cellm, const uint32_t* __restrict__ celloff,
-                                 float* __restrict__ cells);
-__global__ void k_dc_quads(DcVol V, uint64_t n, const uint32_t* __restrict__ cm, const uint32_t* __restrict__ cellm,
-                           const uint32_t* __restrict__ celloff, const float* __restrict__ cells, float h,
-                           uint32_t* __restrict__ vcount, const uint32_t* __restrict__ voff, float* __restrict__ tris);
+// Declaration of the hash fill kernel in offset.cu (same definition as there).
 __global__ void k_hash_insert(LeafHash h, const int4* __restrict__ org, uint64_t n, int* __restrict__ err);
 
 }  // namespace bs
 
 namespace {
 
-// Limits of the static working memory (about 24 MiB in use of 32 MiB).
+// Limits of the static working memory (about 16 MiB in use of 32 MiB).
 constexpr uint64_t DCNA_MAX_LEAVES = 2048;       // leaves of the input volume
 constexpr uint64_t DCNA_MAX_CROSSINGS = 393216;  // sign-change edges
 constexpr uint64_t DCNA_MAX_CELLS = 393216;      // cells that get a vertex
@@ -147,8 +127,8 @@ extern "C" bs_status bs_dual_contour_noalloc(int device, void* stream, const int
     uint32_t* cellc = c.take<uint32_t>(n + 1);
     uint32_t* celloff = c.take<uint32_t>(n + 1);
     float* cells = c.take<float>(DCNA_MAX_CELLS * 3);
-    uint32_t* vcnt = c.take<uint32_t>(n * 512 + 1);
-    uint32_t* voff = c.take<uint32_t>(n * 512 + 1);
+    uint64_t* vcnt = c.take<uint64_t>(n + 1);
+    uint64_t* voff = c.take<uint64_t>(n + 1);
     const size_t temp_bytes = 1u << 20;
     void* temp = c.take<unsigned char>(temp_bytes);
     // start empty: hash, error flags
@@ -164,7 +144,7 @@ extern "C" bs_status bs_dual_contour_noalloc(int device, void* stream, const int
     hash.mask = DCNA_HASH_CAP - 1;
     k_hash_insert<<<nblocks(n, 256), 256, 0, s>>>(hash, org, n, herr);
     BS_CUDA(cudaGetLastError());
-    DcVol V{org, d_values, d_masks, hash};
+    DcVol V{org, d_values, d_masks, hash, TileLookup{}};  // the caller's arrays hold leaves only
     k_dc_edge_mask<<<unsigned(n), 128, 0, s>>>(V, n, cm, ccnt);
     BS_CUDA(cudaGetLastError());
     scan_in(s, temp, temp_bytes, ccnt, coff, n * 3 + 1);
@@ -181,8 +161,8 @@ extern "C" bs_status bs_dual_contour_noalloc(int device, void* stream, const int
     BS_CUDA(cudaGetLastError());
     k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm, cellm, celloff, cells, voxel_size, vcnt, nullptr, nullptr);
     BS_CUDA(cudaGetLastError());
-    scan_in(s, temp, temp_bytes, vcnt, voff, n * 512 + 1);
-    const uint32_t nt = read1(s, voff + n * 512);
+    scan_in(s, temp, temp_bytes, vcnt, voff, n + 1);
+    const uint64_t nt = read1(s, voff + n);
     if (read1(s, herr)) return BS_ERR_CAPACITY;
     if (read1(s, st).error == 1) return BS_ERR_UNSUPPORTED;
     *n_tris = nt;

@@ -30,6 +30,7 @@
 
 #include "bs_internal.cuh"
 #include "leaf_hash.cuh"
+#include "tiles.cuh"
 #include "volume_upper.cuh"
 
 namespace bs {
@@ -59,38 +60,9 @@ struct McVol {
 
 // Active tiles of the internal levels: node origin -> node index hashes and
 // the slot tables (state -2 = active tile, value in tile[]).
-struct McTiles {
-  LeafHash h1, h2;
-  const int* s1;
-  const float* t1;
-  const int* s2;
-  const float* t2;
-  int any;
-};
-
-// Value of voxel (x, y, z) from an active tile, for a voxel outside every leaf.
-__device__ __forceinline__ bool tile_value(const McTiles& T, int x, int y, int z, float& v) {
-  if (!T.any) return false;
-  const int n1 = T.h1.find(x & ~127, y & ~127, z & ~127);
-  if (n1 >= 0) {
-    const int slot = (((x >> 3) & 15) << 8) | (((y >> 3) & 15) << 4) | ((z >> 3) & 15);
-    const uint64_t k = uint64_t(n1) * L1_SLOTS + slot;
-    if (T.s1[k] != -2) return false;
-    v = T.t1[k];
-    return true;
-  }
-  const int n2 = T.h2.find(x & ~4095, y & ~4095, z & ~4095);
-  if (n2 < 0) return false;
-  const int slot = (((x >> 7) & 31) << 10) | (((y >> 7) & 31) << 5) | ((z >> 7) & 31);
-  const uint64_t k = uint64_t(n2) * L2_SLOTS + slot;
-  if (T.s2[k] != -2) return false;
-  v = T.t2[k];
-  return true;
-}
-
 // Value of an arbitrary voxel: its leaf decides when it has one (inactive =
 // absent, Grid::at), else an active tile.
-__device__ __forceinline__ float value_at(const McVol& V, const McTiles& T, int x, int y, int z) {
+__device__ __forceinline__ float value_at(const McVol& V, const TileLookup& T, int x, int y, int z) {
   const int l = V.hash.find(x & ~7, y & ~7, z & ~7);
   if (l >= 0) {
     const int o = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
@@ -195,7 +167,7 @@ __device__ __forceinline__ int leaf_cube(const float* W, int x, int y, int z, in
 
 // One warp per leaf.  Pass 1 (tris == nullptr) stores each leaf's triangle
 // count; pass 2 writes them from the leaf's scanned offset.
-__global__ void __launch_bounds__(32 * MC_WARPS) k_mc(McVol V, McTiles T, uint64_t n, float h,
+__global__ void __launch_bounds__(32 * MC_WARPS) k_mc(McVol V, TileLookup T, uint64_t n, float h,
                                                      uint32_t* __restrict__ leaf_count,
                                                      const uint32_t* __restrict__ leaf_off, float* __restrict__ tris) {
   __shared__ float tile[MC_WARPS][T9 * T9 * T9];
@@ -264,7 +236,7 @@ __global__ void __launch_bounds__(32 * MC_WARPS) k_mc(McVol V, McTiles T, uint64
 // Cubes of the tiles' boundary faces (marching_cubes.rs:969-994): for tile
 // t of size s, cube c in [cbase[t], cbase[t + 1]) is face f = r / s^2 of
 // (left, right, top, bottom, front, back) at (i, j) = ((r % s^2) / s, r % s).
-__global__ void k_mc_tiles(McVol V, McTiles T, const int4* __restrict__ tiles, const uint64_t* __restrict__ cbase,
+__global__ void k_mc_tiles(McVol V, TileLookup T, const int4* __restrict__ tiles, const uint64_t* __restrict__ cbase,
                            int n_tiles, uint64_t n_cubes, float h, uint32_t* __restrict__ count,
                            const uint64_t* __restrict__ off, float* __restrict__ tris) {
   const uint64_t c = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
@@ -333,14 +305,14 @@ void marching_cubes_impl(bs_ctx* ctx, bs_volume* v, float voxel_size) {
   LeafHashBuf hb, h1, h2;
   hb.build(ctx, v->d_origins, n, n);
   McVol V{v->d_origins, v->d_values, v->d_masks, hb.h};
-  McTiles T{};
+  TileLookup T{};
   T.any = 0;
   if (ntl) {
     const Upper* u = v->upper;
     if (!u) fail(BS_ERR_UNSUPPORTED, "marching cubes: tiles without internal levels");
     h1.build(ctx, u->l1.d_key, u->l1.n, u->l1.n);
     h2.build(ctx, u->l2.d_key, u->l2.n, u->l2.n);
-    T = McTiles{h1.h, h2.h, u->l1.d_state, u->l1.d_tile, u->l2.d_state, u->l2.d_tile, 1};
+    T = TileLookup{h1.h, h2.h, u->l1.d_state, u->l1.d_tile, u->l2.d_state, u->l2.d_tile, 1};
   }
   // leaves: count, scan, (write below)
   uint32_t nt_leaf = 0;

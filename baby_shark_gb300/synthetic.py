@@ -153,6 +153,37 @@ def uneven_batch(n=256, seed=4):
     return out
 
 
+def random_rotation(rng):
+    """Uniform random rotation matrix (unit quaternion from four normal deviates)."""
+    q = rng.normal(size=4)
+    w, x, y, z = q / np.linalg.norm(q)
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def large_union(n=16, seed=5, tri_min=524288, tri_max=1048576):
+    """Large combined workload: n displaced tori with major radius in
+    [0.5, 1.5], minor radius in [0.1, 0.4], a random rotation, centre in
+    [-1, 1]^3 and tri_min..tri_max triangles each (grid aspect nu / nv = R / r),
+    gradient-noise displacement of amplitude 0.02 r / 0.3.  Returns
+    [(vertices, triangles)]; the defaults give about 12 M triangles."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        R = float(rng.uniform(0.5, 1.5))
+        r = float(rng.uniform(0.1, 0.4))
+        target = float(rng.uniform(tri_min, tri_max))
+        nv = max(8, int(round((target / 2.0 * r / R) ** 0.5)))
+        nu = max(8, int(round(target / 2.0 / nv)))
+        rot = random_rotation(rng)
+        centre = rng.uniform(-1.0, 1.0, size=3)
+        v, f = torus(R, r, nu, nv, 0.02 * r / 0.3, seed=seed * 1000 + k)
+        v = (v.astype(np.float64) @ rot.T + centre).astype(np.float32)
+        out.append((v, f))
+    return out
+
+
 def open_icosphere(subdiv=9, amplitude=0.1, octaves=4, remove=0.1, seed=3):
     """Non-watertight workload: subdivision-9 icosphere (5,242,880 triangles),
     4-octave radial noise of amplitude 0.1, 10 % of faces removed."""

@@ -521,6 +521,100 @@ def order3_secondary(ctx, params, dev, L, N, bs, C, args):
             "sign_differences_vs_reference_parameters": diff, "band_voxels": int(band)}
 
 
+def run_large_union(args):
+    """The large combined workload: the union of 16 displaced tori
+    (synthetic.large_union: major radius 0.5-1.5, minor 0.1-0.4, random
+    rotation and centre in [-1, 1]^3, about 12 M triangles), voxel 0.0005,
+    band 3.  All tori go to SDF + sign in one batched call with the meshes
+    resident in HBM, the 16 volumes are united pairwise, and the union is
+    dual-contoured (triangles counted on the device, not copied out).
+    Reports band voxels/s of the conversion, the union and dual-contouring
+    times, output triangles/s and the peak device memory of the library's
+    pool (the whole run has to stay within 180 GB)."""
+    import ctypes as C
+
+    import torch
+
+    import baby_shark_gb300 as bs
+    from baby_shark_gb300 import _native as N
+    from baby_shark_gb300 import build as bs_build
+    from baby_shark_gb300 import synthetic
+
+    bs_build.build()
+    L = N.load()
+    ctx = bs.Context(0)
+    t_gen = time.perf_counter()
+    meshes = synthetic.large_union()
+    t_gen = time.perf_counter() - t_gen
+    h = 0.0005
+    K = len(meshes)
+    xyz = torch.from_numpy(np.concatenate([v for v, _ in meshes])).cuda()
+    tri = torch.from_numpy(np.concatenate([f for _, f in meshes]).astype(np.int32)).cuda()
+    nv = np.array([len(v) for v, _ in meshes], np.uint64)
+    nt = np.array([len(f) for _, f in meshes], np.uint64)
+    P = (N.M2VParams * K)()
+    for k in range(K):
+        L.bs_m2v_params_default(C.byref(P[k]))
+        P[k].voxel_size = h
+        P[k].band_width = BAND
+    torch.cuda.synchronize()
+
+    def once():
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        outs = (C.c_void_p * K)()
+        N.check(L.bs_mesh_to_volume_batch_device(ctx.h, K, xyz.data_ptr(), nv.ctypes.data, tri.data_ptr(),
+                                                 nt.ctypes.data, P, outs), ctx.h)
+        vols = [bs.Volume(C.c_void_p(outs[k]), ctx) for k in range(K)]
+        ctx.synchronize()
+        t1 = time.perf_counter()
+        band = sum(v.counts()["active_voxels"] for v in vols)
+        leaves_in = sum(v.counts()["leaves"] for v in vols)
+        ctx.synchronize()
+        t1b = time.perf_counter()
+        while len(vols) > 1:
+            nxt = [vols[i].union(vols[i + 1]) for i in range(0, len(vols) - 1, 2)]
+            if len(vols) % 2:
+                nxt.append(vols[-1])
+            vols = nxt
+        u = vols[0]
+        ctx.synchronize()
+        t2 = time.perf_counter()
+        n_tris = C.c_uint64()
+        N.check(L.bs_dual_contour(ctx.h, u.h, C.c_float(h), None, 0, C.byref(n_tris)), ctx.h)
+        ctx.synchronize()
+        t3 = time.perf_counter()
+        cu = u.counts()
+        return {"convert_s": t1 - t0, "union_s": t2 - t1b, "dc_s": t3 - t2, "band_voxels": int(band),
+                "leaves_in": int(leaves_in), "union_leaves": int(cu["leaves"]), "union_tiles": int(cu["tiles"]),
+                "union_active_voxels": int(cu["active_voxels"]), "dc_triangles": int(n_tris.value)}
+
+    for _ in range(args.warmup):
+        once()
+    ctx.memory_reset(trim=True)
+    runs = [once() for _ in range(max(1, args.steps))]
+    mem = ctx.memory()
+    best = min(runs, key=lambda r: r["convert_s"] + r["union_s"] + r["dc_s"])
+    line = {"metric": "band voxels/s mesh->SDF+sign (batched, 16 tori) and output triangles/s",
+            "value": best["band_voxels"] / best["convert_s"], "unit": UNIT, "n_gpus": 1,
+            "steps": len(runs), "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "union of 16 displaced tori (synthetic.large_union, %d triangles), "
+                                   "voxel 0.0005, band 3: batched mesh->SDF+sign, pairwise union, dual contouring"
+                                   % int(nt.sum()),
+                       "parallelism": "single GPU"},
+            "convert_ms": best["convert_s"] * 1e3, "union_ms": best["union_s"] * 1e3,
+            "dc_ms": best["dc_s"] * 1e3,
+            "dc_triangles_per_s": best["dc_triangles"] / best["dc_s"] if best["dc_s"] else None,
+            "pipeline_ms": (best["convert_s"] + best["union_s"] + best["dc_s"]) * 1e3,
+            "counts": {k: best[k] for k in ("band_voxels", "leaves_in", "union_leaves", "union_tiles",
+                                            "union_active_voxels", "dc_triangles")},
+            "device_memory_gb": {"peak_in_use": mem["used_high"] / 1e9, "reserved": mem["reserved"] / 1e9,
+                                 "budget": 180.0},
+            "generation_s": t_gen}
+    print(json.dumps(line), flush=True)
+
+
 def batch_secondary(ctx, L, N, bs, C, n_meshes, reps=3):
     """The uneven-batch workload (synthetic.uneven_batch: icospheres and
     displaced tori, 1k-500k triangles, grids 64^3-512^3, band 3), resident in
@@ -679,7 +773,7 @@ def main():
                     help="skip the order-3 / accuracy-scale-1.5 sign-pass comparison")
     ap.add_argument("--batch-meshes", type=int, default=256,
                     help="meshes of the uneven-batch comparison (0 skips it)")
-    ap.add_argument("--workload", default="tori", choices=["tori", "open-icosphere"],
+    ap.add_argument("--workload", default="tori", choices=["tori", "open-icosphere", "large-union"],
                     help="tori: the boolean workload's two tori (the headline line); open-icosphere: the "
                          "non-watertight subdivision-9 icosphere with an exact-sign check")
     ap.add_argument("--wn-order", type=int, default=2, choices=[2, 3],
@@ -697,6 +791,8 @@ def main():
         run_reference(args)
     elif args.workload == "open-icosphere":
         run_open(args)
+    elif args.workload == "large-union":
+        run_large_union(args)
     else:
         run_ours(args)
 

@@ -41,7 +41,7 @@ typedef enum bs_status {
   BS_ERR_CAPACITY = 4,     /* a grid or table bound was exceeded */
   BS_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
   BS_ERR_CUDA = 6,         /* CUDA runtime error (see bs_ctx_last_error) */
-  BS_ERR_UNSUPPORTED = 7,  /* input the reference panics on (e.g. tiles in DC) */
+  BS_ERR_UNSUPPORTED = 7,  /* input the reference panics on (e.g. a gradient with no neighbours in DC) */
   BS_ERR_NO_DEVICE = 8     /* no CUDA device / driver */
 } bs_status;
 
@@ -93,6 +93,13 @@ enum bs_stats_kind {
   BS_STATS_WINDING_NUMBERS = 4
 };
 bs_status bs_ctx_last_counters(const bs_ctx* ctx, uint64_t* out16);
+/* Device memory of the context's stream-ordered pool in bytes: in use now,
+ * the most in use since creation or the last reset, and reserved from the
+ * device (freed blocks stay reserved for reuse).  No reference counterpart. */
+bs_status bs_ctx_memory(bs_ctx* ctx, uint64_t* used, uint64_t* used_high, uint64_t* reserved);
+/* Resets the high-water mark of bs_ctx_memory; with trim != 0 also returns
+ * the pool's unused reserved memory to the device. */
+bs_status bs_ctx_memory_reset(bs_ctx* ctx, int trim);
 /* Measured FP32 FMA throughput of the context's device in TFLOP/s (a timed
  * FFMA loop over all SMs); the denominator of FP32-bound roofline fractions. */
 bs_status bs_diag_fp32_peak(bs_ctx* ctx, double* tflops);
@@ -235,8 +242,11 @@ bs_status bs_marching_cubes(bs_ctx* ctx, bs_volume* v, float voxel_size, float* 
  * Writes up to `capacity` triangles (9 floats each, world units) to h_tris and
  * the total count to *n_tris; call with capacity 0 to size the buffer (the
  * extraction is cached on the volume, so the second call only copies).
- * Volumes holding active tiles give BS_ERR_UNSUPPORTED, where the reference
- * stops with todo!() (dual_contouring.rs:139). */
+ * Active tiles (after booleans): the reference stops with todo!()
+ * (dual_contouring.rs:139, 186, 347); here the passes visit the leaves and
+ * read every neighbour, cell corner and gradient voxel as the tree's `at`
+ * returns it (internal_node/tree_node.rs:34-42), so a voxel of an active tile
+ * carries the tile's value — a uniform tile adds no cells of its own. */
 bs_status bs_dual_contour(bs_ctx* ctx, bs_volume* v, float voxel_size, float* h_tris,
                           uint64_t capacity, uint64_t* n_tris);
 

@@ -61,7 +61,7 @@ def lib():
                 "orc_volume_intersect": (C.c_int, [vp, vp]),
                 "orc_volume_flood_fill": (C.c_int, [vp]),
                 "orc_volume_offset": (C.c_int, [vp, f32]),
-                "orc_dual_contour": (i64, [vp, f32, vp, i64, vp, vp, vp]),
+                "orc_dual_contour": (i64, [vp, f32, vp, i64, vp, vp, vp, C.c_int]),
                 "orc_mc_count": (i64, [vp, vp, vp]),
                 "orc_marching_cubes": (i64, [vp, f32, vp, i64]),
                 "orc_subtriangles": (i64, [f32p, i64, u32p, i64, f32, i64, vp, vp, i64]),
@@ -149,12 +149,15 @@ class OracleVolume:
             raise RuntimeError("oracle offset met a tile")
         return self
 
-    def dual_contour(self):
+    def dual_contour(self, tiles_via_at=False):
+        """Triangles, status, crossings, cells.  tiles_via_at: read active
+        tiles through Grid::at instead of stopping (status 1) at them."""
         st = C.c_int(0)
         ne, nc = C.c_int64(0), C.c_int64(0)
-        n = lib().orc_dual_contour(self.h, self.voxel_size, None, 0, C.byref(st), C.byref(ne), C.byref(nc))
+        f = int(bool(tiles_via_at))
+        n = lib().orc_dual_contour(self.h, self.voxel_size, None, 0, C.byref(st), C.byref(ne), C.byref(nc), f)
         out = np.zeros((max(n, 1), 9), np.float32)
-        lib().orc_dual_contour(self.h, self.voxel_size, _ptr(out), n, C.byref(st), None, None)
+        lib().orc_dual_contour(self.h, self.voxel_size, _ptr(out), n, C.byref(st), None, None, f)
         return out[:n].reshape(n, 3, 3), st.value, ne.value, nc.value
 
     def marching_cubes(self, voxel_size=None):

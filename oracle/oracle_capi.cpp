@@ -211,9 +211,11 @@ int orc_volume_offset(void* v, float d) {
 // out (9 floats each) when out_cap is large enough, else the required count.
 // *status: 0 ok, 1 active tile (the reference panics), 2 gradient without
 // neighbours (the reference panics).
+// tiles_via_at: 0 stops at active tiles as the reference does, 1 reads them
+// through Grid::at (the GPU's extension).
 int64_t orc_dual_contour(void* v, float voxel_size, float* out, int64_t out_cap, int* status,
-                         int64_t* n_edges, int64_t* n_cells) {
-  DcResult r = dual_contour(*static_cast<Volume*>(v)->grid, voxel_size);
+                         int64_t* n_edges, int64_t* n_cells, int tiles_via_at) {
+  DcResult r = dual_contour(*static_cast<Volume*>(v)->grid, voxel_size, tiles_via_at != 0);
   if (status) *status = r.status;
   if (n_edges) *n_edges = int64_t(r.n_edges);
   if (n_cells) *n_cells = int64_t(r.n_cells);

@@ -66,14 +66,19 @@ inline uint64_t pack3(int64_t x, int64_t y, int64_t z) {
   return (uint64_t(x + (1 << 20)) << 42) | (uint64_t(y + (1 << 20)) << 21) | uint64_t(z + (1 << 20));
 }
 
-// dual_contouring.rs:23-91 (face order: leaves in tree order, voxels x-y-z)
-inline DcResult dual_contour(const Grid& g, float voxel_size) {
+// dual_contouring.rs:23-91 (face order: leaves in tree order, voxels x-y-z).
+// The reference stops at an active tile (todo!(), dual_contouring.rs:139,
+// 186, 347): status 1.  With tiles_via_at the passes still visit the leaves
+// only and read every neighbour through Grid::at, which returns an active
+// tile's value for a voxel outside the leaves — the extension the GPU
+// implements for volumes with tiles.
+inline DcResult dual_contour(const Grid& g, float voxel_size, bool tiles_via_at = false) {
   DcResult res;
   bool tile = false;
   std::vector<const Leaf3*> leaves;
   g.visit_leafs([&](const Leaf3& l) { leaves.push_back(&l); },
                 [&](I3, int, float) { tile = true; });
-  if (tile) { res.status = 1; return res; }
+  if (tile && !tiles_via_at) { res.status = 1; return res; }
   std::unordered_map<uint64_t, IntPoint> ints[3];
   auto grad = [&](I3 p, int axis, float& out) -> bool {
     I3 pl = p, pr = p;

@@ -59,8 +59,10 @@ def test_offset_then_dc():
     assert_same_mesh(g, o, 0.012)
 
 
-def test_dc_rejects_tiles():
-    """Active tiles: the reference stops with todo!() (dual_contouring.rs:139)."""
+def test_dc_union_with_tiles_matches_oracle_extension():
+    """Active tiles: the reference stops with todo!() (dual_contouring.rs:139);
+    both the oracle (tiles_via_at) and the GPU read tile voxels through the
+    tree's `at` and give the same triangles, bit for bit."""
     va, fa = synthetic.icosphere(3, 0.6, 0.02, seed=11)
     vb, fb = synthetic.icosphere(3, 0.5, 0.02, seed=12)
     vb = vb + np.array([0.45, 0.1, -0.05], np.float32)
@@ -69,9 +71,16 @@ def test_dc_rejects_tiles():
     b = bs.MeshToVolume(ctx).with_voxel_size(0.02).with_narrow_band_width(3).convert((vb, fb))
     u = a.union(b)
     assert u.counts()["tiles"] > 0
-    with pytest.raises(bs.BsError) as e:
-        bs.DualContouringMesher().with_voxel_size(0.02).mesh(u)
-    assert e.value.status == 7
+    oa, _, _ = ob.mesh_to_volume(va, fa, 0.02, 3)
+    obb, _, _ = ob.mesh_to_volume(vb, fb, 0.02, 3)
+    ou = oa.union(obb)
+    _, status, _, _ = ou.dual_contour()
+    assert status == 1  # the reference's behaviour
+    ot, status, _, _ = ou.dual_contour(tiles_via_at=True)
+    assert status == 0
+    gt = bs.DualContouringMesher().with_voxel_size(0.02).mesh(u)
+    assert gt.shape == ot.shape and len(gt) > 1000
+    assert np.array_equal(tri_multiset(gt), tri_multiset(ot))
 
 
 def test_corner_table_from_dc_matches_oracle_builder():
