@@ -5,7 +5,7 @@ signs, SDF booleans and offset, dual-contouring extraction.
 The compute lives in libbs_gb300.so (csrc/, C ABI in include/baby_shark_gb300.h);
 this package is the host-side mirror of the reference's builder API.
 """
-from .api import (Context, CornerTable, DualContouringMesher, MarchingCubesMesher, MeshToVolume,  # noqa: F401
-                  Volume, VolumeBuilder, VoxelRemesher, WindingNumbers, convert_batch, default_context,
-                  winding_numbers_exact)
+from .api import (Context, CornerTable, DualContouringMesher, LearnedFarField, MarchingCubesMesher,  # noqa: F401
+                  MeshToVolume, Volume, VolumeBuilder, VoxelRemesher, WindingNumbers, convert_batch,
+                  default_context, winding_numbers_exact)
 from ._native import BsError  # noqa: F401

@@ -40,6 +40,15 @@ SIGNATURES = {
     "bs_ctx_stage_reset": (i32, [vp]),
     "bs_ctx_last_stats": (i32, [vp, C.POINTER(u64)]),
     "bs_ctx_last_counters": (i32, [vp, C.POINTER(u64)]),
+    "bs_mlp_num_params": (i32, []),
+    "bs_mlp_create": (i32, [vp, vp, f32, vp, vp, C.POINTER(vp)]),
+    "bs_mlp_free": (i32, [vp]),
+    "bs_mlp_get_params": (i32, [vp, vp, vp]),
+    "bs_mlp_predict": (i32, [vp, vp, vp, u64, vp]),
+    "bs_mlp_train": (i32, [vp, vp, vp, vp, u64, C.c_uint32, C.c_uint32, f32, f32, vp]),
+    "bs_mlp_gradients": (i32, [vp, vp, vp, vp, u64, C.c_uint32, vp, vp]),
+    "bs_mlp_classify": (i32, [vp, vp, vp, vp, vp, u64, f32, f32, f32, vp, C.POINTER(u64)]),
+    "bs_volume_band_flags": (i32, [vp, vp, vp, u64, vp]),
     "bs_ctx_memory": (i32, [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
     "bs_ctx_memory_reset": (i32, [vp, C.c_int]),
     "bs_diag_fp32_peak": (i32, [vp, C.POINTER(C.c_double)]),

@@ -376,6 +376,190 @@ class WindingNumbers:
         return out.cpu().numpy()
 
 
+class LearnedFarField:
+    """Learned far field (no reference counterpart; the reference evaluates
+    winding numbers only at band voxels, mesh_to_volume.rs:245-280): a small
+    per-mesh network trained on the GPU (bs_mlp_*) on winding numbers that
+    the tree traversal computes at sampled points, 70 % uniform in the padded
+    bounding box and 30 % near the surface.  It answers only points outside
+    the narrow band of a volume of the mesh (by default voxel 1/200 of the
+    largest extent, band 3): classify() takes the network's value there when
+    it lies more than the calibrated margin from the sign threshold, and the
+    traversal's everywhere else.  The margin is the smallest one under which
+    no calibration point outside the band (a separate sample) gets the other
+    side of the threshold than the traversal gives it, times a safety factor.
+    `timings` holds the seconds spent on the tree, the band, sampling, labels,
+    training and calibration; comparisons against the plain traversal count
+    them all."""
+
+    def __init__(self):
+        self.h = None
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            try:
+                N.load().bs_mlp_free(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+    @staticmethod
+    def sample(vertices, faces, n, seed, near_fraction=0.3, sigma=0.02, pad=0.1):
+        """Sample points as a CUDA tensor (n, 3): uniform in the box padded by
+        `pad` of its extent, and near the surface (area-weighted triangle
+        points moved along the normal by N(0, sigma times the largest
+        extent)), in random order."""
+        import torch
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(int(seed))
+        v = torch.as_tensor(np.ascontiguousarray(vertices, np.float32)).cuda()
+        f = torch.as_tensor(np.ascontiguousarray(faces, np.int64)).cuda()
+        lo, hi = v.min(dim=0).values, v.max(dim=0).values
+        ext = hi - lo
+        n_near = int(n * near_fraction)
+        uni = lo - pad * ext + torch.rand(n - n_near, 3, generator=gen, device=v.device) * (ext * (1 + 2 * pad))
+        a, b, c = v[f[:, 0]], v[f[:, 1]], v[f[:, 2]]
+        cr = torch.cross(b - a, c - a, dim=1)
+        area = cr.norm(dim=1)
+        idx = torch.multinomial(area, n_near, replacement=True, generator=gen)
+        r1 = torch.rand(n_near, generator=gen, device=v.device)
+        r2 = torch.rand(n_near, generator=gen, device=v.device)
+        sq = r1.sqrt()
+        pts = ((1 - sq)[:, None] * a[idx] + (sq * (1 - r2))[:, None] * b[idx] + (sq * r2)[:, None] * c[idx])
+        nrm = cr[idx] / area[idx].clamp_min(1e-30)[:, None]
+        pts = pts + nrm * (torch.randn(n_near, 1, generator=gen, device=v.device) * (sigma * float(ext.max())))
+        out = torch.cat([uni, pts])
+        return out[torch.randperm(n, generator=gen, device=v.device)].contiguous()
+
+    @classmethod
+    def train(cls, mesh, ctx=None, tree=None, band=None, n_samples=2_000_000, n_calibration=262_144, epochs=16,
+              batch=8192, lr=3e-3, lr_min=1e-4, beta=2.0, thresh=0.2, order=2, max_frequency=16.0, seed=0,
+              safety=1.25, band_voxel=None, band_width=3):
+        import time
+
+        import torch
+        ctx = ctx or default_context()
+        v, f = _mesh_arrays(mesh)
+        rng = np.random.default_rng(seed)
+        self = cls()
+        self.ctx = ctx
+        self.beta = float(beta)
+        self.thresh = float(thresh)
+        L = N.load()
+
+        def sync():
+            ctx.synchronize()
+            torch.cuda.synchronize()
+
+        lo, hi = v.min(axis=0), v.max(axis=0)
+        extent = float((hi - lo).max())
+        t0 = time.perf_counter()
+        self.tree = tree if tree is not None else WindingNumbers.from_mesh((v, f), order=order, ctx=ctx)
+        sync()
+        t1 = time.perf_counter()
+        if band is None:
+            hb = band_voxel if band_voxel is not None else extent / 200.0
+            band = MeshToVolume(ctx).with_voxel_size(hb).with_narrow_band_width(band_width).convert((v, f))
+        self.band = band
+        sync()
+        t2 = time.perf_counter()
+        dp = cls.sample(v, f, n_samples, seed)
+        dc = cls.sample(v, f, n_calibration, seed + 1)
+        sync()
+        t3 = time.perf_counter()
+        lab = torch.empty(len(dp), dtype=torch.float32, device=dp.device)
+        clab = torch.empty(len(dc), dtype=torch.float32, device=dp.device)
+        N.check(L.bs_winding_numbers_approximate(ctx.h, self.tree.h, dp.data_ptr(), len(dp), self.beta,
+                                                 lab.data_ptr()), ctx.h)
+        N.check(L.bs_winding_numbers_approximate(ctx.h, self.tree.h, dc.data_ptr(), len(dc), self.beta,
+                                                 clab.data_ptr()), ctx.h)
+        sync()
+        t4 = time.perf_counter()
+        centre = ((lo + hi) * 0.5).astype(np.float32)
+        scale = np.float32(1.0 / (0.55 * extent))
+        dirs = rng.normal(size=(32, 3))
+        dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+        mags = np.exp(np.linspace(0.0, np.log(max_frequency), 32))
+        self.freq = np.ascontiguousarray(dirs * mags[:, None], np.float32)
+        p = np.zeros(L.bs_mlp_num_params(), np.float32)
+        lim = np.sqrt(6.0 / 128.0)
+        p[0:4096] = rng.uniform(-lim, lim, 4096)
+        p[4160:8256] = rng.uniform(-lim, lim, 4096)
+        p[8320:8384] = rng.uniform(-0.1, 0.1, 64)
+        p[8384] = float(lab.mean().item())
+        self.centre, self.scale = centre, float(scale)
+        h = C.c_void_p()
+        N.check(L.bs_mlp_create(ctx.h, centre.ctypes.data, float(scale), self.freq.ctypes.data, p.ctypes.data,
+                                C.byref(h)), ctx.h)
+        self.h = h
+        loss = np.zeros(epochs, np.float32)
+        N.check(L.bs_mlp_train(ctx.h, self.h, dp.data_ptr(), lab.data_ptr(), len(dp), int(batch), int(epochs),
+                               float(lr), float(lr_min), loss.ctypes.data), ctx.h)
+        self.epoch_loss = loss
+        sync()
+        t5 = time.perf_counter()
+        pred = torch.empty(len(dc), dtype=torch.float32, device=dp.device)
+        N.check(L.bs_mlp_predict(ctx.h, self.h, dc.data_ptr(), len(dc), pred.data_ptr()), ctx.h)
+        inb = self.band_flags(dc)
+        pr, cl = pred.cpu().numpy(), clab.cpu().numpy()
+        out = inb == 0
+        wrong = out & ((pr > self.thresh) != (cl > self.thresh))
+        worst = float(np.abs(pr[wrong] - self.thresh).max()) if wrong.any() else 0.0
+        self.margin = safety * worst + 0.01
+        self.calibration = {"points": len(dc), "outside_band": int(out.sum()), "wrong_side": int(wrong.sum()),
+                            "worst_wrong_margin": worst,
+                            "answered_fraction": float(np.mean(out & (np.abs(pr - self.thresh) > self.margin))),
+                            "mean_abs_error_outside_band": float(np.mean(np.abs(pr - cl)[out]))}
+        sync()
+        t6 = time.perf_counter()
+        self.timings = {"tree_s": t1 - t0, "band_s": t2 - t1, "sampling_s": t3 - t2, "labels_s": t4 - t3,
+                        "training_s": t5 - t4, "calibration_s": t6 - t5}
+        self.timings["total_s"] = sum(self.timings.values())
+        return self
+
+    def band_flags(self, points):
+        """1 where a point's nearest grid point is in the band volume's active set."""
+        import torch
+        p = points if isinstance(points, torch.Tensor) else torch.from_numpy(
+            np.ascontiguousarray(points, np.float32).reshape(-1, 3)).cuda()
+        out = torch.empty(p.shape[0], dtype=torch.int32, device=p.device)
+        torch.cuda.synchronize()
+        N.check(N.load().bs_volume_band_flags(self.ctx.h, self.band.h, p.data_ptr(), p.shape[0], out.data_ptr()),
+                self.ctx.h)
+        return out.cpu().numpy()
+
+    def params(self):
+        out = np.zeros(N.load().bs_mlp_num_params(), np.float32)
+        N.check(N.load().bs_mlp_get_params(self.ctx.h, self.h, out.ctypes.data), self.ctx.h)
+        return out
+
+    def predict(self, points):
+        """Network predictions (float32 numpy array) at an (n, 3) array or CUDA tensor of points."""
+        import torch
+        p = points if isinstance(points, torch.Tensor) else torch.from_numpy(
+            np.ascontiguousarray(points, np.float32).reshape(-1, 3)).cuda()
+        out = torch.empty(p.shape[0], dtype=torch.float32, device=p.device)
+        torch.cuda.synchronize()
+        N.check(N.load().bs_mlp_predict(self.ctx.h, self.h, p.data_ptr(), p.shape[0], out.data_ptr()), self.ctx.h)
+        return out.cpu().numpy()
+
+    def classify(self, points):
+        """Winding numbers at the points (numpy array or CUDA tensor): the
+        network's where the point is outside the band and the prediction is
+        confident, the traversal's elsewhere.  Returns (CUDA tensor of
+        values, number of points that went to the traversal)."""
+        import torch
+        p = points if isinstance(points, torch.Tensor) else torch.from_numpy(
+            np.ascontiguousarray(points, np.float32).reshape(-1, 3)).cuda()
+        out = torch.empty(p.shape[0], dtype=torch.float32, device=p.device)
+        nt = C.c_uint64()
+        torch.cuda.synchronize()
+        N.check(N.load().bs_mlp_classify(self.ctx.h, self.h, self.tree.h, self.band.h, p.data_ptr(), p.shape[0],
+                                         self.thresh, float(self.margin), self.beta, out.data_ptr(), C.byref(nt)),
+                self.ctx.h)
+        return out, int(nt.value)
+
+
 def winding_numbers_exact(vertices, triangles, points, ctx=None):
     """Exact generalised winding numbers (float64) of `points` w.r.t. a mesh by
     direct summation on the GPU (bs_winding_numbers_exact).  Arguments are

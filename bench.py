@@ -521,6 +521,94 @@ def order3_secondary(ctx, params, dev, L, N, bs, C, args):
             "sign_differences_vs_reference_parameters": diff, "band_voxels": int(band)}
 
 
+def run_learned(args):
+    """The learned far field on the non-watertight workload (subdivision-9
+    icosphere, 4.7 M triangles, 4-octave noise 0.1, 10 % of faces removed):
+    winding numbers (signs at the 0.2 threshold) of a query set of points
+    uniform in the padded bounding box.  Plain = the tree traversal (the
+    reference's order-2 far field, accuracy scale 2) for every point;
+    learned = train a network (band volume, sampling, traversal labels,
+    training, calibration: all timed) and answer the points outside the band
+    whose prediction is confident from the network, the rest from the same
+    traversal.  Both include the tree build.  Reports both times, the share
+    of points the network answered, sign differences between the two, and
+    signs of a seeded sample against exact winding numbers."""
+    import torch
+
+    import baby_shark_gb300 as bs
+    from baby_shark_gb300 import build as bs_build
+    from baby_shark_gb300 import synthetic
+
+    bs_build.build()
+    ctx = bs.Context(0)
+    v, f = synthetic.open_icosphere()
+    n_q = args.queries
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(12345)
+    lo = torch.from_numpy(v.min(axis=0)).cuda()
+    hi = torch.from_numpy(v.max(axis=0)).cuda()
+    ext = hi - lo
+    q = (lo - 0.1 * ext + torch.rand(n_q, 3, generator=gen, device="cuda") * (1.2 * ext)).contiguous()
+    torch.cuda.synchronize()
+
+    def plain():
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        tree = bs.WindingNumbers.from_mesh((v, f), order=2, ctx=ctx)
+        out = torch.empty(n_q, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        bs_native = bs._native
+        bs_native.check(bs_native.load().bs_winding_numbers_approximate(ctx.h, tree.h, q.data_ptr(), n_q, 2.0,
+                                                                        out.data_ptr()), ctx.h)
+        ctx.synchronize()
+        return time.perf_counter() - t0, out
+
+    def learned():
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        lf = bs.LearnedFarField.train((v, f), ctx=ctx, seed=1)
+        t1 = time.perf_counter()
+        out, n_trav = lf.classify(q)
+        ctx.synchronize()
+        return time.perf_counter() - t0, time.perf_counter() - t1, out, n_trav, lf
+
+    for _ in range(max(1, args.warmup)):
+        plain()
+        learned()
+    tp, wp = min((plain() for _ in range(max(1, args.steps))), key=lambda r: r[0])
+    runs = [learned() for _ in range(max(1, args.steps))]
+    tl, tq, wl, n_trav, lf = min(runs, key=lambda r: r[0])
+    diff = int((wp > 0.2).ne(wl > 0.2).sum().item())
+    # exact check on a seeded sample
+    idx = torch.randperm(n_q, generator=gen, device="cuda")[:args.validation]
+    exact = bs.winding_numbers_exact(v, f, q[idx], ctx=ctx)
+    ex = (exact > 0.2).cpu().numpy()
+    mism_plain = int(np.sum(ex != (wp[idx] > 0.2).cpu().numpy()))
+    mism_learned = int(np.sum(ex != (wl[idx] > 0.2).cpu().numpy()))
+    answered = 1.0 - n_trav / n_q
+    # tensor-core work of the network (forward 2 (64 x 64 + 64 x 64 + 64) FLOP a sample, training about 3x)
+    fwd_flop = 2 * (64 * 64 + 64 * 64 + 64)
+    train_samples = 2_000_000 * 16
+    line = {"metric": "winding numbers / s of points in the padded box (learned far field vs traversal)",
+            "value": n_q / tl, "unit": "points/s", "n_gpus": 1, "steps": len(runs), "warmup": args.warmup,
+            "higher_is_better": True, "dtype": "bf16 network, f32 traversal", "data": "synthetic",
+            "config": {"workload": "subdivision-9 icosphere, 4-octave noise 0.1, 10 %% of faces removed (%d "
+                                   "triangles); %d query points uniform in the box padded by 10 %%" % (len(f), n_q),
+                       "parallelism": "single GPU"},
+            "plain_s": tp, "plain_points_per_s": n_q / tp,
+            "learned_s": tl, "learned_over_plain": tp / tl,
+            "learned_breakdown_s": dict(lf.timings, classify_s=tq),
+            "network_answered_fraction": answered,
+            "sign_differences_learned_vs_plain": diff,
+            "validation": {"points": int(args.validation), "plain_vs_exact": mism_plain,
+                           "learned_vs_exact": mism_learned},
+            "calibration": lf.calibration, "margin": lf.margin,
+            "epoch_loss": [float(x) for x in lf.epoch_loss],
+            "network_tflops": {"training": 3 * fwd_flop * train_samples / lf.timings["training_s"] / 1e12,
+                               "inference_in_classify": fwd_flop * n_q / tq / 1e12}}
+    print(json.dumps(line), flush=True)
+
+
 def run_large_union(args):
     """The large combined workload: the union of 16 displaced tori
     (synthetic.large_union: major radius 0.5-1.5, minor 0.1-0.4, random
@@ -773,13 +861,15 @@ def main():
                     help="skip the order-3 / accuracy-scale-1.5 sign-pass comparison")
     ap.add_argument("--batch-meshes", type=int, default=256,
                     help="meshes of the uneven-batch comparison (0 skips it)")
-    ap.add_argument("--workload", default="tori", choices=["tori", "open-icosphere", "large-union"],
+    ap.add_argument("--workload", default="tori", choices=["tori", "open-icosphere", "large-union", "learned"],
                     help="tori: the boolean workload's two tori (the headline line); open-icosphere: the "
                          "non-watertight subdivision-9 icosphere with an exact-sign check")
     ap.add_argument("--wn-order", type=int, default=2, choices=[2, 3],
                     help="far-field order of the sign pass for --workload open-icosphere (2 = the reference's)")
     ap.add_argument("--wn-beta", type=float, default=2.0,
                     help="accuracy scale of the sign pass for --workload open-icosphere (2 = the reference's)")
+    ap.add_argument("--queries", type=int, default=16_000_000,
+                    help="query points of --workload learned")
     ap.add_argument("--validation", type=int, default=200000,
                     help="band voxels checked against exact winding numbers (open-icosphere)")
     ap.add_argument("--pipeline-only", action="store_true",
@@ -793,6 +883,8 @@ def main():
         run_open(args)
     elif args.workload == "large-union":
         run_large_union(args)
+    elif args.workload == "learned":
+        run_learned(args)
     else:
         run_ours(args)
 

@@ -193,6 +193,45 @@ bs_status bs_winding_numbers_approximate(bs_ctx* ctx, const bs_wn_tree* tree, co
                                          float beta, float* d_out);
 bs_status bs_winding_numbers_free(bs_wn_tree* tree);
 
+/* ------------------------------------------------ learned far field ---- */
+/* A per-mesh network that predicts the winding number at a point (no
+ * reference counterpart: the reference evaluates winding numbers only at band
+ * voxels, mesh_to_volume.rs:245-280).  x -> (x - centre) * scale -> 64 Fourier
+ * features [sin(pi f_k . x_n), cos(pi f_k . x_n)] of 32 frequency vectors ->
+ * Linear 64x64 + SiLU -> Linear 64x64 + SiLU -> Linear 64x1, BF16 tensor-core
+ * kernels with FP32 accumulation.  Parameters (bs_mlp_num_params() floats):
+ * W1[in][out] (4096), b1 (64), W2[in][out] (4096), b2 (64), w3 (64), b3. */
+typedef struct bs_mlp bs_mlp;
+int bs_mlp_num_params(void);
+/* centre[3], scale > 0, h_freq[32*3], h_params[num_params] (host). */
+bs_status bs_mlp_create(bs_ctx* ctx, const float* centre, float scale, const float* h_freq, const float* h_params,
+                        bs_mlp** out);
+bs_status bs_mlp_free(bs_mlp* net);
+bs_status bs_mlp_get_params(bs_ctx* ctx, const bs_mlp* net, float* h_params);
+/* Predictions at n device points into d_out (device). */
+bs_status bs_mlp_predict(bs_ctx* ctx, const bs_mlp* net, const float* d_points, uint64_t n, float* d_out);
+/* Adam training on mean squared error: epochs over floor(n / batch)
+ * minibatches of the device arrays in their order (batch a multiple of 512),
+ * cosine learning rate lr_max -> lr_min; each step is replayed from one
+ * captured CUDA graph.  h_epoch_loss (optional, epochs floats): mean loss. */
+bs_status bs_mlp_train(bs_ctx* ctx, bs_mlp* net, const float* d_points, const float* d_targets, uint64_t n,
+                       uint32_t batch, uint32_t epochs, float lr_max, float lr_min, float* h_epoch_loss);
+/* Gradient (h_grad, num_params floats) and loss of the first `batch` samples,
+ * without an update (gradient checks). */
+bs_status bs_mlp_gradients(bs_ctx* ctx, bs_mlp* net, const float* d_points, const float* d_targets, uint64_t n,
+                           uint32_t batch, float* h_grad, float* h_loss);
+/* Winding numbers of n device points into d_out: the prediction for points
+ * outside the narrow band of `band` (a volume of the mesh; null: no band)
+ * whose prediction is more than `margin` from `thresh`, the tree traversal
+ * with accuracy scale beta (bs_winding_numbers_approximate) for every other
+ * point; *n_traversed counts the latter. */
+bs_status bs_mlp_classify(bs_ctx* ctx, const bs_mlp* net, const bs_wn_tree* tree, const bs_volume* band,
+                          const float* d_points, uint64_t n, float thresh, float margin, float beta, float* d_out,
+                          uint64_t* n_traversed);
+/* d_flags[i] = 1 when the grid point nearest to device point i is an active
+ * voxel of the volume (inside its narrow band), else 0. */
+bs_status bs_volume_band_flags(bs_ctx* ctx, const bs_volume* v, const float* d_points, uint64_t n, uint32_t* d_flags);
+
 /* ------------------------------------------- from_fn / VolumeBuilder ---- */
 /* Volume::from_fn (volume/mod.rs:40-72) over values the caller sampled: the
  * grid points (idx_min + (i, j, k)) * voxel_size for i < dims[0], j < dims[1],

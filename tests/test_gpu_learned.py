@@ -1,0 +1,93 @@
+"""The learned far field (bs_mlp_*; no reference counterpart): the GPU's
+BF16 tensor-core forward pass and gradients against the numpy restatement,
+training that lowers the loss, and classification whose network-answered
+points (outside the band, confident) carry no sign mismatch against exact
+winding numbers and at most a rare difference from the traversal."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import baby_shark_gb300 as bs
+from baby_shark_gb300 import _native as N
+from baby_shark_gb300 import synthetic
+from oracle import mlp_ref
+from tests.gpu_common import context
+
+pytestmark = pytest.mark.gpu
+
+
+def random_net(rng, ctx):
+    L = N.load()
+    p = np.zeros(L.bs_mlp_num_params(), np.float32)
+    p[:] = rng.normal(0.0, 0.15, size=p.shape)
+    freq = (rng.normal(size=(32, 3)) * 3.0).astype(np.float32)
+    centre = np.array([0.1, -0.2, 0.05], np.float32)
+    h = C.c_void_p()
+    N.check(L.bs_mlp_create(ctx.h, centre.ctypes.data, 0.8, freq.ctypes.data, p.ctypes.data, C.byref(h)), ctx.h)
+    return h, p, freq, centre, np.float32(0.8)
+
+
+def test_forward_and_gradients_match_numpy():
+    import torch
+    ctx = context()
+    L = N.load()
+    rng = np.random.default_rng(7)
+    h, p, freq, centre, scale = random_net(rng, ctx)
+    try:
+        n = 2048
+        pts = rng.uniform(-1.5, 1.5, size=(n, 3)).astype(np.float32)
+        tgt = rng.uniform(0.0, 1.0, size=n).astype(np.float32)
+        dp = torch.from_numpy(pts).cuda()
+        dt = torch.from_numpy(tgt).cuda()
+        out = torch.empty(n, dtype=torch.float32, device=dp.device)
+        torch.cuda.synchronize()
+        N.check(L.bs_mlp_predict(ctx.h, h, dp.data_ptr(), n, out.data_ptr()), ctx.h)
+        y_ref, _ = mlp_ref.forward(p, freq, centre, scale, pts)
+        y = out.cpu().numpy()
+        assert np.max(np.abs(y - y_ref)) < 2e-2 * max(1.0, np.max(np.abs(y_ref)))
+        g = np.zeros(L.bs_mlp_num_params(), np.float32)
+        loss = np.zeros(1, np.float32)
+        N.check(L.bs_mlp_gradients(ctx.h, h, dp.data_ptr(), dt.data_ptr(), n, n, g.ctypes.data, loss.ctypes.data),
+                ctx.h)
+        l_ref, g_ref = mlp_ref.gradients(p, freq, centre, scale, pts, tgt)
+        assert abs(loss[0] - l_ref) < 1e-2 * l_ref
+        blocks = {"W1": (0, 4096), "b1": (4096, 4160), "W2": (4160, 8256), "b2": (8256, 8320), "w3": (8320, 8384),
+                  "b3": (8384, 8385)}
+        for name, (a, b) in blocks.items():
+            err = np.linalg.norm(g[a:b] - g_ref[a:b]) / max(np.linalg.norm(g_ref[a:b]), 1e-12)
+            assert err < 2e-2, (name, err)
+    finally:
+        L.bs_mlp_free(h)
+
+
+def small_open_mesh():
+    v, f = synthetic.icosphere(4, 0.8, 0.05, seed=21)
+    return v, synthetic.remove_faces(f, 0.1, seed=22)
+
+
+def test_training_lowers_loss_and_classification_keeps_signs():
+    import torch
+    ctx = context()
+    v, f = small_open_mesh()
+    lf = bs.LearnedFarField.train((v, f), ctx=ctx, n_samples=524288, n_calibration=131072, epochs=16, batch=4096,
+                                  seed=3)
+    loss = lf.epoch_loss
+    assert loss[-1] < 0.5 * loss[0], loss
+    val = bs.LearnedFarField.sample(v, f, 100000, seed=11)
+    wn, n_trav = lf.classify(val)
+    wn = wn.cpu().numpy()
+    plain = lf.tree.approximate(val.cpu().numpy(), lf.beta)
+    # the calibrated margin keeps the network on the traversal's side of the
+    # threshold for all but a rare point (calibration is on a finite sample)
+    assert np.sum((wn > 0.2) != (plain > 0.2)) <= 1e-4 * len(wn)
+    # which points the network answered: outside the band and confident
+    pred = lf.predict(val)
+    answered = (lf.band_flags(val) == 0) & (np.abs(pred - 0.2) > lf.margin)
+    assert n_trav == int((~answered).sum())
+    assert np.array_equal(wn[answered], pred[answered])
+    # network-answered points: 0 sign mismatches against exact winding numbers
+    exact = bs.winding_numbers_exact(v, f, val[torch.from_numpy(answered).cuda()], ctx=ctx).cpu().numpy()
+    assert np.array_equal(pred[answered] > 0.2, exact > 0.2)
+    # the network answers a good part of the uniform-plus-near-surface sample
+    assert answered.mean() > 0.3, (answered.mean(), lf.calibration, lf.margin)
