@@ -400,9 +400,9 @@ __global__ void k_act_starts(const uint32_t* __restrict__ voff, const uint32_t* 
 //
 // Pairs that cannot lower the voxel's minimum are culled before the exact
 // point-triangle distance is evaluated: a pair is dropped when the distance
-// from the voxel to the sub-triangle's bounding box, less a per-triangle
-// bound rho on how far the float32 closest point of the reference's formula
-// can stray from the triangle, already exceeds the voxel's running minimum.
+// from the voxel to the sub-triangle's bounding box, less a bound on how far
+// the float32 closest point of the reference's formula can stray from the
+// triangle (cull_coeffs), already exceeds the voxel's running minimum.
 // The running minimum is a value some evaluated pair produced, so the
 // minimum over the surviving pairs equals the minimum over all pairs, bit
 // for bit, whatever the order; a voxel whose minimum is still +inf keeps all
@@ -422,43 +422,50 @@ struct __align__(16) BatchTri {
   float4 v1;   // ab.y ab.z ac.x ac.y
   float4 v2;   // ac.z b.x b.y b.z
   float4 v3;   // c.x c.y c.z cb.x
-  float4 v4;   // cb.y cb.z rho2 1/nz
+  float4 v4;   // cb.y cb.z c2 1/nz (cull coefficient, see cull_coeffs)
   float4 dxa;  // (1 - 2^-20) dx^2 of the brick's voxel columns x = 0..3: distance to the bounding box in x
   float4 dxb;  //   ... x = 4..7
   float4 yz;   // bounding box lo.y lo.z hi.y hi.z
   int4 box;    // x0 y0 z0 nx: first voxel of (widened box) x (brick) and its x extent
-  int4 box1;   // nz, mask of the brick x covered by the widened box, - -
+  int4 box1;   // nz, mask of the brick x covered by the widened box, bits of E0, -
 };
 
-// Squared cull margin 17 rho^2 of one sub-triangle (+inf: never cull).
-// In the reference's closest-point formula (Ericson, point_triangle_dist2)
-// the vertex cases return a vertex exactly and the edge cases a parameter in
-// [0, 1] (their denominators add two numbers of one sign), so there the
-// float32 closest point leaves the triangle only by rounding: 16 u (e + R)
-// + 4 u M with u = 2^-24, e the longest edge, R a bound on |p - vertex| and M
-// on |coordinates|.  The face case divides by va + vb + vc, whose exact value
-// is |ab x ac|^2 and whose float32 error is at most about 70 u e^2 R^2 (the
-// six dot products carry 5 u e R each); the parameters then move by at most
-// about 93 u e^2 R^2 / (|ab x ac|^2 / 4) and the point by 188 u e^3 R^2 /
-// |ab x ac|^2, bounded here by 1024 u e^3 R^2 / |ab x ac|^2 =: eps_face.
-// Sub-triangles where that perturbation is not small (eps_face > e) are never
-// culled.  rho = 2 eps also covers the rounding of the final |q - p|^2.  The
-// cull test lb' > cur * 17/16 + 17 rho^2, with lb' the float32 sum of the
-// squared box distances each scaled by 1 - 2^-20 (so lb' < lb (1 - 8 u)),
-// implies sqrt(lb) > sqrt(cur) + rho (2 rho sqrt(cur) <= cur / 16 + 16 rho^2),
-// so a culled pair's float32 distance is above cur.
-__device__ __forceinline__ float cull_margin2(F3 ab, F3 ac, F3 cb, float R, float M) {
+// Cull coefficients of one sub-triangle.  In the reference's closest-point
+// formula (Ericson, point_triangle_dist2) the vertex cases return a vertex
+// exactly and the edge cases a parameter in [0, 1] (their denominators add
+// two numbers of one sign), so there the float32 closest point leaves the
+// triangle only by rounding.  The face case divides by va + vb + vc, whose
+// exact value is |ab x ac|^2 and whose float32 error is at most about
+// 70 u e^2 R_p^2 (u = 2^-24, e the longest edge, R_p the largest distance
+// from the voxel p to a vertex: the six dot products carry 5 u e R_p each);
+// the parameters then move by at most about 93 u e^2 R_p^2 / (|ab x ac|^2 / 4)
+// and the point by 188 u e^3 R_p^2 / |ab x ac|^2, bounded here by
+// c (d + e)^2 with c = 1024 u e^3 / |ab x ac|^2, since every vertex is within
+// d + e of p for d the exact distance.  With the rounding of the vertex,
+// edge and final |q - p| terms (19 u (d + e) + 16 u e + 4 u M, M a bound on
+// |coordinates|) the float32 distance is at least d - eps(d), and
+// eps(sqrt(lb)) <= c2 lb + E0 for c2 = 2 c and E0 = 2 c e^2 + 19 u (R + e)
+// + 16 u e + 4 u M, R the widened box diagonal.  The cull test
+// lb' > cur * 33/32 + 33 t^2 with t = c2 lb' + E0 (lb' the float32 sum of the
+// squared box distances each scaled by 1 - 2^-20, so lb' < lb (1 - 8 u))
+// implies sqrt(lb) - t > sqrt(cur) (2 t sqrt(cur) <= cur / 32 + 32 t^2), so a
+// culled pair's float32 distance is above cur.  Conditions checked here:
+// the perturbation is small (c R^2 <= e), d - eps(d) increases on [0, R]
+// (c (R + e) <= 1/4), and the right side grows slower than lb
+// (132 c (c2 R^2 + E0) <= 1/2); a sub-triangle that fails one (every
+// degenerate one does) is never culled (c2 = +inf).
+__device__ __forceinline__ void cull_coeffs(F3 ab, F3 ac, F3 cb, float R, float M, float& c2, float& E0) {
   const float u = 5.9604645e-8f;
   const float e2 = fmaxf(dot3(ab, ab), fmaxf(dot3(ac, ac), dot3(cb, cb)));
   const float e = sqrtf(e2);
   const F3 n = cross3(ab, ac);
   const float a2sq = dot3(n, n);
-  const float face = 1024.0f * u * (e2 * e * R * R / a2sq);  // +inf or NaN for a degenerate triangle
-  if (!(face <= e)) return __int_as_float(0x7f800000);
-  const float eps = face + 16.0f * u * (e + R) + 4.0f * u * M;
-  const float rho = 2.0f * eps;
-  const float r2 = 17.0f * rho * rho;
-  return r2 == r2 ? r2 : __int_as_float(0x7f800000);
+  const float c = 1024.0f * u * (e2 * e / a2sq);  // +inf or NaN for a degenerate triangle
+  const float e0 = 2.0f * c * e2 + 19.0f * u * (R + e) + 16.0f * u * e + 4.0f * u * M;
+  const bool ok = c * R * R <= e && c * (R + e) <= 0.25f && 132.0f * c * (2.0f * c * R * R + e0) <= 0.5f &&
+                  e0 < __int_as_float(0x7f800000);
+  c2 = ok ? 2.0f * c : __int_as_float(0x7f800000);
+  E0 = ok ? e0 : 0.0f;
 }
 
 constexpr float CULL_SCALE = 1.0f - 0x1p-20f;
@@ -538,13 +545,15 @@ __global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
         q.v1 = make_float4(ab.y, ab.z, ac.x, ac.y);
         q.v2 = make_float4(ac.z, bb.x, bb.y, bb.z);
         q.v3 = make_float4(c.x, c.y, c.z, cb.x);
-        q.v4 = make_float4(cb.y, cb.z, cull_margin2(ab, ac, cb, R, M), 1.0f / float(nz));
+        float c2, e0;
+        cull_coeffs(ab, ac, cb, R, M, c2, e0);
+        q.v4 = make_float4(cb.y, cb.z, c2, 1.0f / float(nz));
         q.dxa = make_float4(dx[0], dx[1], dx[2], dx[3]);
         q.dxb = make_float4(dx[4], dx[5], dx[6], dx[7]);
         q.yz = make_float4(fminf(fminf(a.y, bb.y), c.y), fminf(fminf(a.z, bb.z), c.z),
                            fmaxf(fmaxf(a.y, bb.y), c.y), fmaxf(fmaxf(a.z, bb.z), c.z));
         q.box = make_int4(x0, y0, z0, nx);
-        q.box1 = make_int4(nz, int(((1u << nx) - 1u) << (x0 - org.x)), 0, 0);
+        q.box1 = make_int4(nz, int(((1u << nx) - 1u) << (x0 - org.x)), __float_as_int(e0), 0);
         cols = ny * nz;
       }
     }
@@ -569,7 +578,7 @@ __global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
         while (k >= P[j + 1]) ++j;  // P[DIST_BATCH] = total > k
         const BatchTri& q = W[j];
         const int4 bx = q.box;
-        const int2 b1 = make_int2(q.box1.x, q.box1.y);
+        const int4 b1 = q.box1;
         const float4 v4 = q.v4, yz = q.yz;
         const int c = k - P[j];
         // c -> (iy, iz) by reciprocal multiply: c < 64 and nz <= 8 keep the
@@ -578,7 +587,7 @@ __global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
         const int oy = bx.y - org.y + iy, oz = bx.z - org.z + iz;
         const float dy = box_d(yz.x, yz.z, gtab[1][oy]), dz = box_d(yz.y, yz.w, gtab[2][oz]);
         const float dyz = fadd(fmul(fmul(dy, dy), CULL_SCALE), fmul(fmul(dz, dz), CULL_SCALE));
-        const float rho2 = v4.z;
+        const float c2 = v4.z, e0 = __int_as_float(b1.z);
         const float4 dxa = q.dxa, dxb = q.dxb;
         colb = uint32_t((oy << 6) | (oz << 3));
         const float4 ca = *reinterpret_cast<const float4*>(&dmin[colb]);
@@ -586,8 +595,11 @@ __global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
         const float dxs[8] = {dxa.x, dxa.y, dxa.z, dxa.w, dxb.x, dxb.y, dxb.z, dxb.w};
         const float cur[8] = {ca.x, ca.y, ca.z, ca.w, cc.x, cc.y, cc.z, cc.w};
 #pragma unroll
-        for (int ix = 0; ix < 8; ++ix)
-          bits |= (fadd(dxs[ix], dyz) > fmaf(cur[ix], 1.0625f, rho2)) ? 0u : (1u << ix);
+        for (int ix = 0; ix < 8; ++ix) {
+          const float lb = fadd(dxs[ix], dyz);
+          const float tt = fmaf(c2, lb, e0);
+          bits |= (lb > fmaf(cur[ix], 1.03125f, 33.0f * (tt * tt))) ? 0u : (1u << ix);
+        }
         bits &= uint32_t(b1.y);  // the voxels of (widened box) x (brick) in this column
       }
       // survivors to the queue: warp prefix of the per-lane counts
