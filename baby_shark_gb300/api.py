@@ -68,6 +68,30 @@ class Context:
             N.check(self._lib.bs_ctx_stage_reset(self.h), self.h)
         return out
 
+    def autotune(self, mesh, voxel_size, band_width):
+        """bs_autotune_mesh_to_volume on a mesh ((vertices, faces) numpy
+        arrays): keeps the fastest launch shapes for this context and
+        returns them with the per-candidate times."""
+        import torch
+        v, f = _mesh_arrays(mesh)
+        dv = torch.from_numpy(v).cuda()
+        df = torch.from_numpy(f.astype(np.int32)).cuda()
+        torch.cuda.synchronize()
+        P = N.M2VParams()
+        self._lib.bs_m2v_params_default(C.byref(P))
+        P.voxel_size = float(voxel_size)
+        P.band_width = int(band_width)
+        ch = (C.c_int32 * 2)()
+        ms = (C.c_float * 6)()
+        N.check(self._lib.bs_autotune_mesh_to_volume(self.h, dv.data_ptr(), len(v), df.data_ptr(), len(f),
+                                                     C.byref(P), ch, ms), self.h)
+        return {"dist_threads": ch[0], "wn_warps": ch[1],
+                "distance_ms": {64: ms[0], 128: ms[1], 256: ms[2]},
+                "sign_ms": {2: ms[3], 4: ms[4], 8: ms[5]}}
+
+    def set_launch_shape(self, dist_threads=0, wn_warps=0):
+        N.check(self._lib.bs_ctx_set_launch_shape(self.h, int(dist_threads), int(wn_warps)), self.h)
+
     def memory(self):
         """Bytes of the context's device pool: in use, peak in use, reserved."""
         u, hi, r = C.c_uint64(), C.c_uint64(), C.c_uint64()

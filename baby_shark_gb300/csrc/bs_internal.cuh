@@ -37,6 +37,11 @@ struct bs_ctx {
     uint64_t launches = 0;
   };
   std::map<std::string, Stage> stages;
+  // launch shapes chosen by bs_autotune_mesh_to_volume: threads per brick of
+  // the distance pass (64, 128, 256) and warps per block of the sign pass
+  // (2, 4, 8)
+  int tune_dist_threads = 128;
+  int tune_wn_warps = 4;
   // counters of the last mesh -> volume, offset or dual contouring call
   // (see bs_ctx_last_counters); [8] names the call that wrote them
   uint64_t last_stats[16] = {};
@@ -47,6 +52,8 @@ struct bs_ctx {
 
 // Drops one reference; the context is torn down with the last one.
 void bs_ctx_release(bs_ctx* ctx);
+// Folds the recorded per-kernel event pairs into ctx->stages.
+extern "C" void bs_ctx_resolve_stages(bs_ctx* ctx);
 
 namespace bs {
 

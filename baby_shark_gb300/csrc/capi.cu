@@ -155,7 +155,7 @@ bs_status bs_ctx_set_stage_timing(bs_ctx* ctx, int enable) {
   return BS_OK;
 }
 
-static void resolve_stages(bs_ctx* ctx) {
+void bs_ctx_resolve_stages(bs_ctx* ctx) {
   for (auto& p : ctx->pending) {
     float ms = 0.f;
     BS_CUDA(cudaEventSynchronize(p.b));
@@ -172,7 +172,7 @@ static void resolve_stages(bs_ctx* ctx) {
 bs_status bs_ctx_stage_count(bs_ctx* ctx, int* n) {
   if (!ctx || !n) return BS_ERR_INVALID_ARG;
   return guarded(ctx, [&] {
-    resolve_stages(ctx);
+    bs_ctx_resolve_stages(ctx);
     *n = int(ctx->stages.size());
   });
 }
@@ -190,7 +190,7 @@ bs_status bs_ctx_stage_info(bs_ctx* ctx, int i, const char** name, double* total
 bs_status bs_ctx_stage_reset(bs_ctx* ctx) {
   if (!ctx) return BS_ERR_INVALID_ARG;
   return guarded(ctx, [&] {
-    resolve_stages(ctx);
+    bs_ctx_resolve_stages(ctx);
     ctx->stages.clear();
   });
 }

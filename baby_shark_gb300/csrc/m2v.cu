@@ -413,7 +413,8 @@ __global__ void k_act_starts(const uint32_t* __restrict__ voff, const uint32_t* 
 // survivors go through a per-warp queue and are evaluated 32 at a time with
 // all lanes busy (the branching closest-point formula measured
 // faster here than a branch-free one with a single division).
-constexpr int DIST_THREADS = 128;
+// Threads per brick of the distance pass: 64, 128 or 256 (bs_autotune_mesh_to_volume
+// picks one per context; 128 by default).
 constexpr int DIST_BATCH = 16;  // sub-triangles a warp stages at a time
 constexpr int DIST_QUEUE = 32 + 8 * 32;  // < 32 left over + one column walk of 8 steps x 32 lanes
 
@@ -472,23 +473,24 @@ constexpr float CULL_SCALE = 1.0f - 0x1p-20f;
 
 __device__ __forceinline__ float box_d(float lo, float hi, float g) { return fmaxf(fmaxf(lo - g, g - hi), 0.0f); }
 
-__global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_brick_distance(
     const int4* __restrict__ origins, const uint32_t* __restrict__ list_off, const uint32_t* __restrict__ list,
     const SubTri* __restrict__ S, const MeshInfo* __restrict__ mi, const uint32_t* __restrict__ leaf_base, int K,
     float* __restrict__ values, uint32_t* __restrict__ masks, M2VStats* st) {
   // per-voxel running minimum of d^2, x fastest: index (y << 6) | (z << 3) | x,
   // so a (y, z) column's eight voxels are two float4 loads
   __shared__ __align__(16) uint32_t dmin[512];
-  __shared__ BatchTri bt[DIST_THREADS / 32][DIST_BATCH];
-  __shared__ int pre[DIST_THREADS / 32][DIST_BATCH + 1];
-  __shared__ uint32_t queue[DIST_THREADS / 32][DIST_QUEUE];
+  __shared__ BatchTri bt[THREADS / 32][DIST_BATCH];
+  __shared__ int pre[THREADS / 32][DIST_BATCH + 1];
+  __shared__ uint32_t queue[THREADS / 32][DIST_QUEUE];
   __shared__ float gtab[3][8];  // grid coordinates x * h of the brick's voxels, per axis
   __shared__ uint32_t evaluated;
   const int b = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int4 org = origins[b];
   const int mesh = find_seg(leaf_base, K, uint64_t(b));
   const float h = mi[mesh].h;
-  for (int o = t; o < 512; o += DIST_THREADS) dmin[o] = 0x7f800000u;  // +inf
+  for (int o = t; o < 512; o += THREADS) dmin[o] = 0x7f800000u;  // +inf
   if (t < 24) {
     const int ax = t >> 3, i = t & 7;
     gtab[ax][i] = fmul(__int2float_rn((ax == 0 ? org.x : ax == 1 ? org.y : org.z) + i), h);
@@ -513,7 +515,7 @@ __global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
       atomicMin(&dmin[o], __float_as_uint(d2));
   };
 
-  for (uint32_t e0 = beg + warp * DIST_BATCH; e0 < end; e0 += (DIST_THREADS / 32) * DIST_BATCH) {
+  for (uint32_t e0 = beg + warp * DIST_BATCH; e0 < end; e0 += (THREADS / 32) * DIST_BATCH) {
     // lanes 0..BATCH-1: stage one sub-triangle each and count its (y, z)
     // columns of voxels in this brick
     int cols = 0;
@@ -636,14 +638,14 @@ __global__ void __launch_bounds__(DIST_THREADS, 8) k_brick_distance(
   __syncthreads();
   if (t == 0 && evaluated) atomicAdd(&st[mesh].n_eval, (unsigned long long)evaluated);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int o = t + DIST_THREADS * k;  // (x << 6) | (y << 3) | z
+  for (int k = 0; k < 512 / THREADS; ++k) {
+    const int o = t + THREADS * k;  // (x << 6) | (y << 3) | z
     const uint32_t u = dmin[((o & 0x38) << 3) | ((o & 7) << 3) | (o >> 6)];
     const float dist = fsqrt(__uint_as_float(u));
     const bool act = dist < __int_as_float(0x7f800000);  // sqrt of a finite square can overflow to inf
     const uint32_t m = __ballot_sync(0xffffffffu, act);
     values[uint64_t(b) * 512 + o] = act ? dist : 0.0f;
-    if (lane == 0) masks[uint64_t(b) * 16 + warp + 4 * k] = m;
+    if (lane == 0) masks[uint64_t(b) * 16 + warp + (THREADS / 32) * k] = m;
   }
 }
 
@@ -1381,18 +1383,18 @@ __device__ __forceinline__ void wn_warp(const uint32_t* __restrict__ act, uint64
   }
 }
 
-template <int ORDER>
-__global__ void __launch_bounds__(WN_THREADS) k_wn_sign(const uint32_t* __restrict__ act, uint64_t na,
+template <int ORDER, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_wn_sign(const uint32_t* __restrict__ act, uint64_t na,
                                                         const int4* __restrict__ origins, float* __restrict__ values,
                                                         const float4* __restrict__ inode,
                                                         const float4* __restrict__ leaf,
                                                         const float4* __restrict__ inode3,
                                                         const float4* __restrict__ leaf3, int n, float h, float beta,
                                                         float thresh, M2VStats* st) {
-  __shared__ int stk[WN_WARPS][WN_STACK];
+  __shared__ int stk[WARPS][WN_STACK];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const uint64_t i = (blockIdx.x * uint64_t(WN_WARPS) + w) * 32 + lane;
-  if ((blockIdx.x * uint64_t(WN_WARPS) + w) * 32 >= na) return;  // whole warp out of range
+  const uint64_t i = (blockIdx.x * uint64_t(WARPS) + w) * 32 + lane;
+  if ((blockIdx.x * uint64_t(WARPS) + w) * 32 >= na) return;  // whole warp out of range
   wn_warp<ORDER>(act, i, i < na, na - 1, origins, values, inode, leaf, inode3, leaf3, n, h, beta, thresh, st, stk);
 }
 
@@ -1832,8 +1834,18 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
     bidx.reset();
     BS_KERNEL(ctx, "k_fill_pairs", (k_fill_pairs<<<blocks(ns, 256), 256, 0, s>>>(S.p, ns, d_dirs.p, d_db.p, cnt.p, list.p)));
     cnt.reset();
-    BS_KERNEL(ctx, "k_brick_distance", (k_brick_distance<<<unsigned(nb), DIST_THREADS, 0, s>>>(origins.p, list_off.p, list.p, S.p, d_mi.p,
-                                                          leaf_base.p, K, values.p, masks.p, st.p)));
+    const int dt = ctx->tune_dist_threads;
+#define BS_DIST(TH)                                                                                              \
+  BS_KERNEL(ctx, "k_brick_distance", (k_brick_distance<TH><<<unsigned(nb), TH, 0, s>>>(origins.p, list_off.p, list.p, \
+                                                                                        S.p, d_mi.p, leaf_base.p, K,   \
+                                                                                        values.p, masks.p, st.p)))
+    if (dt == 64)
+      BS_DIST(64);
+    else if (dt == 256)
+      BS_DIST(256);
+    else
+      BS_DIST(128);
+#undef BS_DIST
   }
   S.reset();
 
@@ -1863,15 +1875,26 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   T.reset();
   if (na > 0) {
     const uint64_t n_warps = warp_base[K];
-    if (K == 1 && mi[0].order < 3)
-      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<2><<<blocks(na, WN_THREADS), WN_THREADS, 0, s>>>(act.p, na, origins.p, values.p, inode.p, leaf.p,
-                                                                                    nullptr, nullptr, int(nt), mi[0].h,
-                                                                                    mi[0].beta, mi[0].thresh, st.p)));
-    else if (K == 1)
-      BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<3><<<blocks(na, WN_THREADS), WN_THREADS, 0, s>>>(act.p, na, origins.p, values.p, inode.p, leaf.p,
-                                                                                    inode3.p, leaf3.p, int(nt), mi[0].h,
-                                                                                    mi[0].beta, mi[0].thresh, st.p)));
-    else if (!any3)
+#define BS_WN1(O, WP, I3, L3)                                                                                   \
+  BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<O, WP><<<blocks(na, 32 * WP), 32 * WP, 0, s>>>(                      \
+                                  act.p, na, origins.p, values.p, inode.p, leaf.p, I3, L3, int(nt), mi[0].h,   \
+                                  mi[0].beta, mi[0].thresh, st.p)))
+    const int ww = ctx->tune_wn_warps;
+    if (K == 1 && mi[0].order < 3) {
+      if (ww == 2)
+        BS_WN1(2, 2, nullptr, nullptr);
+      else if (ww == 8)
+        BS_WN1(2, 8, nullptr, nullptr);
+      else
+        BS_WN1(2, 4, nullptr, nullptr);
+    } else if (K == 1) {
+      if (ww == 2)
+        BS_WN1(3, 2, inode3.p, leaf3.p);
+      else if (ww == 8)
+        BS_WN1(3, 8, inode3.p, leaf3.p);
+      else
+        BS_WN1(3, 4, inode3.p, leaf3.p);
+    } else if (!any3)
       BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign_batch<2><<<blocks(n_warps, WN_WARPS), WN_THREADS, 0, s>>>(act.p, act_base.p, d_wb.p, K, d_mi.p, d_tb.p,
                                                                                        d_ib.p, origins.p, values.p, inode.p, leaf.p,
                                                                                        nullptr, nullptr, st.p)));
@@ -1879,6 +1902,7 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
       BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign_batch<3><<<blocks(n_warps, WN_WARPS), WN_THREADS, 0, s>>>(act.p, act_base.p, d_wb.p, K, d_mi.p, d_tb.p,
                                                                                        d_ib.p, origins.p, values.p, inode.p, leaf.p,
                                                                                        inode3.p, leaf3.p, st.p)));
+#undef BS_WN1
   }
   read_back(ctx, hst.data(), st.p, K * sizeof(M2VStats));
   uint64_t n_vp = 0, n_p = 0, visits = 0, far = 0, exact = 0, n_ev = 0;
@@ -2082,6 +2106,79 @@ bs_status bs_winding_numbers_approximate(bs_ctx* ctx, const bs_wn_tree* t, const
 bs_status bs_winding_numbers_free(bs_wn_tree* t) {
   if (!t) return BS_ERR_INVALID_ARG;
   delete t;
+  return BS_OK;
+}
+
+// Times the distance and sign passes of one mesh -> volume conversion under
+// each candidate launch shape (threads per brick 64 / 128 / 256 with 2 / 4 /
+// 8 warps per sign block; two rounds, best of each) and keeps the fastest of
+// each pass for the context's later calls.  h_choice: [threads per brick,
+// warps per sign block]; h_ms (optional, 6 floats): the distance then the
+// sign times per candidate.
+bs_status bs_autotune_mesh_to_volume(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
+                                     const bs_m2v_params* p, int32_t* h_choice, float* h_ms) {
+  if (!ctx || !p || !h_choice || !d_xyz || !d_tri || !nt) return BS_ERR_INVALID_ARG;
+  const bool timing0 = ctx->timing;
+  const int dt0 = ctx->tune_dist_threads, ww0 = ctx->tune_wn_warps;
+  try {
+    BS_CUDA(cudaSetDevice(ctx->device));
+    bs_ctx_resolve_stages(ctx);
+    auto saved = ctx->stages;
+    const int cand[3][2] = {{64, 2}, {128, 4}, {256, 8}};
+    double best[3][2] = {{1e30, 1e30}, {1e30, 1e30}, {1e30, 1e30}};
+    bs::volume_release(bs::mesh_to_volume_impl(ctx, d_xyz, nv, d_tri, nt, *p));  // warm-up
+    ctx->timing = true;
+    for (int round = 0; round < 2; ++round) {
+      for (int c = 0; c < 3; ++c) {
+        ctx->tune_dist_threads = cand[c][0];
+        ctx->tune_wn_warps = cand[c][1];
+        ctx->stages.clear();
+        bs::volume_release(bs::mesh_to_volume_impl(ctx, d_xyz, nv, d_tri, nt, *p));
+        bs_ctx_resolve_stages(ctx);
+        const auto d = ctx->stages.find("k_brick_distance"), w = ctx->stages.find("k_wn_sign");
+        if (d != ctx->stages.end()) best[c][0] = std::min(best[c][0], d->second.ms);
+        if (w != ctx->stages.end()) best[c][1] = std::min(best[c][1], w->second.ms);
+      }
+    }
+    int bd = 1, bw = 1;
+    for (int c = 0; c < 3; ++c) {
+      if (best[c][0] < best[bd][0]) bd = c;
+      if (best[c][1] < best[bw][1]) bw = c;
+    }
+    ctx->tune_dist_threads = cand[bd][0];
+    ctx->tune_wn_warps = cand[bw][1];
+    ctx->stages = saved;
+    ctx->timing = timing0;
+    h_choice[0] = ctx->tune_dist_threads;
+    h_choice[1] = ctx->tune_wn_warps;
+    if (h_ms)
+      for (int c = 0; c < 3; ++c) {
+        h_ms[c] = float(best[c][0]);
+        h_ms[3 + c] = float(best[c][1]);
+      }
+    return BS_OK;
+  } catch (const bs::Error& e) {
+    ctx->timing = timing0;
+    ctx->tune_dist_threads = dt0;
+    ctx->tune_wn_warps = ww0;
+    ctx->last_error = e.msg;
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    ctx->timing = timing0;
+    ctx->tune_dist_threads = dt0;
+    ctx->tune_wn_warps = ww0;
+    return BS_ERR_OOM;
+  }
+}
+
+// Sets the launch shapes directly (0 keeps a value): threads per brick of
+// the distance pass (64, 128, 256), warps per sign block (2, 4, 8).
+bs_status bs_ctx_set_launch_shape(bs_ctx* ctx, int32_t dist_threads, int32_t wn_warps) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  if (dist_threads && dist_threads != 64 && dist_threads != 128 && dist_threads != 256) return BS_ERR_INVALID_ARG;
+  if (wn_warps && wn_warps != 2 && wn_warps != 4 && wn_warps != 8) return BS_ERR_INVALID_ARG;
+  if (dist_threads) ctx->tune_dist_threads = dist_threads;
+  if (wn_warps) ctx->tune_wn_warps = wn_warps;
   return BS_OK;
 }
 

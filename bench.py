@@ -227,6 +227,8 @@ def run_ours(args):
     L.bs_m2v_params_default(C.byref(params))
     params.voxel_size = H
     params.band_width = BAND
+    tune_choice = (C.c_int32 * 2)()
+    tune_ms = (C.c_float * 6)()
     if args.pipeline_only:
         params.voxel_size = args.voxel_size
         # the boolean / offset / dual-contouring tail alone, once (a profiling case)
@@ -283,6 +285,14 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
+    # autotuned launch shapes (on torus A), part of the warm-up
+    tuned = None
+    if args.autotune:
+        N.check(L.bs_autotune_mesh_to_volume(ctx.h, dev[0][0].data_ptr(), dev[0][0].shape[0], dev[0][1].data_ptr(),
+                                             dev[0][1].shape[0], C.byref(params), tune_choice, tune_ms), ctx.h)
+        tuned = {"dist_threads": int(tune_choice[0]), "wn_warps": int(tune_choice[1]),
+                 "distance_ms_64_128_256": [round(float(x), 2) for x in tune_ms[:3]],
+                 "sign_ms_2_4_8_warps": [round(float(x), 2) for x in tune_ms[3:]]}
     for _ in range(args.warmup):
         step_device()
     ctx.synchronize()
@@ -388,6 +398,7 @@ def run_ours(args):
             "last_stats": stats,
             "pipeline": pipe,
             "batched": batch,
+            "autotuned_launch_shape": tuned,
             "order3_beta1.5": fast3}
     if rank == 0:
         if world == 1:
@@ -857,6 +868,8 @@ def main():
                     help="skip the secondary boolean / offset / dual-contouring timings")
     ap.add_argument("--tris-fraction", type=float, default=1.0,
                     help="use only the first part of each torus ring (smaller case for profiling)")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the default launch shapes (128 threads per brick, 4 warps per sign block)")
     ap.add_argument("--no-order3", dest="order3", action="store_false",
                     help="skip the order-3 / accuracy-scale-1.5 sign-pass comparison")
     ap.add_argument("--batch-meshes", type=int, default=256,

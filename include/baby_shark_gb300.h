@@ -150,6 +150,18 @@ bs_status bs_mesh_to_volume_batch_device(bs_ctx* ctx, uint64_t n_meshes, const f
                                          const uint64_t* vertex_counts, const uint32_t* d_tri,
                                          const uint64_t* triangle_counts, const bs_m2v_params* params,
                                          bs_volume** out);
+/* Autotuner (no reference counterpart): converts the given mesh (device
+ * arrays) once per candidate launch shape — 64 / 128 / 256 threads per brick
+ * in the distance pass with 2 / 4 / 8 warps per block in the sign pass, two
+ * rounds — and keeps the fastest shape of each pass for the context's later
+ * conversions (results do not depend on the shape).  h_choice[2]: the
+ * chosen threads per brick and warps per block; h_ms (optional, 6 floats):
+ * the best distance-pass then sign-pass times per candidate, in ms.  The
+ * brick stays 8^3 (the reference's leaf) and the sub-triangle tile 16. */
+bs_status bs_autotune_mesh_to_volume(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
+                                     const bs_m2v_params* p, int32_t* h_choice, float* h_ms);
+/* Sets the launch shapes directly (0 keeps the current value). */
+bs_status bs_ctx_set_launch_shape(bs_ctx* ctx, int32_t dist_threads, int32_t wn_warps);
 /* ------------------------------------------------------------- volumes --- */
 bs_status bs_volume_free(bs_volume* v);
 /* Volume::voxel_size (volume/mod.rs:31-34). */

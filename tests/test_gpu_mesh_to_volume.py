@@ -299,3 +299,23 @@ def test_distance_error_vs_float64_fine_voxel():
     d64 = min_distance_f64(vox, h, sub, box)
     err = np.abs(np.abs(val[li, vi]).astype(np.float64) - d64) / h
     assert err.max() < 2e-4
+
+
+def test_launch_shapes_give_identical_volumes_and_autotune_picks_one():
+    """Every launch shape the autotuner chooses from gives the same volume,
+    bit for bit; the autotuner returns one of them."""
+    ctx = bs.Context(0)
+    v, f = synthetic.torus(1.0, 0.3, 96, 48, 0.02, seed=5)
+    ref = None
+    for dt, ww in ((64, 2), (128, 4), (256, 8), (64, 8), (256, 2)):
+        ctx.set_launch_shape(dt, ww)
+        vol = bs.MeshToVolume(ctx).with_voxel_size(0.01).with_narrow_band_width(2).convert((v, f))
+        o, val, m = vol.export()
+        if ref is None:
+            ref = (o, val, m)
+        else:
+            assert np.array_equal(o, ref[0]) and np.array_equal(m, ref[2])
+            assert np.array_equal(val.view(np.uint32), ref[1].view(np.uint32))
+    choice = ctx.autotune((v, f), 0.01, 2)
+    assert choice["dist_threads"] in (64, 128, 256) and choice["wn_warps"] in (2, 4, 8)
+    assert all(t > 0 for t in choice["distance_ms"].values())
