@@ -440,14 +440,16 @@ __device__ __forceinline__ int voxel_tris(const DcVol& V, const int* nb, const u
   return nt;
 }
 
-// Counts (tris == nullptr: vcount[l] = triangles of leaf l) or writes the
-// leaf's triangles from tris + voff[l], voxels in ascending index order.
-// Thread t owns voxels 4t .. 4t+3; a block prefix over the 128 threads
-// places them.
+// Count pass (tris == nullptr): vcount[l] = triangles of leaf l, and the
+// counts of thread t's voxels 4t .. 4t+3 as four 4-bit fields in
+// packed[l * 128 + t] (a voxel has at most 6 triangles).  Write pass: the
+// leaf's triangles from tris + voff[l], voxels in ascending index order,
+// placed by a block prefix over the packed counts.
 __global__ void __launch_bounds__(128) k_dc_quads(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
                                                   const uint32_t* __restrict__ cellm, const uint32_t* __restrict__ celloff,
                                                   const float* __restrict__ cells, float h, uint64_t* __restrict__ vcount,
-                                                  const uint64_t* __restrict__ voff, float* __restrict__ tris) {
+                                                  const uint64_t* __restrict__ voff, uint16_t* __restrict__ packed,
+                                                  float* __restrict__ tris) {
   __shared__ int nb[27];
   __shared__ uint32_t wsum[4];
   const uint64_t l = blockIdx.x;
@@ -456,13 +458,19 @@ __global__ void __launch_bounds__(128) k_dc_quads(DcVol V, uint64_t n, const uin
   load_neighbours(V, org, nb);
   __syncthreads();
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  int c[4];
-  uint32_t mine = 0;
+  uint32_t pk = 0, mine = 0;
+  if (!tris) {
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int o = 4 * t + k;
-    c[k] = voxel_tris(V, nb, cm, cellm, celloff, cells, l, o >> 6, (o >> 3) & 7, o & 7, h, nullptr);
-    mine += uint32_t(c[k]);
+    for (int k = 0; k < 4; ++k) {
+      const int o = 4 * t + k;
+      const uint32_t c = uint32_t(voxel_tris(V, nb, cm, cellm, celloff, cells, l, o >> 6, (o >> 3) & 7, o & 7, h, nullptr));
+      pk |= c << (4 * k);
+      mine += c;
+    }
+    packed[l * 128 + t] = uint16_t(pk);
+  } else {
+    pk = packed[l * 128 + t];
+    mine = (pk & 15u) + ((pk >> 4) & 15u) + ((pk >> 8) & 15u) + (pk >> 12);
   }
   // inclusive prefix over the block's threads
   uint32_t inc = mine;
@@ -483,10 +491,11 @@ __global__ void __launch_bounds__(128) k_dc_quads(DcVol V, uint64_t n, const uin
   uint64_t pos = voff[l] + before + inc - mine;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    if (!c[k]) continue;
+    const uint32_t c = (pk >> (4 * k)) & 15u;
+    if (!c) continue;
     const int o = 4 * t + k;
     voxel_tris(V, nb, cm, cellm, celloff, cells, l, o >> 6, (o >> 3) & 7, o & 7, h, tris + pos * 9);
-    pos += uint64_t(c[k]);
+    pos += c;
   }
 }
 
@@ -542,7 +551,8 @@ void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size, int mode) {
     BS_KERNEL(ctx, "k_dc_cell_points", (k_dc_cell_points<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, coff.p, pts.p, cellm.p, celloff.p, cells.p)));
   // 3. quads
   DBuf<uint64_t> vcnt(ctx, n + 1), voff(ctx, n + 1);
-  BS_KERNEL(ctx, "k_dc_quads", (k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, cellm.p, celloff.p, cells.p, voxel_size, vcnt.p, nullptr, nullptr)));
+  DBuf<uint16_t> packed(ctx, n * 128);
+  BS_KERNEL(ctx, "k_dc_quads", (k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, cellm.p, celloff.p, cells.p, voxel_size, vcnt.p, nullptr, packed.p, nullptr)));
   scan_e(ctx, vcnt.p, voff.p, n + 1);
   uint64_t nt = 0;
   read_back(ctx, &nt, voff.p + n, sizeof(uint64_t));
@@ -552,7 +562,7 @@ void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size, int mode) {
     fail(BS_ERR_UNSUPPORTED, "dual contouring: gradient at a voxel with no active neighbour on an axis (the reference stops with unreachable!())");
   v->d_dc_tris = dalloc<float>(ctx, uint64_t(nt) * 9);
   if (nt)
-    BS_KERNEL(ctx, "k_dc_quads", (k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, cellm.p, celloff.p, cells.p, voxel_size, nullptr, voff.p, v->d_dc_tris)));
+    BS_KERNEL(ctx, "k_dc_quads", (k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, cellm.p, celloff.p, cells.p, voxel_size, nullptr, voff.p, packed.p, v->d_dc_tris)));
   v->n_dc_tris = nt;
   v->dc_valid = true;
   v->dc_h = voxel_size;

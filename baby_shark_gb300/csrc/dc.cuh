@@ -29,6 +29,7 @@ __global__ void k_dc_cell_points(DcVol V, uint64_t n, const uint32_t* __restrict
                                  float* __restrict__ cells);
 __global__ void k_dc_quads(DcVol V, uint64_t n, const uint32_t* __restrict__ cm, const uint32_t* __restrict__ cellm,
                            const uint32_t* __restrict__ celloff, const float* __restrict__ cells, float h,
-                           uint64_t* __restrict__ vcount, const uint64_t* __restrict__ voff, float* __restrict__ tris);
+                           uint64_t* __restrict__ vcount, const uint64_t* __restrict__ voff,
+                           uint16_t* __restrict__ packed, float* __restrict__ tris);
 
 }  // namespace bs

@@ -129,6 +129,7 @@ extern "C" bs_status bs_dual_contour_noalloc(int device, void* stream, const int
     float* cells = c.take<float>(DCNA_MAX_CELLS * 3);
     uint64_t* vcnt = c.take<uint64_t>(n + 1);
     uint64_t* voff = c.take<uint64_t>(n + 1);
+    uint16_t* packed = c.take<uint16_t>(n * 128);
     const size_t temp_bytes = 1u << 20;
     void* temp = c.take<unsigned char>(temp_bytes);
     // start empty: hash, error flags
@@ -159,7 +160,7 @@ extern "C" bs_status bs_dual_contour_noalloc(int device, void* stream, const int
     if (nc > DCNA_MAX_CELLS) return BS_ERR_CAPACITY;
     k_dc_cell_points<<<unsigned(n), 128, 0, s>>>(V, n, cm, coff, pts, cellm, celloff, cells);
     BS_CUDA(cudaGetLastError());
-    k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm, cellm, celloff, cells, voxel_size, vcnt, nullptr, nullptr);
+    k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm, cellm, celloff, cells, voxel_size, vcnt, nullptr, packed, nullptr);
     BS_CUDA(cudaGetLastError());
     scan_in(s, temp, temp_bytes, vcnt, voff, n + 1);
     const uint64_t nt = read1(s, voff + n);
@@ -168,7 +169,7 @@ extern "C" bs_status bs_dual_contour_noalloc(int device, void* stream, const int
     *n_tris = nt;
     if (nt > capacity) return BS_ERR_CAPACITY;  // *n_tris tells the caller the size to provide
     if (nt) {
-      k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm, cellm, celloff, cells, voxel_size, nullptr, voff, d_tris);
+      k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm, cellm, celloff, cells, voxel_size, nullptr, voff, packed, d_tris);
       BS_CUDA(cudaGetLastError());
     }
     BS_CUDA(cudaStreamSynchronize(s));

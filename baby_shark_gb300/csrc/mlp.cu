@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(MLP_THREADS) k_mlp_fwd_bwd(MlpW W, MlpTrain T,
 // and layer-1 gradients into W1, b1; 1 -> layer-1 activations and layer-2
 // gradients into W2, b2).  Warp w owns input rows 16w .. 16w+15 of dW; K is
 // the samples of the block's chunk.  Block (0, 0) counts the step.
-constexpr uint32_t WG_CHUNK = 512;
+constexpr uint32_t WG_CHUNK = 128;
 __global__ void __launch_bounds__(MLP_THREADS) k_mlp_wgrad(MlpTrain T, uint32_t batch) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, w = threadIdx.x >> 5;
   const bool second = blockIdx.y == 1;

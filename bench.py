@@ -47,10 +47,10 @@ WN_FAR_PER_VOXEL = 110.1    # the oracle's traversal of the reference's SAH tree
 WN_EXACT_PER_VOXEL = 14.4   # torus (1/8 ring sample, 4.5 M band voxels): counts per band voxel
 WN_FLOP_PER_VOXEL = int(round(WN_FAR_PER_VOXEL * WN_FLOP_FAR + WN_EXACT_PER_VOXEL * WN_FLOP_EXACT))
 # dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture of
-# the half-ring case (k_wn_sign 324 MB for 17,900,503 band voxels,
+# the half-ring case (k_wn_sign 322 MB for 17,900,503 band voxels,
 # k_brick_distance 716 MB for 3,416,413,115 voxel pairs), scaled to a full
 # torus by the units processed (35,669,277 voxels; 6,848,421,294 pairs)
-TRAFFIC_PER_LAUNCH = {"k_wn_sign": 647e6, "k_brick_distance": 1436e6}
+TRAFFIC_PER_LAUNCH = {"k_wn_sign": 642e6, "k_brick_distance": 1436e6}
 METRIC = "band voxels/s mesh→SDF+sign: learned/batched vs plain GPU, 0 sign flips"
 UNIT = "band_voxels/s"
 WORKLOAD = "two displaced tori, 1,048,576 triangles each, voxel 0.002, band 3: mesh->SDF+sign (plain GPU path)"

@@ -223,7 +223,7 @@ bs_status bs_mlp_get_params(bs_ctx* ctx, const bs_mlp* net, float* h_params);
 /* Predictions at n device points into d_out (device). */
 bs_status bs_mlp_predict(bs_ctx* ctx, const bs_mlp* net, const float* d_points, uint64_t n, float* d_out);
 /* Adam training on mean squared error: epochs over floor(n / batch)
- * minibatches of the device arrays in their order (batch a multiple of 512),
+ * minibatches of the device arrays in their order (batch a multiple of 128),
  * cosine learning rate lr_max -> lr_min; each step is replayed from one
  * captured CUDA graph.  h_epoch_loss (optional, epochs floats): mean loss. */
 bs_status bs_mlp_train(bs_ctx* ctx, bs_mlp* net, const float* d_points, const float* d_targets, uint64_t n,
