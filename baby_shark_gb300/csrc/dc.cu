@@ -45,10 +45,13 @@ __device__ __forceinline__ void load_neighbours(const DcVol& V, int4 org, int* n
 // as the tree's `at` returns it: an active leaf voxel, or, for a voxel
 // outside every leaf, its active tile's value.  Inactive voxels of a leaf
 // have no value.
+// TILES: the volume has active tiles (the kernels reading neighbour values
+// come in both forms, so tile-free volumes run without the lookup).
+template <bool TILES>
 __device__ __forceinline__ bool at(const DcVol& V, const int* nb, int4 org, int x, int y, int z, float& v) {
   const int k = ((x >> 3) + 1) * 9 + ((y >> 3) + 1) * 3 + ((z >> 3) + 1);
   const int l = nb[k];
-  if (l < 0) return V.tiles.any && tile_value(V.tiles, org.x + x, org.y + y, org.z + z, v);
+  if (l < 0) return TILES && tile_value(V.tiles, org.x + x, org.y + y, org.z + z, v);
   const int o = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
   if (!((V.msk[uint64_t(l) * 16 + (o >> 5)] >> (o & 31)) & 1u)) return false;
   v = V.val[uint64_t(l) * 512 + o];
@@ -56,13 +59,14 @@ __device__ __forceinline__ bool at(const DcVol& V, const int* nb, int4 org, int 
 }
 
 // dual_contouring.rs:362-386
+template <bool TILES>
 __device__ __forceinline__ bool grad(const DcVol& V, const int* nb, int4 org, int x, int y, int z, int axis,
                                      float& g) {
   const int lx = axis == 0 ? 1 : 0, ly = axis == 1 ? 1 : 0, lz = axis == 2 ? 1 : 0;
   float vp, vl, vr;
-  const bool hp = at(V, nb, org, x, y, z, vp);
-  const bool hl = at(V, nb, org, x - lx, y - ly, z - lz, vl);
-  const bool hr = at(V, nb, org, x + lx, y + ly, z + lz, vr);
+  const bool hp = at<TILES>(V, nb, org, x, y, z, vp);
+  const bool hl = at<TILES>(V, nb, org, x - lx, y - ly, z - lz, vl);
+  const bool hr = at<TILES>(V, nb, org, x + lx, y + ly, z + lz, vr);
   if (hp && hl && hr) { g = fmul(fsub(vr, vl), 0.5f); return true; }
   if (hp && hr) { g = fsub(vr, vp); return true; }
   if (hp && hl) { g = fsub(vp, vl); return true; }
@@ -70,6 +74,7 @@ __device__ __forceinline__ bool grad(const DcVol& V, const int* nb, int4 org, in
 }
 
 // Pass 1a: crossing masks.  cm[l][dir][16]
+template <bool TILES>
 __global__ void __launch_bounds__(128) k_dc_edge_mask(DcVol V, uint64_t n, uint32_t* __restrict__ cm,
                                                       uint32_t* __restrict__ ccount) {
   __shared__ int nb[27];
@@ -85,11 +90,11 @@ __global__ void __launch_bounds__(128) k_dc_edge_mask(DcVol V, uint64_t n, uint3
     const int o = t + 128 * k;
     const int x = o >> 6, y = (o >> 3) & 7, z = o & 7;
     float v1;
-    const bool h1 = at(V, nb, org, x, y, z, v1);
+    const bool h1 = at<TILES>(V, nb, org, x, y, z, v1);
 #pragma unroll
     for (int dir = 0; dir < 3; ++dir) {
       float v2;
-      const bool cross = h1 && at(V, nb, org, x + (dir == 0), y + (dir == 1), z + (dir == 2), v2) &&
+      const bool cross = h1 && at<TILES>(V, nb, org, x + (dir == 0), y + (dir == 1), z + (dir == 2), v2) &&
                          (signbit(v1) != signbit(v2));
       const uint32_t m = __ballot_sync(0xffffffffu, cross);
       if (lane == 0) {
@@ -115,6 +120,7 @@ __device__ __forceinline__ uint32_t rank512(const uint32_t* m, int o) {
 }
 
 // Pass 1b: crossing points and normals (dual_contouring.rs:249-313).
+template <bool TILES>
 __global__ void __launch_bounds__(128) k_dc_edge_points(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
                                                         const uint32_t* __restrict__ coff, float* __restrict__ pts,
                                                         DcStats* st) {
@@ -131,8 +137,8 @@ __global__ void __launch_bounds__(128) k_dc_edge_points(DcVol V, uint64_t n, con
     const int x = o >> 6, y = (o >> 3) & 7, z = o & 7;
     const int x2 = x + (dir == 0), y2 = y + (dir == 1), z2 = z + (dir == 2);
     float v1, v2;
-    at(V, nb, org, x, y, z, v1);
-    at(V, nb, org, x2, y2, z2, v2);
+    at<TILES>(V, nb, org, x, y, z, v1);
+    at<TILES>(V, nb, org, x2, y2, z2, v2);
     const float t = (v1 == v2) ? 0.5f : fdiv(v1, fsub(v1, v2));
     float p[3] = {__int2float_rn(org.x + x), __int2float_rn(org.y + y), __int2float_rn(org.z + z)};
     p[dir] = fadd(p[dir], t);
@@ -140,7 +146,7 @@ __global__ void __launch_bounds__(128) k_dc_edge_points(DcVol V, uint64_t n, con
     bool ok = true;
     for (int a = 0; a < 3; ++a) {
       float g1, g2;
-      ok = ok && grad(V, nb, org, x, y, z, a, g1) && grad(V, nb, org, x2, y2, z2, a, g2);
+      ok = ok && grad<TILES>(V, nb, org, x, y, z, a, g1) && grad<TILES>(V, nb, org, x2, y2, z2, a, g2);
       if (ok) nrm[a] = fadd(fmul(fsub(1.0f, t), g1), fmul(t, g2));
     }
     if (!ok) {
@@ -170,6 +176,7 @@ __constant__ int8_t c_cells[3][4][3] = {{{0, 0, 0}, {0, 0, -1}, {0, -1, -1}, {0,
                                         {{0, -1, 0}, {-1, -1, 0}, {-1, 0, 0}, {0, 0, 0}}};
 
 // Pass 2a: cells with all 8 corners active and a sign change (dual_contouring.rs:193-217).
+template <bool TILES>
 __global__ void __launch_bounds__(128) k_dc_cell_mask(DcVol V, uint64_t n, uint32_t* __restrict__ cellm,
                                                       uint32_t* __restrict__ ccount) {
   __shared__ int nb[27];
@@ -188,7 +195,7 @@ __global__ void __launch_bounds__(128) k_dc_cell_mask(DcVol V, uint64_t n, uint3
     bool ok = true, any_neg = false, any_pos = false;
     for (int c = 0; c < 8 && ok; ++c) {
       float v;
-      ok = at(V, nb, org, x + c_cube[c][0], y + c_cube[c][1], z + c_cube[c][2], v);
+      ok = at<TILES>(V, nb, org, x + c_cube[c][0], y + c_cube[c][1], z + c_cube[c][2], v);
       if (ok) {
         if (signbit(v)) any_neg = true;
         else any_pos = true;
@@ -441,62 +448,93 @@ __device__ __forceinline__ int voxel_tris(const DcVol& V, const int* nb, const u
 }
 
 // Count pass (tris == nullptr): vcount[l] = triangles of leaf l, and the
-// counts of thread t's voxels 4t .. 4t+3 as four 4-bit fields in
-// packed[l * 128 + t] (a voxel has at most 6 triangles).  Write pass: the
-// leaf's triangles from tris + voff[l], voxels in ascending index order,
-// placed by a block prefix over the packed counts.
+// counts of thread t's voxels t, t + 128, t + 256, t + 384 as four 4-bit
+// fields in packed[l * 128 + t] (a voxel has at most 6 triangles).  Write
+// pass: the leaf's triangles from tris + voff[l], voxels in ascending index
+// order; one block scan of the four counts packed in 16-bit fields of a
+// 64-bit word gives every round's prefix at once.
 __global__ void __launch_bounds__(128) k_dc_quads(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
                                                   const uint32_t* __restrict__ cellm, const uint32_t* __restrict__ celloff,
                                                   const float* __restrict__ cells, float h, uint64_t* __restrict__ vcount,
                                                   const uint64_t* __restrict__ voff, uint16_t* __restrict__ packed,
                                                   float* __restrict__ tris) {
   __shared__ int nb[27];
-  __shared__ uint32_t wsum[4];
+  __shared__ unsigned long long wsum[4];
   const uint64_t l = blockIdx.x;
   if (l >= n) return;
   const int4 org = V.org[l];
   load_neighbours(V, org, nb);
   __syncthreads();
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  uint32_t pk = 0, mine = 0;
   if (!tris) {
-#pragma unroll
+    uint32_t pk = 0, mine = 0;
+#pragma unroll 1
     for (int k = 0; k < 4; ++k) {
-      const int o = 4 * t + k;
+      const int o = t + 128 * k;
       const uint32_t c = uint32_t(voxel_tris(V, nb, cm, cellm, celloff, cells, l, o >> 6, (o >> 3) & 7, o & 7, h, nullptr));
       pk |= c << (4 * k);
       mine += c;
     }
     packed[l * 128 + t] = uint16_t(pk);
-  } else {
-    pk = packed[l * 128 + t];
-    mine = (pk & 15u) + ((pk >> 4) & 15u) + ((pk >> 8) & 15u) + (pk >> 12);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, d);
+    if (lane == 0) wsum[w] = mine;
+    __syncthreads();
+    if (t == 0) vcount[l] = wsum[0] + wsum[1] + wsum[2] + wsum[3];
+    if (l == n - 1 && t == 1) vcount[n] = 0;
+    return;
   }
-  // inclusive prefix over the block's threads
-  uint32_t inc = mine;
+  const uint32_t pk = packed[l * 128 + t];
+  if (__syncthreads_or(pk) == 0) return;  // no triangles in this leaf
+  // counts of rounds 0..3 in 16-bit fields (a round's prefix is at most 768)
+  const unsigned long long mine = (unsigned long long)(pk & 15u) | ((unsigned long long)((pk >> 4) & 15u) << 16) |
+                                  ((unsigned long long)((pk >> 8) & 15u) << 32) |
+                                  ((unsigned long long)(pk >> 12) << 48);
+  unsigned long long inc = mine;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
-    const uint32_t v = __shfl_up_sync(0xffffffffu, inc, d);
+    const unsigned long long v = __shfl_up_sync(0xffffffffu, inc, d);
     if (lane >= d) inc += v;
   }
   if (lane == 31) wsum[w] = inc;
   __syncthreads();
-  uint32_t before = 0;
+  unsigned long long before = 0;
   for (int i = 0; i < w; ++i) before += wsum[i];
-  if (!tris) {
-    if (t == 127) vcount[l] = before + inc;
-    if (l == n - 1 && t == 0) vcount[n] = 0;
-    return;
-  }
-  uint64_t pos = voff[l] + before + inc - mine;
-#pragma unroll
+  const unsigned long long total = wsum[0] + wsum[1] + wsum[2] + wsum[3];
+  const unsigned long long excl = before + inc - mine;
+  uint64_t run = voff[l];
+#pragma unroll 1
   for (int k = 0; k < 4; ++k) {
     const uint32_t c = (pk >> (4 * k)) & 15u;
-    if (!c) continue;
-    const int o = 4 * t + k;
-    voxel_tris(V, nb, cm, cellm, celloff, cells, l, o >> 6, (o >> 3) & 7, o & 7, h, tris + pos * 9);
-    pos += c;
+    if (c) {
+      const int o = t + 128 * k;
+      const uint64_t pos = run + ((excl >> (16 * k)) & 0xffffull);
+      voxel_tris(V, nb, cm, cellm, celloff, cells, l, o >> 6, (o >> 3) & 7, o & 7, h, tris + pos * 9);
+    }
+    run += (total >> (16 * k)) & 0xffffull;
   }
+}
+
+// Launches of the kernels that read neighbour values, in the form for
+// volumes with or without active tiles (also used by dc_noalloc.cu).
+void launch_dc_edge_mask(bool tiles, const DcVol& V, uint64_t n, uint32_t* cm, uint32_t* ccnt, cudaStream_t s) {
+  if (tiles)
+    k_dc_edge_mask<true><<<unsigned(n), 128, 0, s>>>(V, n, cm, ccnt);
+  else
+    k_dc_edge_mask<false><<<unsigned(n), 128, 0, s>>>(V, n, cm, ccnt);
+}
+void launch_dc_edge_points(bool tiles, const DcVol& V, uint64_t n, const uint32_t* cm, const uint32_t* coff,
+                           float* pts, DcStats* st, cudaStream_t s) {
+  if (tiles)
+    k_dc_edge_points<true><<<unsigned(n), 128, 0, s>>>(V, n, cm, coff, pts, st);
+  else
+    k_dc_edge_points<false><<<unsigned(n), 128, 0, s>>>(V, n, cm, coff, pts, st);
+}
+void launch_dc_cell_mask(bool tiles, const DcVol& V, uint64_t n, uint32_t* cellm, uint32_t* cellc, cudaStream_t s) {
+  if (tiles)
+    k_dc_cell_mask<true><<<unsigned(n), 128, 0, s>>>(V, n, cellm, cellc);
+  else
+    k_dc_cell_mask<false><<<unsigned(n), 128, 0, s>>>(V, n, cellm, cellc);
 }
 
 static bool has_active_tiles(const bs_volume* v) { return v->n_tiles != 0; }
@@ -532,15 +570,15 @@ void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size, int mode) {
   BS_CUDA(cudaMemsetAsync(st.p, 0, sizeof(DcStats), s));
   // 1. crossings
   DBuf<uint32_t> cm(ctx, n * 3 * 16), ccnt(ctx, n * 3 + 1), coff(ctx, n * 3 + 1);
-  BS_KERNEL(ctx, "k_dc_edge_mask", (k_dc_edge_mask<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, ccnt.p)));
+  BS_KERNEL(ctx, "k_dc_edge_mask", launch_dc_edge_mask(V.tiles.any, V, n, cm.p, ccnt.p, s));
   scan_e(ctx, ccnt.p, coff.p, n * 3 + 1);
   uint32_t ne = 0;
   read_back(ctx, &ne, coff.p + n * 3, sizeof(uint32_t));
   DBuf<float> pts(ctx, uint64_t(ne) * 6);
-  BS_KERNEL(ctx, "k_dc_edge_points", (k_dc_edge_points<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, coff.p, pts.p, st.p)));
+  BS_KERNEL(ctx, "k_dc_edge_points", launch_dc_edge_points(V.tiles.any, V, n, cm.p, coff.p, pts.p, st.p, s));
   // 2. cells
   DBuf<uint32_t> cellm(ctx, n * 16), cellc(ctx, n + 1), celloff(ctx, n + 1);
-  BS_KERNEL(ctx, "k_dc_cell_mask", (k_dc_cell_mask<<<unsigned(n), 128, 0, s>>>(V, n, cellm.p, cellc.p)));
+  BS_KERNEL(ctx, "k_dc_cell_mask", launch_dc_cell_mask(V.tiles.any, V, n, cellm.p, cellc.p, s));
   scan_e(ctx, cellc.p, celloff.p, n + 1);
   uint32_t nc = 0;
   read_back(ctx, &nc, celloff.p + n, sizeof(uint32_t));
@@ -552,7 +590,7 @@ void dual_contour_impl(bs_ctx* ctx, bs_volume* v, float voxel_size, int mode) {
   // 3. quads
   DBuf<uint64_t> vcnt(ctx, n + 1), voff(ctx, n + 1);
   DBuf<uint16_t> packed(ctx, n * 128);
-  BS_KERNEL(ctx, "k_dc_quads", (k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, cellm.p, celloff.p, cells.p, voxel_size, vcnt.p, nullptr, packed.p, nullptr)));
+  BS_KERNEL(ctx, "k_dc_quads_count", (k_dc_quads<<<unsigned(n), 128, 0, s>>>(V, n, cm.p, cellm.p, celloff.p, cells.p, voxel_size, vcnt.p, nullptr, packed.p, nullptr)));
   scan_e(ctx, vcnt.p, voff.p, n + 1);
   uint64_t nt = 0;
   read_back(ctx, &nt, voff.p + n, sizeof(uint64_t));

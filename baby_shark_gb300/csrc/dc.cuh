@@ -19,10 +19,12 @@ struct DcStats {
   int error;  // 1: gradient with no neighbours
 };
 
-__global__ void k_dc_edge_mask(DcVol V, uint64_t n, uint32_t* __restrict__ cm, uint32_t* __restrict__ ccount);
-__global__ void k_dc_edge_points(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
-                                 const uint32_t* __restrict__ coff, float* __restrict__ pts, DcStats* st);
-__global__ void k_dc_cell_mask(DcVol V, uint64_t n, uint32_t* __restrict__ cellm, uint32_t* __restrict__ ccount);
+// Launches of the kernels that read neighbour values (tiles: the volume has
+// active tiles, read through the tree's `at`).
+void launch_dc_edge_mask(bool tiles, const DcVol& V, uint64_t n, uint32_t* cm, uint32_t* ccnt, cudaStream_t s);
+void launch_dc_edge_points(bool tiles, const DcVol& V, uint64_t n, const uint32_t* cm, const uint32_t* coff,
+                           float* pts, DcStats* st, cudaStream_t s);
+void launch_dc_cell_mask(bool tiles, const DcVol& V, uint64_t n, uint32_t* cellm, uint32_t* cellc, cudaStream_t s);
 __global__ void k_dc_cell_points(DcVol V, uint64_t n, const uint32_t* __restrict__ cm,
                                  const uint32_t* __restrict__ coff, const float* __restrict__ pts,
                                  const uint32_t* __restrict__ cellm, const uint32_t* __restrict__ celloff,

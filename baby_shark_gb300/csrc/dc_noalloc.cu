@@ -146,14 +146,14 @@ extern "C" bs_status bs_dual_contour_noalloc(int device, void* stream, const int
     k_hash_insert<<<nblocks(n, 256), 256, 0, s>>>(hash, org, n, herr);
     BS_CUDA(cudaGetLastError());
     DcVol V{org, d_values, d_masks, hash, TileLookup{}};  // the caller's arrays hold leaves only
-    k_dc_edge_mask<<<unsigned(n), 128, 0, s>>>(V, n, cm, ccnt);
+    launch_dc_edge_mask(false, V, n, cm, ccnt, s);
     BS_CUDA(cudaGetLastError());
     scan_in(s, temp, temp_bytes, ccnt, coff, n * 3 + 1);
     const uint32_t ne = read1(s, coff + n * 3);
     if (ne > DCNA_MAX_CROSSINGS) return BS_ERR_CAPACITY;
-    k_dc_edge_points<<<unsigned(n), 128, 0, s>>>(V, n, cm, coff, pts, st);
+    launch_dc_edge_points(false, V, n, cm, coff, pts, st, s);
     BS_CUDA(cudaGetLastError());
-    k_dc_cell_mask<<<unsigned(n), 128, 0, s>>>(V, n, cellm, cellc);
+    launch_dc_cell_mask(false, V, n, cellm, cellc, s);
     BS_CUDA(cudaGetLastError());
     scan_in(s, temp, temp_bytes, cellc, celloff, n + 1);
     const uint32_t nc = read1(s, celloff + n);
