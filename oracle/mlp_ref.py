@@ -13,15 +13,20 @@ import numpy as np
 OFF_W1, OFF_B1, OFF_W2, OFF_B2, OFF_W3, OFF_B3, NP = 0, 4096, 4160, 8256, 8320, 8384, 8385
 
 
+ROUND = True  # False: no BF16 rounding (for finite-difference checks of the restatement itself)
+
+
 def bf16(x):
     """Round float32 values to bfloat16 (nearest even), returned as float32."""
+    if not ROUND:
+        return np.asarray(x, np.float64)
     u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
     u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
     return u.astype(np.uint32).view(np.float32)
 
 
 def unpack(params):
-    p = np.asarray(params, np.float32)
+    p = np.asarray(params, np.float32 if ROUND else np.float64)
     return (p[OFF_W1:OFF_B1].reshape(64, 64), p[OFF_B1:OFF_W2], p[OFF_W2:OFF_B2].reshape(64, 64),
             p[OFF_B2:OFF_W3], p[OFF_W3:OFF_B3], p[OFF_B3])
 
@@ -38,7 +43,8 @@ def dsilu(z):
 def features(points, freq, centre, scale):
     xn = ((np.asarray(points, np.float32) - np.asarray(centre, np.float32)) * np.float32(scale)).astype(np.float64)
     v = xn @ np.asarray(freq, np.float64).reshape(32, 3).T
-    return bf16(np.concatenate([np.sin(np.pi * v), np.cos(np.pi * v)], axis=1).astype(np.float32)).astype(np.float64)
+    f = np.concatenate([np.sin(np.pi * v), np.cos(np.pi * v)], axis=1)
+    return bf16(f if not ROUND else f.astype(np.float32)).astype(np.float64)
 
 
 def forward(params, freq, centre, scale, points):
@@ -46,7 +52,7 @@ def forward(params, freq, centre, scale, points):
     W1, b1, W2, b2, w3, b3 = unpack(params)
     F = features(points, freq, centre, scale)
     z1 = F @ bf16(W1).astype(np.float64) + b1
-    h1 = bf16(silu(z1).astype(np.float32)).astype(np.float64)
+    h1 = bf16(silu(z1) if not ROUND else silu(z1).astype(np.float32)).astype(np.float64)
     z2 = h1 @ bf16(W2).astype(np.float64) + b2
     h2 = silu(z2)
     y = h2 @ w3.astype(np.float64) + float(b3)
@@ -65,9 +71,11 @@ def gradients(params, freq, centre, scale, points, targets):
     g = np.zeros(NP)
     g[OFF_W3:OFF_B3] = h2.T @ dy
     g[OFF_B3] = dy.sum()
-    dz2 = bf16((dy[:, None] * w3.astype(np.float64)[None, :] * dsilu(z2)).astype(np.float32)).astype(np.float64)
+    dz2 = dy[:, None] * w3.astype(np.float64)[None, :] * dsilu(z2)
+    dz2 = bf16(dz2 if not ROUND else dz2.astype(np.float32)).astype(np.float64)
     dh1 = dz2 @ bf16(W2).astype(np.float64).T
-    dz1 = bf16((dh1 * dsilu(z1)).astype(np.float32)).astype(np.float64)
+    dz1 = dh1 * dsilu(z1)
+    dz1 = bf16(dz1 if not ROUND else dz1.astype(np.float32)).astype(np.float64)
     g[OFF_W2:OFF_B2] = (h1.T @ dz2).ravel()
     g[OFF_B2:OFF_W3] = dz2.sum(axis=0)
     g[OFF_W1:OFF_B1] = (F.T @ dz1).ravel()
