@@ -20,6 +20,9 @@ struct bs_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // second stream of the library's own (the tree build overlaps the distance
+  // pass on it); created on first use, ordered against `stream` by events
+  cudaStream_t side = nullptr;
   cudaMemPool_t pool = nullptr;
   uint64_t launches = 0;
   std::string last_error;

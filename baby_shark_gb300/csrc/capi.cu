@@ -47,6 +47,10 @@ void bs_ctx_release(bs_ctx* ctx) {
     cudaEventDestroy(p.a);
     cudaEventDestroy(p.b);
   }
+  if (ctx->side) {
+    cudaStreamSynchronize(ctx->side);
+    cudaStreamDestroy(ctx->side);
+  }
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);

@@ -16,13 +16,13 @@
 // Steps 1-3 use IEEE-exact arithmetic (bs_internal.cuh) so distances and the
 // active set match the reference bit for bit.
 #include <cub/device/device_radix_sort.cuh>
-
-#include <vector>
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <exception>
+#include <vector>
 
 #include "bs_internal.cuh"
 
@@ -1530,6 +1530,36 @@ __global__ void k_split(const uint32_t* __restrict__ leaf_base, int K, const Spl
 // [tri_base[m], tri_base[m+1])), from Morton order and PLOC, with the
 // far-field records of every node (and the order-3 ones when order3).
 // st[m] holds each mesh's centroid bounds.
+struct Event {
+  cudaEvent_t e = nullptr;
+  Event() { BS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming)); }
+  ~Event() {
+    if (e) cudaEventDestroy(e);
+  }
+  Event(const Event&) = delete;
+  Event& operator=(const Event&) = delete;
+};
+
+// Points the context's stream at its side stream for the lifetime of the
+// object (allocations, frees, launches and read-backs of the calls inside
+// go there) and back afterwards, also when a call throws.
+struct SideStream {
+  bs_ctx* ctx;
+  cudaStream_t main;
+  explicit SideStream(bs_ctx* c) : ctx(c), main(c->stream) {
+    if (!ctx->side) BS_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+    ctx->stream = ctx->side;
+  }
+  ~SideStream() {
+    // a throwing call may leave work in flight that reads buffers the
+    // unwinding frees on the main stream: finish it first
+    if (std::uncaught_exceptions()) cudaStreamSynchronize(ctx->side);
+    ctx->stream = main;
+  }
+  SideStream(const SideStream&) = delete;
+  SideStream& operator=(const SideStream&) = delete;
+};
+
 static void build_trees(bs_ctx* ctx, const float4* T, uint64_t nt, int K, const uint32_t* d_tb, const uint32_t* d_ib,
                         const M2VStats* st, bool order3, DBuf<float4>& leaf, DBuf<float4>& inode,
                         DBuf<float4>& leaf3, DBuf<float4>& inode3) {
@@ -1755,6 +1785,9 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   DBuf<float4> T(ctx, 3 * nt);
   DBuf<uint32_t> nsub(ctx, nt + 1), soff(ctx, nt + 1);
   BS_KERNEL(ctx, "k_gather", (k_gather<<<blocks(nt + 1, 256), 256, 0, s>>>(d_xyz, d_tri, nt, d_mi.p, d_tb.p, K, T.p, nsub.p, st.p)));
+  // the triangles, offsets and stats the tree build reads are ready here
+  Event gathered, built;
+  BS_CUDA(cudaEventRecord(gathered.e, s));
   exclusive_scan(ctx, nsub.p, soff.p, nt + 1);
   uint32_t total = 0;
   read_back(ctx, hst.data(), st.p, K * sizeof(M2VStats));
@@ -1850,6 +1883,17 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   S.reset();
 
   // active voxels, and per mesh its first brick / voxel
+  // one tree per mesh over its original triangles, built on the side stream
+  // while the distance pass runs (the build's own syncs wait for it alone)
+  const bool any3 = std::any_of(mi.begin(), mi.end(), [](const MeshInfo& q) { return q.order >= 3; });
+  DBuf<float4> leaf, inode, leaf3, inode3;
+  {
+    SideStream side(ctx);
+    BS_CUDA(cudaStreamWaitEvent(ctx->stream, gathered.e, 0));
+    build_trees(ctx, T.p, nt, K, d_tb.p, d_ib.p, st.p, any3, leaf, inode, leaf3, inode3);
+    BS_CUDA(cudaEventRecord(built.e, ctx->stream));
+  }
+
   DBuf<uint32_t> vc(ctx, nb + 1), voff(ctx, nb + 1);
   BS_KERNEL(ctx, "k_brick_popcount", (k_brick_popcount<<<blocks(nb + 1, 256), 256, 0, s>>>(masks.p, nb, vc.p)));
   exclusive_scan(ctx, vc.p, voff.p, nb + 1);
@@ -1867,11 +1911,8 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   vc.reset();
   voff.reset();
 
-  // one tree per mesh over its original triangles
-  const bool any3 = std::any_of(mi.begin(), mi.end(), [](const MeshInfo& q) { return q.order >= 3; });
-  const uint64_t n_int = nt - uint64_t(K);
-  DBuf<float4> leaf, inode, leaf3, inode3;
-  build_trees(ctx, T.p, nt, K, d_tb.p, d_ib.p, st.p, any3, leaf, inode, leaf3, inode3);
+  // join the tree build; the triangles are freed after it
+  BS_CUDA(cudaStreamWaitEvent(s, built.e, 0));
   T.reset();
   if (na > 0) {
     const uint64_t n_warps = warp_base[K];
