@@ -358,6 +358,11 @@ def run_ours(args):
         extra["pairs_evaluated_fraction"] = ev / max(1, stats["voxel_pairs"])
     elif name == "k_wn_sign":
         flops = WN_FLOP_PER_VOXEL * stats["active_voxels"]
+        # what the warp-coherent traversal executes: every lane of a warp evaluates
+        # each node the warp takes as far, and each leaf the warp opens exactly
+        executed = 32 * (WN_FLOP_FAR * stats["wn_warp_far"] + WN_FLOP_EXACT * stats["wn_warp_exact"])
+        extra["executed_tflops"] = executed / per_launch_s / 1e12
+        extra["executed_flop_per_launch"] = executed
         algo = ("%d FLOP per band voxel (the reference's own traversal: %.0f far-field nodes x %d FLOP + "
                 "%.0f exact triangles x %d FLOP, counted by the oracle) x %d voxels per launch"
                 % (WN_FLOP_PER_VOXEL, WN_FAR_PER_VOXEL, WN_FLOP_FAR, WN_EXACT_PER_VOXEL, WN_FLOP_EXACT,
