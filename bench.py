@@ -19,6 +19,17 @@ Synthetic, seeded (baby_shark_gb300.synthetic).
   cpu_baseline: the oracle (CPU restatement of the reference path, OpenMP,
           all host cores) on a bounded sample of the same workload.
 
+Beside the headline line (default run): the boolean / offset / meshing tail
+on those volumes (`pipeline`), the order-3 far field at accuracy scale 1.5
+(`order3_beta1.5`), the 256-mesh uneven batch (`batched`) and the launch
+shapes the autotuner picked during warm-up (`autotuned_launch_shape`).
+
+Other workloads (`--workload`): `open-icosphere` (4.7 M triangles with
+holes, voxel 0.001, signs of a sample checked against exact winding
+numbers), `large-union` (16 tori, 12 M triangles, voxel 0.0005: batched
+conversion, union, dual contouring, peak device memory), `learned` (the
+learned far field against the traversal on points in the padded box).
+
 `--impl reference` times the reference path's CPU implementation (the
 oracle port; the Rust crate cannot be built here) on the same metric.
 """
