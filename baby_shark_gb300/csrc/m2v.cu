@@ -124,10 +124,10 @@ __device__ __forceinline__ void warp_max(T* dst, T v, bool uniform, unsigned mas
   }
 }
 
-struct SubTri {  // 64 B: vertices and the widened inclusive integer box
+struct SubTri {  // 64 B: vertices, cull coefficients and the widened inclusive integer box
   float4 p0;     // a.x a.y a.z b.x
   float4 p1;     // b.y b.z c.x c.y
-  float4 p2;     // c.z, -, -, -
+  float4 p2;     // c.z, cull coefficients c2 and E0 (cull_coeffs), -
   int4 lo;       // box min (x, y, z), mesh
   int4 hi;       // box max
 };
@@ -218,14 +218,64 @@ __device__ __forceinline__ void widened_box(F3 a, F3 b, F3 c, float inv_h, int b
   }
 }
 
-__device__ __forceinline__ void put_subtri(SubTri* S, uint64_t idx, F3 a, F3 b, F3 c, float inv_h, int band,
+// Cull coefficients of one sub-triangle.  In the reference's closest-point
+// formula (Ericson, point_triangle_dist2) the vertex cases return a vertex
+// exactly and the edge cases a parameter in [0, 1] (their denominators add
+// two numbers of one sign), so there the float32 closest point leaves the
+// triangle only by rounding.  The face case divides by va + vb + vc, whose
+// exact value is |ab x ac|^2 and whose float32 error is at most about
+// 70 u e^2 R_p^2 (u = 2^-24, e the longest edge, R_p the largest distance
+// from the voxel p to a vertex: the six dot products carry 5 u e R_p each);
+// the parameters then move by at most about 93 u e^2 R_p^2 / (|ab x ac|^2 / 4)
+// and the point by 188 u e^3 R_p^2 / |ab x ac|^2, bounded here by
+// c (d + e)^2 with c = 1024 u e^3 / |ab x ac|^2, since every vertex is within
+// d + e of p for d the exact distance.  With the rounding of the vertex,
+// edge and final |q - p| terms (19 u (d + e) + 16 u e + 4 u M, M a bound on
+// |coordinates|) the float32 distance is at least d - eps(d), and
+// eps(sqrt(lb)) <= c2 lb + E0 for c2 = 2 c and E0 = 2 c e^2 + 19 u (R + e)
+// + 16 u e + 4 u M, R the widened box diagonal.  The cull test
+// lb' > cur * 33/32 + 33 t^2 with t = c2 lb' + E0 (lb' the float32 sum of the
+// squared box distances each scaled by 1 - 2^-20, so lb' < lb (1 - 8 u))
+// implies sqrt(lb) - t > sqrt(cur) (2 t sqrt(cur) <= cur / 32 + 32 t^2), so a
+// culled pair's float32 distance is above cur.  Conditions checked here:
+// the perturbation is small (c R^2 <= e), d - eps(d) increases on [0, R]
+// (c (R + e) <= 1/4), and the right side grows slower than lb
+// (132 c (c2 R^2 + E0) <= 1/2); a sub-triangle that fails one (every
+// degenerate one does) is never culled (c2 = +inf).
+__device__ __forceinline__ void cull_coeffs(F3 ab, F3 ac, F3 cb, float R, float M, float& c2, float& E0) {
+  const float u = 5.9604645e-8f;
+  const float e2 = fmaxf(dot3(ab, ab), fmaxf(dot3(ac, ac), dot3(cb, cb)));
+  const float e = sqrtf(e2);
+  const F3 n = cross3(ab, ac);
+  const float a2sq = dot3(n, n);
+  const float c = 1024.0f * u * (e2 * e / a2sq);  // +inf or NaN for a degenerate triangle
+  const float e0 = 2.0f * c * e2 + 19.0f * u * (R + e) + 16.0f * u * e + 4.0f * u * M;
+  const bool ok = c * R * R <= e && c * (R + e) <= 0.25f && 132.0f * c * (2.0f * c * R * R + e0) <= 0.5f &&
+                  e0 < __int_as_float(0x7f800000);
+  c2 = ok ? 2.0f * c : __int_as_float(0x7f800000);
+  E0 = ok ? e0 : 0.0f;
+}
+
+// A sub-triangle record: vertices, widened box, mesh, and the cull
+// coefficients of the distance pass (computed once here rather than for
+// every brick the box meets).
+__device__ __forceinline__ void put_subtri(SubTri* S, uint64_t idx, F3 a, F3 b, F3 c, float h, float inv_h, int band,
                                            int mesh) {
   int lo[3], hi[3];
   widened_box(a, b, c, inv_h, band, lo, hi);
+  // R: the widened box holds the vertices and every voxel it covers
+  const float ex = float(hi[0] - lo[0]), ey = float(hi[1] - lo[1]), ez = float(hi[2] - lo[2]);
+  const float R = h * (sqrtf(ex * ex + ey * ey + ez * ez) + 2.0f);
+  const float gm = h * float(max(max(max(abs(lo[0]), abs(hi[0])), max(abs(lo[1]), abs(hi[1]))),
+                                 max(abs(lo[2]), abs(hi[2]))) + 1);
+  const float M = fmaxf(gm, fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(b.x))),
+                                  fmaxf(fmaxf(fabsf(b.y), fabsf(b.z)), fmaxf(fmaxf(fabsf(c.x), fabsf(c.y)), fabsf(c.z)))));
+  float c2, e0;
+  cull_coeffs(sub3(b, a), sub3(c, a), sub3(c, b), R, M, c2, e0);
   SubTri s;
   s.p0 = make_float4(a.x, a.y, a.z, b.x);
   s.p1 = make_float4(b.y, b.z, c.x, c.y);
-  s.p2 = make_float4(c.z, 0.f, 0.f, 0.f);
+  s.p2 = make_float4(c.z, c2, e0, 0.f);
   s.lo = make_int4(lo[0], lo[1], lo[2], mesh);
   s.hi = make_int4(hi[0], hi[1], hi[2], 0);
   S[idx] = s;
@@ -244,7 +294,7 @@ __global__ void k_subdivide(const float4* __restrict__ T, const uint32_t* __rest
   F3 p1 = f3(ta.x, ta.y, ta.z), p2 = f3(tb.x, tb.y, tb.z), p3 = f3(tc.x, tc.y, tc.z);
   uint64_t o = off[i];
   if (nsub[i] == 1) {
-    put_subtri(S, o, p1, p2, p3, inv_h, band, mesh);
+    put_subtri(S, o, p1, p2, p3, h, inv_h, band, mesh);
     return;
   }
   F3 e0 = sub3(p2, p1), e1 = sub3(p3, p1), e2 = sub3(p3, p2);
@@ -261,14 +311,14 @@ __global__ void k_subdivide(const float4* __restrict__ T, const uint32_t* __rest
     F3 a_s = add3(a, s2), b_s = add3(b, s2), c_s = add3(c, s2);
     F3 a_prev = a;
     for (uint32_t k = 0; k < r; ++k) {
-      put_subtri(S, o++, a_prev, b_s, a_s, inv_h, band, mesh);
-      put_subtri(S, o++, a_s, b_s, c_s, inv_h, band, mesh);
+      put_subtri(S, o++, a_prev, b_s, a_s, h, inv_h, band, mesh);
+      put_subtri(S, o++, a_s, b_s, c_s, h, inv_h, band, mesh);
       a_prev = a_s;
       a_s = add3(a_s, s2);
       b_s = add3(b_s, s2);
       c_s = add3(c_s, s2);
     }
-    put_subtri(S, o++, a, b, c, inv_h, band, mesh);
+    put_subtri(S, o++, a, b, c, h, inv_h, band, mesh);
     a = add3(a, s1);
   }
 }
@@ -431,44 +481,6 @@ struct __align__(16) BatchTri {
   int4 box1;   // nz, mask of the brick x covered by the widened box, bits of E0, -
 };
 
-// Cull coefficients of one sub-triangle.  In the reference's closest-point
-// formula (Ericson, point_triangle_dist2) the vertex cases return a vertex
-// exactly and the edge cases a parameter in [0, 1] (their denominators add
-// two numbers of one sign), so there the float32 closest point leaves the
-// triangle only by rounding.  The face case divides by va + vb + vc, whose
-// exact value is |ab x ac|^2 and whose float32 error is at most about
-// 70 u e^2 R_p^2 (u = 2^-24, e the longest edge, R_p the largest distance
-// from the voxel p to a vertex: the six dot products carry 5 u e R_p each);
-// the parameters then move by at most about 93 u e^2 R_p^2 / (|ab x ac|^2 / 4)
-// and the point by 188 u e^3 R_p^2 / |ab x ac|^2, bounded here by
-// c (d + e)^2 with c = 1024 u e^3 / |ab x ac|^2, since every vertex is within
-// d + e of p for d the exact distance.  With the rounding of the vertex,
-// edge and final |q - p| terms (19 u (d + e) + 16 u e + 4 u M, M a bound on
-// |coordinates|) the float32 distance is at least d - eps(d), and
-// eps(sqrt(lb)) <= c2 lb + E0 for c2 = 2 c and E0 = 2 c e^2 + 19 u (R + e)
-// + 16 u e + 4 u M, R the widened box diagonal.  The cull test
-// lb' > cur * 33/32 + 33 t^2 with t = c2 lb' + E0 (lb' the float32 sum of the
-// squared box distances each scaled by 1 - 2^-20, so lb' < lb (1 - 8 u))
-// implies sqrt(lb) - t > sqrt(cur) (2 t sqrt(cur) <= cur / 32 + 32 t^2), so a
-// culled pair's float32 distance is above cur.  Conditions checked here:
-// the perturbation is small (c R^2 <= e), d - eps(d) increases on [0, R]
-// (c (R + e) <= 1/4), and the right side grows slower than lb
-// (132 c (c2 R^2 + E0) <= 1/2); a sub-triangle that fails one (every
-// degenerate one does) is never culled (c2 = +inf).
-__device__ __forceinline__ void cull_coeffs(F3 ab, F3 ac, F3 cb, float R, float M, float& c2, float& E0) {
-  const float u = 5.9604645e-8f;
-  const float e2 = fmaxf(dot3(ab, ab), fmaxf(dot3(ac, ac), dot3(cb, cb)));
-  const float e = sqrtf(e2);
-  const F3 n = cross3(ab, ac);
-  const float a2sq = dot3(n, n);
-  const float c = 1024.0f * u * (e2 * e / a2sq);  // +inf or NaN for a degenerate triangle
-  const float e0 = 2.0f * c * e2 + 19.0f * u * (R + e) + 16.0f * u * e + 4.0f * u * M;
-  const bool ok = c * R * R <= e && c * (R + e) <= 0.25f && 132.0f * c * (2.0f * c * R * R + e0) <= 0.5f &&
-                  e0 < __int_as_float(0x7f800000);
-  c2 = ok ? 2.0f * c : __int_as_float(0x7f800000);
-  E0 = ok ? e0 : 0.0f;
-}
-
 constexpr float CULL_SCALE = 1.0f - 0x1p-20f;
 
 __device__ __forceinline__ float box_d(float lo, float hi, float g) { return fmaxf(fmaxf(lo - g, g - hi), 0.0f); }
@@ -528,14 +540,6 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_brick_distance(
       if (nx > 0 && ny > 0 && nz > 0) {
         BatchTri& q = W[lane];
         const F3 ab = sub3(bb, a), ac = sub3(c, a), cb = sub3(c, bb);
-        // R: the widened box holds the vertices and every voxel it covers
-        const float ex = float(sb.hi.x - sb.lo.x), ey = float(sb.hi.y - sb.lo.y), ez = float(sb.hi.z - sb.lo.z);
-        const float R = h * (sqrtf(ex * ex + ey * ey + ez * ez) + 2.0f);
-        const float gm = h * float(max(max(max(abs(sb.lo.x), abs(sb.hi.x)), max(abs(sb.lo.y), abs(sb.hi.y))),
-                                       max(abs(sb.lo.z), abs(sb.hi.z))) + 1);
-        const float M = fmaxf(gm, fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(bb.x))),
-                                        fmaxf(fmaxf(fabsf(bb.y), fabsf(bb.z)),
-                                              fmaxf(fmaxf(fabsf(c.x), fabsf(c.y)), fabsf(c.z)))));
         const float lox = fminf(fminf(a.x, bb.x), c.x), hix = fmaxf(fmaxf(a.x, bb.x), c.x);
         float dx[8];
 #pragma unroll
@@ -547,8 +551,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_brick_distance(
         q.v1 = make_float4(ab.y, ab.z, ac.x, ac.y);
         q.v2 = make_float4(ac.z, bb.x, bb.y, bb.z);
         q.v3 = make_float4(c.x, c.y, c.z, cb.x);
-        float c2, e0;
-        cull_coeffs(ab, ac, cb, R, M, c2, e0);
+        const float c2 = sb.p2.y, e0 = sb.p2.z;  // cull coefficients (put_subtri)
         q.v4 = make_float4(cb.y, cb.z, c2, 1.0f / float(nz));
         q.dxa = make_float4(dx[0], dx[1], dx[2], dx[3]);
         q.dxb = make_float4(dx[4], dx[5], dx[6], dx[7]);
