@@ -725,7 +725,7 @@ def run_large_union(args):
             "counts": {k: best[k] for k in ("band_voxels", "leaves_in", "union_leaves", "union_tiles",
                                             "union_active_voxels", "dc_triangles")},
             "device_memory_gb": {"peak_in_use": mem["used_high"] / 1e9, "reserved": mem["reserved"] / 1e9,
-                                 "budget": 180.0},
+                                 "workload_limit": 180.0},
             "generation_s": t_gen}
     print(json.dumps(line), flush=True)
 
