@@ -1452,6 +1452,52 @@ __global__ void __launch_bounds__(WN_THREADS) k_wn_points(const float* __restric
   if (i < np) out[i] = sum;
 }
 
+// Large point sets in no particular order (a warp of 32 scattered points opens
+// the union of 32 unrelated cuts) are traversed in Morton order: 30-bit keys
+// over the cube of half-size 2 r around the root's dipole centre (points
+// outside clamp to its faces, NaN to its low corner).
+__device__ __forceinline__ uint32_t expand10(uint32_t v) {
+  v &= 0x3ffu;
+  v = (v | v << 16) & 0x030000ffu;
+  v = (v | v << 8) & 0x0300f00fu;
+  v = (v | v << 4) & 0x030c30c3u;
+  v = (v | v << 2) & 0x09249249u;
+  return v;
+}
+
+__global__ void k_point_keys(const float* __restrict__ pts, uint64_t np, const float4* __restrict__ inode,
+                             uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= np) return;
+  const float4 R = inode[0];
+  const float inv = R.w > 0.f ? 0.25f / R.w : 0.f;
+  const float c[3] = {R.x, R.y, R.z};
+  uint32_t q[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float u = fminf(fmaxf((pts[3 * i + k] - c[k]) * inv + 0.5f, 0.f), 1.f);
+    q[k] = uint32_t(fminf(u * 1024.0f, 1023.0f));
+  }
+  keys[i] = (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
+  vals[i] = uint32_t(i);
+}
+
+__global__ void k_point_gather(const float* __restrict__ pts, const uint32_t* __restrict__ order, uint64_t np,
+                               float* __restrict__ dst) {
+  const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= np) return;
+  const uint64_t k = order[i];
+  dst[3 * i] = pts[3 * k];
+  dst[3 * i + 1] = pts[3 * k + 1];
+  dst[3 * i + 2] = pts[3 * k + 2];
+}
+
+__global__ void k_point_scatter(const float* __restrict__ v, const uint32_t* __restrict__ order, uint64_t np,
+                                float* __restrict__ out) {
+  const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i < np) out[order[i]] = v[i];
+}
+
 // ------------------------------------------------ exact winding numbers ---
 // Direct sum over every triangle (no tree, no far field): the solid angle of
 // each triangle in the reference's operation order (IEEE, unfused), the sum
@@ -2098,12 +2144,34 @@ static void wn_tree_approximate(bs_ctx* ctx, const bs_wn_tree* t, const float* d
   cudaStream_t s = ctx->stream;
   DBuf<M2VStats> st(ctx, 1);
   BS_CUDA(cudaMemsetAsync(st.p, 0, sizeof(M2VStats), s));
+  // from 2^20 points on, traverse a Morton-sorted copy and scatter back
+  const bool sorted = np >= (1ull << 20) && np < (1ull << 31) && t->nt >= 2;
+  DBuf<uint32_t> order;
+  DBuf<float> spts, sout;
+  const float* q = d_pts;
+  float* o = d_out;
+  if (sorted) {
+    DBuf<uint32_t> keys(ctx, np), keys2(ctx, np), vals(ctx, np);
+    order = DBuf<uint32_t>(ctx, np);
+    BS_KERNEL(ctx, "k_point_keys", (k_point_keys<<<blocks(np, 256), 256, 0, s>>>(d_pts, np, t->inode, keys.p, vals.p)));
+    size_t tmp = 0;
+    BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, keys.p, keys2.p, vals.p, order.p, int(np), 0, 30, s));
+    DBuf<uint8_t> tb(ctx, tmp);
+    BS_CUDA(cub::DeviceRadixSort::SortPairs(tb.p, tmp, keys.p, keys2.p, vals.p, order.p, int(np), 0, 30, s));
+    spts = DBuf<float>(ctx, 3 * np);
+    sout = DBuf<float>(ctx, np);
+    BS_KERNEL(ctx, "k_point_gather", (k_point_gather<<<blocks(np, 256), 256, 0, s>>>(d_pts, order.p, np, spts.p)));
+    q = spts.p;
+    o = sout.p;
+  }
   if (t->order >= 3)
-    BS_KERNEL(ctx, "k_wn_points", (k_wn_points<3><<<blocks(np, WN_THREADS), WN_THREADS, 0, s>>>(d_pts, np, t->inode, t->leaf, t->inode3,
-                                                                                         t->leaf3, int(t->nt), beta, d_out, st.p)));
+    BS_KERNEL(ctx, "k_wn_points", (k_wn_points<3><<<blocks(np, WN_THREADS), WN_THREADS, 0, s>>>(q, np, t->inode, t->leaf, t->inode3,
+                                                                                         t->leaf3, int(t->nt), beta, o, st.p)));
   else
-    BS_KERNEL(ctx, "k_wn_points", (k_wn_points<2><<<blocks(np, WN_THREADS), WN_THREADS, 0, s>>>(d_pts, np, t->inode, t->leaf, nullptr,
-                                                                                         nullptr, int(t->nt), beta, d_out, st.p)));
+    BS_KERNEL(ctx, "k_wn_points", (k_wn_points<2><<<blocks(np, WN_THREADS), WN_THREADS, 0, s>>>(q, np, t->inode, t->leaf, nullptr,
+                                                                                         nullptr, int(t->nt), beta, o, st.p)));
+  if (sorted)
+    BS_KERNEL(ctx, "k_point_scatter", (k_point_scatter<<<blocks(np, 256), 256, 0, s>>>(sout.p, order.p, np, d_out)));
   M2VStats hs;
   read_back(ctx, &hs, st.p, sizeof hs);
   if (hs.error == 3) fail(BS_ERR_CAPACITY, "winding-number traversal stack overflow");

@@ -65,3 +65,28 @@ def test_invalid_order():
     with pytest.raises(bs.BsError) as e:
         bs.WindingNumbers.from_mesh((v, f), order=4, ctx=context())
     assert e.value.status == 1
+
+
+def test_large_point_sets_traverse_in_morton_order():
+    """From 2^20 points on, the points are traversed in Morton order and the
+    values scattered back to the caller's order: every value stays within the
+    approximation error of the exact one and of the same points traversed
+    unsorted (in chunks below that size), since a warp of different
+    neighbours only opens a different set of nodes."""
+    v, f, pts = open_mesh_and_points()
+    rng = np.random.default_rng(24)
+    big = np.concatenate([pts[rng.permutation(len(pts))] + rng.normal(0, 1e-3, pts.shape).astype(np.float32)
+                          for _ in range(44)]).astype(np.float32)
+    assert len(big) >= 1 << 20
+    wn = bs.WindingNumbers.from_mesh((v, f), order=2, ctx=context())
+    g_big = wn.approximate(big, 2.0)
+    g_chunk = np.concatenate([wn.approximate(big[i:i + 500_000], 2.0) for i in range(0, len(big), 500_000)])
+    d = np.abs(g_big - g_chunk)
+    assert d.mean() < 5e-3 and d.max() < 0.06, (d.mean(), d.max())
+    # against exact values: no less accurate than the reference tree's own
+    # per-point traversal (the oracle's fast winding number) of the same points
+    pick = rng.choice(len(big), 20000, replace=False)
+    ex = bs.winding_numbers_exact(v, f, big[pick], ctx=context()).cpu().numpy()
+    o, _ = ob.fast_wn(v, f, big[pick], 2.0)
+    e_gpu, e_ref = np.abs(g_big[pick] - ex).mean(), np.abs(o - ex).mean()
+    assert e_gpu < 1.2 * e_ref, (e_gpu, e_ref)
