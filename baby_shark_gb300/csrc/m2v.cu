@@ -1280,19 +1280,17 @@ __device__ __forceinline__ float wn_traverse(F3 q, const float4* __restrict__ in
   const float beta2 = beta * beta;
   float sum = 0.f, comp = 0.f;  // Kahan-compensated accumulation
   bool overflow = false;
-  uint32_t c_visit = 0, c_far = 0, c_exact = 0;
+  uint32_t c_exact = 0;  // node visits and far-field evaluations follow from the loop count
 
   // Tests one node (>= 0 internal, < 0 leaf ~index) for the whole warp and
   // sums its far field or exact solid angle; returns true when the warp has
   // to open it (an internal node that is near for some lane).
   auto visit = [&](int node) -> bool {
-    ++c_visit;
     if (node >= 0) {
       const float4 P = inode[5 * node];
       const float rx = P.x - q.x, ry = P.y - q.y, rz = P.z - q.z;
       const float r2 = rx * rx + ry * ry + rz * rz;
       if (!__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) return true;
-      ++c_far;
       const float4 A = inode[5 * node + 1], B0 = inode[5 * node + 2], B1 = inode[5 * node + 3],
                    B2 = inode[5 * node + 4];
       // a.r / (4 pi r^3) + trace(B) / (4 pi r^3) - 3 r^T B r / (4 pi r^5)
@@ -1315,7 +1313,6 @@ __device__ __forceinline__ float wn_traverse(F3 q, const float4* __restrict__ in
     const float r2 = rx * rx + ry * ry + rz * rz;
     float wv;
     if (__all_sync(0xffffffffu, r2 > P.w * P.w * beta2)) {
-      ++c_far;
       const float4 A = leaf[5 * li + 1];
       const float ri = rsqrtf(r2);
       const float inv = ri * ri * ri * (1.0f / FOUR_PI);
@@ -1334,7 +1331,8 @@ __device__ __forceinline__ float wn_traverse(F3 q, const float4* __restrict__ in
   // other pushed, so the stack holds at most one pending node per level.
   int sp = 0;
   int node = (n > 1) ? (visit(0) ? 0 : -1) : (visit(~0), -1);
-  for (int guard = 0; guard < n + 2; ++guard) {
+  int it = 0;  // nodes opened
+  for (; it < n + 2; ++it) {
     if (node < 0) {
       if (sp == 0) break;
       --sp;
@@ -1358,6 +1356,10 @@ __device__ __forceinline__ float wn_traverse(F3 q, const float4* __restrict__ in
     }
   }
   if (overflow && lane == 0) atomicExch(&st->error, 3);
+  // every visit either opens a node (one per iteration; a stack overflow,
+  // flagged above, would drop some), takes a far field or an exact solid angle
+  const uint32_t c_visit = (n > 1) ? 1u + 2u * uint32_t(it) : 1u;
+  const uint32_t c_far = c_visit - c_exact - uint32_t(it);
   if (lane == 0) {
     atomicAdd(&st->wn_visits, (unsigned long long)c_visit);
     atomicAdd(&st->wn_far, (unsigned long long)c_far);
