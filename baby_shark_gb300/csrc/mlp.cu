@@ -556,6 +556,7 @@ bs_status bs_mlp_create(bs_ctx* ctx, const float* centre, float scale, const flo
 }
 
 bs_status bs_mlp_free(bs_mlp* q) {
+  if (!q) return BS_ERR_INVALID_ARG;  // as every other release call
   delete q;
   return BS_OK;
 }

@@ -46,3 +46,32 @@ def test_params_default_matches_reference():
     lib.bs_m2v_params_default(ctypes.byref(p))
     assert (p.voxel_size, p.band_width) == (1.0, 0)  # MeshToVolume::default (mesh_to_volume.rs:223-236)
     assert abs(p.wn_beta - 2.0) < 1e-7 and abs(p.wn_threshold - 0.2) < 1e-7  # mesh_to_volume.rs:264-266
+
+
+def test_every_call_rejects_null_arguments_before_device_work():
+    """Every status-returning entry point checks its handles, pointers and
+    sizes before it touches a device: with null pointers and zero sizes it
+    returns BS_ERR_INVALID_ARG (where the crate would panic on a missing
+    object, the boundary reports a status)."""
+    lib = N.load()
+    checked = 0
+    for name, (res, args) in N.SIGNATURES.items():
+        if res is not N.i32 or name == "bs_mlp_num_params":
+            continue
+        vals = [0.0 if a in (ctypes.c_float, ctypes.c_double) else
+                0 if a in (ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int64) else None
+                for a in args]
+        assert getattr(lib, name)(*vals) == 1, name  # BS_ERR_INVALID_ARG
+        checked += 1
+    assert checked >= 50
+
+
+def test_context_creation_without_a_device():
+    import pytest
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = N.load()
+    out = ctypes.c_void_p()
+    assert lib.bs_ctx_create(0, None, ctypes.byref(out)) == 8  # BS_ERR_NO_DEVICE
+    assert not out.value
