@@ -54,8 +54,9 @@ FLOP_PER_PAIR = 84          # closest point + norm, triangle3.rs:317-382 (face-r
 CULL_FLOP_PER_PAIR = 20     # voxel to bounding box distance and the cull comparison
 WN_FLOP_FAR = 31            # far test + order-1/2 terms, aabb_tree.rs:662-671, 803-816
 WN_FLOP_EXACT = 70          # Van Oosterom-Strackee solid angle, aabb_tree.rs:582-615 (atan2 as 20)
-WN_FAR_PER_VOXEL = 110.1    # the oracle's traversal of the reference's SAH tree on this workload's
-WN_EXACT_PER_VOXEL = 14.4   # torus (1/8 ring sample, 4.5 M band voxels): counts per band voxel
+WN_FAR_PER_VOXEL = 141.46   # the oracle's traversal of the reference's SAH tree over the whole torus
+WN_EXACT_PER_VOXEL = 14.96  # (1,048,576 triangles) from the 4.5 M band voxels of a 1/16 ring slice:
+#                             counts per band voxel (oracle/traversal_counts.py)
 WN_FLOP_PER_VOXEL = int(round(WN_FAR_PER_VOXEL * WN_FLOP_FAR + WN_EXACT_PER_VOXEL * WN_FLOP_EXACT))
 # dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture of
 # the half-ring case (k_wn_sign 322 MB for 17,900,503 band voxels,
