@@ -49,7 +49,10 @@ typedef struct bs_ctx bs_ctx;
 typedef struct bs_volume bs_volume;
 
 /* ---------------------------------------------------------------- context */
-/* Creates a context on `device`.  `stream` is a cudaStream_t to run on, or
+/* No reference counterpart: the crate runs on rayon's implicit global pool
+ * and owns its trees in Box allocations; a context holds what that takes here
+ * (device, stream, stream-ordered memory pool, launch shapes, counters).
+ * Creates a context on `device`.  `stream` is a cudaStream_t to run on, or
  * NULL for a stream the context creates and owns. */
 bs_status bs_ctx_create(int device, void* stream, bs_ctx** out);
 bs_status bs_ctx_destroy(bs_ctx* ctx);
@@ -163,12 +166,15 @@ bs_status bs_autotune_mesh_to_volume(bs_ctx* ctx, const float* d_xyz, uint64_t n
 /* Sets the launch shapes directly (0 keeps the current value). */
 bs_status bs_ctx_set_launch_shape(bs_ctx* ctx, int32_t dist_threads, int32_t wn_warps);
 /* ------------------------------------------------------------- volumes --- */
+/* Dropping a Volume (its Box<VolumeGrid>, volume/mod.rs:10-14). */
 bs_status bs_volume_free(bs_volume* v);
 /* Volume::voxel_size (volume/mod.rs:31-34). */
 bs_status bs_volume_voxel_size(const bs_volume* v, float* out);
 /* Volume's Clone impl (volume/mod.rs:114-121). */
 bs_status bs_volume_clone(bs_ctx* ctx, const bs_volume* v, bs_volume** out);
-/* Number of leaves and of active tiles (tiles appear only after booleans). */
+/* Number of leaves and of active tiles (tiles appear only after booleans).
+ * This and the two exports have no reference counterpart: they read a volume
+ * out for parity checks and hosts that store it. */
 bs_status bs_volume_counts(const bs_volume* v, uint64_t* n_leaves, uint64_t* n_tiles,
                            uint64_t* n_active_voxels);
 /* Copies the volume to HOST memory: h_origins[3*n_leaves] (int32 leaf origins,
@@ -200,9 +206,14 @@ typedef struct bs_wn_tree bs_wn_tree;
 bs_status bs_winding_numbers_build(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
                                    int order, bs_wn_tree** out);
 /* WindingNumbers::approximate(point, accuracy_scale) (aabb_tree.rs:654-660) at
- * n_points device points (3 floats each) into d_out; beta = accuracy_scale. */
+ * n_points device points (3 floats each) into d_out; beta = accuracy_scale.
+ * From 2^20 points on the call traverses a Morton-sorted copy of the points
+ * and returns the values in the caller's order: each warp of 32 then holds
+ * nearby points and opens few nodes beyond its lanes' own cuts, so values
+ * differ from those of smaller calls only within the approximation error. */
 bs_status bs_winding_numbers_approximate(bs_ctx* ctx, const bs_wn_tree* tree, const float* d_points, uint64_t n_points,
                                          float beta, float* d_out);
+/* Dropping the WindingNumbers tree. */
 bs_status bs_winding_numbers_free(bs_wn_tree* tree);
 
 /* ------------------------------------------------ learned far field ---- */
@@ -338,7 +349,8 @@ bs_status bs_corner_table_from_dual_contour(bs_ctx* ctx, bs_volume* v, float vox
 /* The same on the marching-cubes output (VoxelRemesher with the default
  * MeshingMethod::Manifold, remeshing/voxel.rs:64-85). */
 bs_status bs_corner_table_from_marching_cubes(bs_ctx* ctx, bs_volume* v, float voxel_size, bs_corner_table** out);
-/* Faces, live vertices, vertex slots (live + deleted) and corners. */
+/* Faces, live vertices, vertex slots (live + deleted) and corners
+ * (CornerTable::count_faces, face.rs:33; count_vertices, vertex.rs:122). */
 bs_status bs_corner_table_counts(const bs_corner_table* t, uint64_t* n_faces, uint64_t* n_vertices,
                                  uint64_t* n_vertex_slots, uint64_t* n_corners);
 /* Copies the tables to HOST memory (any pointer may be NULL): positions
@@ -346,6 +358,7 @@ bs_status bs_corner_table_counts(const bs_corner_table* t, uint64_t* n_faces, ui
  * corner -> vertex [corners], corner -> opposite corner [corners] (-1 none). */
 bs_status bs_corner_table_export(const bs_corner_table* t, float* h_positions, uint8_t* h_deleted,
                                  int32_t* h_vertex_corner, int32_t* h_corner_vertex, int32_t* h_corner_opposite);
+/* Dropping the CornerTable. */
 bs_status bs_corner_table_free(bs_corner_table* t);
 
 #ifdef __cplusplus
