@@ -14,11 +14,17 @@
 // the library's rule, the reference's box bound (aabb_tree.rs:738-741), or
 // the farthest vertex below the node.
 //
-// Usage: tree_sim vertices.f32 triangles.u32 warps.f32 S leafmax radius
+// Usage: tree_sim vertices.f32 triangles.u32 warps.f32 S leafmax radius [values.f32]
 //   S: 0 = PLOC alone; radius: 0 library, 1 box bound, 2 farthest vertex.
-//   warps.f32: groups of 32 query points (3 floats each).
+//   warps.f32: groups of 32 query points (3 floats each).  With values.f32
+//   each lane's winding number is written there: the order-2 far field of
+//   aabb_tree.rs:662-671, 803-816 for the nodes the warp takes as far, the
+//   solid angle of aabb_tree.rs:582-615 for the triangles it takes exactly.
 #include <algorithm>
 #include <cmath>
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -78,6 +84,7 @@ struct Leaf {
 struct Node {
   float p[3], r;
   int c0, c1, ntri;
+  float a[3], B[9];  // order-1 vector and order-2 matrix about p
 };
 
 }  // namespace
@@ -265,12 +272,18 @@ int main(int argc, char** argv) {
     double cx, cy, cz, s;
     Box b;
     int ntri;
+    double a[3], m[9];  // sum of area * normal; sum of centroid (area * normal)^T
   };
   std::vector<Sum> sum(static_cast<size_t>(ni));
   std::vector<Node> node(static_cast<size_t>(ni));
   auto leaf_sum = [&](int i) {
     const Leaf& l = leaf[size_t(i)];
-    return Sum{double(l.area) * l.c[0], double(l.area) * l.c[1], double(l.area) * l.c[2], double(l.area), l.b, 1};
+    Sum s{double(l.area) * l.c[0], double(l.area) * l.c[1], double(l.area) * l.c[2], double(l.area), l.b, 1, {}, {}};
+    for (int r = 0; r < 3; ++r) {
+      s.a[r] = l.a[r];
+      for (int q = 0; q < 3; ++q) s.m[3 * r + q] = double(l.c[r]) * l.a[q];
+    }
+    return s;
   };
   auto sphere = [&](int c, float* p, float& r) {
     const float* q = c >= 0 ? node[size_t(c)].p : leaf[size_t(~c)].c;
@@ -280,8 +293,10 @@ int main(int argc, char** argv) {
   for (int id = 0; id < ni; ++id) {
     const Sum a = child[size_t(id)].first >= 0 ? sum[size_t(child[size_t(id)].first)] : leaf_sum(~child[size_t(id)].first);
     const Sum b = child[size_t(id)].second >= 0 ? sum[size_t(child[size_t(id)].second)] : leaf_sum(~child[size_t(id)].second);
-    Sum s{a.cx + b.cx, a.cy + b.cy, a.cz + b.cz, a.s + b.s, a.b, a.ntri + b.ntri};
+    Sum s{a.cx + b.cx, a.cy + b.cy, a.cz + b.cz, a.s + b.s, a.b, a.ntri + b.ntri, {}, {}};
     s.b.add(b.b);
+    for (int k = 0; k < 3; ++k) s.a[k] = a.a[k] + b.a[k];
+    for (int k = 0; k < 9; ++k) s.m[k] = a.m[k] + b.m[k];
     sum[size_t(id)] = s;
     Node& q = node[size_t(id)];
     q.p[0] = float(s.cx / s.s);
@@ -304,6 +319,10 @@ int main(int argc, char** argv) {
     q.c0 = child[size_t(id)].first;
     q.c1 = child[size_t(id)].second;
     q.ntri = s.ntri;
+    for (int r = 0; r < 3; ++r) {
+      q.a[r] = float(s.a[r]);
+      for (int c = 0; c < 3; ++c) q.B[3 * r + c] = float(s.m[3 * r + c] - double(q.p[r]) * s.a[c]);
+    }
   }
   if (radius == 2) {
     std::vector<int> st;
@@ -331,11 +350,45 @@ int main(int argc, char** argv) {
 
   // warp-coherent traversal at accuracy scale 2
   const float beta2 = 4.0f;
+  const float inv4pi = float(1.0 / (4.0 * M_PI));
+  std::vector<float> value(argc > 7 ? static_cast<size_t>(32 * nw) : 0);
+  auto far_field = [&](int nd, const float* x) -> float {  // order 1 + 2 about the node centre
+    float p[3], r, a[3], B[9] = {0.f};
+    sphere(nd, p, r);
+    if (nd >= 0) {
+      for (int k = 0; k < 3; ++k) a[k] = node[size_t(nd)].a[k];
+      for (int k = 0; k < 9; ++k) B[k] = node[size_t(nd)].B[k];
+    } else {
+      for (int k = 0; k < 3; ++k) a[k] = leaf[size_t(~nd)].a[k];
+    }
+    const float d[3] = {p[0] - x[0], p[1] - x[1], p[2] - x[2]};
+    const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const float ri = 1.0f / std::sqrt(r2), ri2 = ri * ri, inv = ri2 * ri * inv4pi;
+    float rbr = 0.f;
+    for (int i = 0; i < 3; ++i) rbr += d[i] * (B[3 * i] * d[0] + B[3 * i + 1] * d[1] + B[3 * i + 2] * d[2]);
+    return inv * ((a[0] * d[0] + a[1] * d[1] + a[2] * d[2] + (B[0] + B[4] + B[8])) - 3.0f * ri2 * rbr);
+  };
+  auto solid_angle = [&](int li, const float* x) -> float {  // Van Oosterom-Strackee
+    const float* v = leaf[size_t(li)].v;
+    float A[3], Bv[3], Cv[3];
+    for (int k = 0; k < 3; ++k) {
+      A[k] = v[k] - x[k];
+      Bv[k] = v[3 + k] - x[k];
+      Cv[k] = v[6 + k] - x[k];
+    }
+    auto dot = [](const float* u, const float* w) { return u[0] * w[0] + u[1] * w[1] + u[2] * w[2]; };
+    const float la = std::sqrt(dot(A, A)), lb = std::sqrt(dot(Bv, Bv)), lc = std::sqrt(dot(Cv, Cv));
+    const float bc[3] = {Bv[1] * Cv[2] - Bv[2] * Cv[1], Bv[2] * Cv[0] - Bv[0] * Cv[2], Bv[0] * Cv[1] - Bv[1] * Cv[0]};
+    const float num = dot(A, bc);
+    const float den = la * lb * lc + dot(A, Bv) * lc + dot(Bv, Cv) * la + dot(Cv, A) * lb;
+    return num == 0.f ? 0.f : 2.0f * std::atan2(num, den) * inv4pi;
+  };
   double visits = 0, far = 0, exact = 0;
 #pragma omp parallel for schedule(dynamic, 64) reduction(+ : visits, far, exact)
   for (int64_t w = 0; w < nw; ++w) {
     const float* q = W + 96 * w;
-    std::vector<int> st{root};
+    double sum[32] = {0.0};
+    std::vector<int> st{root}, below;
     while (!st.empty()) {
       const int nd = st.back();
       st.pop_back();
@@ -349,15 +402,34 @@ int main(int argc, char** argv) {
       }
       if (all_far) {
         far += 1;
-      } else if (nd < 0) {
-        exact += 1;
-      } else if (node[size_t(nd)].ntri <= leafmax) {
-        exact += node[size_t(nd)].ntri;
+        if (!value.empty())
+          for (int l = 0; l < 32; ++l) sum[l] += far_field(nd, q + 3 * l);
+      } else if (nd < 0 || node[size_t(nd)].ntri <= leafmax) {
+        below.assign(1, nd);
+        while (!below.empty()) {  // the triangles below, exactly
+          const int c = below.back();
+          below.pop_back();
+          if (c >= 0) {
+            below.push_back(node[size_t(c)].c0);
+            below.push_back(node[size_t(c)].c1);
+            continue;
+          }
+          exact += 1;
+          if (!value.empty())
+            for (int l = 0; l < 32; ++l) sum[l] += solid_angle(~c, q + 3 * l);
+        }
       } else {
         st.push_back(node[size_t(nd)].c1);
         st.push_back(node[size_t(nd)].c0);
       }
     }
+    if (!value.empty())
+      for (int l = 0; l < 32; ++l) value[size_t(32 * w + l)] = float(sum[l]);
+  }
+  if (!value.empty()) {
+    FILE* f = fopen(argv[7], "wb");
+    if (!f || fwrite(value.data(), sizeof(float), value.size(), f) != value.size()) return 4;
+    fclose(f);
   }
   printf("S %d leafmax %d radius %d: warps %lld, per warp: node visits %.1f, far-field %.1f, exact %.1f, "
          "FLOP per lane %.0f\n",
