@@ -142,3 +142,43 @@ def test_culled_pairs_never_lower_the_minimum():
         tight += int((cull & (d2 < F(1.25) * cur)).sum())
     # the property is exercised, and on pairs where the margin is thin
     assert culled_ever > 0.25 * checked and tight > 0.01 * checked, (culled_ever, tight, checked)
+
+
+def test_cull_test_is_monotone_in_the_bound():
+    """cull_coeffs keeps a sub-triangle eligible only while 132 c (2 c R^2 +
+    E0) <= 1/2, which makes lb - 33 (c2 lb + E0)^2 grow with lb over the
+    widened box: a pair culled at a bound lb is culled at every larger bound
+    against the same running minimum.  Checked in float32 with the kernel's
+    operations over random eligible sub-triangles, bounds in [0, R^2] and
+    minima at the smaller bound's threshold."""
+    rng = np.random.default_rng(11)
+    h = F(0.002)
+    inv_h = F(1.0) / h
+    n = 400_000
+    tri = triangles(rng, n)
+    a, b, c = tri[:, 0], tri[:, 1], tri[:, 2]
+    mn, mx = np.minimum(np.minimum(a, b), c), np.maximum(np.maximum(a, b), c)
+    lo = np.floor(mn * inv_h).astype(np.int64) - 3
+    hi = np.ceil(mx * inv_h).astype(np.int64) + 3
+    ext = (hi - lo).astype(F)
+    R = (h * (np.sqrt(dot3(ext, ext)) + F(2.0))).astype(F)
+    gm = h * (np.maximum(np.abs(lo), np.abs(hi)).max(axis=1) + 1).astype(F)
+    M = np.maximum(gm, np.abs(tri).reshape(n, 9).max(axis=1)).astype(F)
+    c2, e0 = cull_coeffs(a, b, c, R, M)
+    ok = np.isfinite(c2)
+    c2, e0, R = c2[ok], e0[ok], R[ok]
+    lb1 = (rng.random(len(R)) * R * R).astype(F)
+    lb2 = (lb1 + rng.random(len(R)) * (R * R - lb1)).astype(F)
+    with np.errstate(all="ignore"):
+        t1 = fmaf(c2, lb1, e0)
+        t2 = fmaf(c2, lb2, e0)
+        k = F(1.03125)
+        extra1 = F(33.0) * (t1 * t1)
+        cur = ((lb1.astype(np.float64) - extra1.astype(np.float64)) / 1.03125).astype(F)
+        for _ in range(4):  # the largest minimum the test culls against at lb1
+            bad = ~(lb1 > fmaf(cur, np.full_like(cur, k), extra1))
+            cur = np.where(bad, np.nextafter(cur, F(-np.inf)), cur)
+        cull1 = (cur > 0) & (lb1 > fmaf(cur, np.full_like(cur, k), extra1))
+        cull2 = lb2 > fmaf(cur, np.full_like(cur, k), F(33.0) * (t2 * t2))
+    assert cull1.sum() > 0.3 * len(cur)
+    assert np.all(cull2[cull1])
