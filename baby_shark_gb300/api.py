@@ -390,7 +390,10 @@ class WindingNumbers:
         return WindingNumbers(out, ctx)
 
     def approximate(self, points, accuracy_scale=2.0):
-        """Winding numbers (float32) of an (n, 3) array of points."""
+        """Winding numbers (float32) of an (n, 3) array of points
+        (WindingNumbers::approximate, aabb_tree.rs:654-660).  From 2^20
+        points on, the library traverses them in Morton order and returns the
+        values in the given order."""
         import torch
         p = torch.from_numpy(np.ascontiguousarray(points, np.float32).reshape(-1, 3)).cuda()
         out = torch.empty(p.shape[0], dtype=torch.float32, device=p.device)
