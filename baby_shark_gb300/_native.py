@@ -81,7 +81,7 @@ SIGNATURES = {
     "bs_marching_cubes": (i32, [vp, vp, f32, vp, u64, C.POINTER(u64)]),
     "bs_dual_contour_qef": (i32, [vp, vp, f32, vp, u64, C.POINTER(u64)]),
     "bs_dual_contour": (i32, [vp, vp, f32, vp, u64, C.POINTER(u64)]),
-    "bs_dual_contour_noalloc": (i32, [i32, vp, vp, vp, vp, u64, f32, vp, u64, C.POINTER(u64)]),
+    "bs_dual_contour_noalloc": (i32, [i32, vp, vp, vp, vp, u64, vp, vp, vp, u64, f32, vp, u64, C.POINTER(u64)]),
     "bs_corner_table_from_soup": (i32, [vp, vp, u64, PP]),
     "bs_corner_table_from_dual_contour": (i32, [vp, vp, f32, PP]),
     "bs_corner_table_from_marching_cubes": (i32, [vp, vp, f32, PP]),

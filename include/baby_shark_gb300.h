@@ -315,23 +315,32 @@ bs_status bs_dual_contour(bs_ctx* ctx, bs_volume* v, float voxel_size, float* h_
 /* Dual contouring that allocates nothing, for callers that cannot allocate
  * device memory at call time (a host that carved all device memory up front,
  * a real-time loop that must not enter the driver's allocator, a plugin whose
- * host owns every allocation).  No counterpart in the reference: it is
- * bs_dual_contour on caller-owned device buffers.  Inputs: the leaves of a
- * volume as exported (d_origins int32[3*n], d_values float[512*n], d_masks
- * uint32[16*n]) in device memory of `device`; output: up to `capacity`
- * triangles (9 floats each) in d_tris, the count in *n_tris (also when the
- * capacity is too small, which returns BS_ERR_CAPACITY).  Work runs on
- * `stream` (a cudaStream_t, NULL for the legacy default stream) and the call
- * returns after synchronising it.
+ * host owns every allocation).  No counterpart in the reference: it gives the
+ * triangles of bs_dual_contour on caller-owned device buffers.  Inputs, in
+ * device memory of `device`: the leaves of a volume as bs_volume_export gives
+ * them (d_origins int32[3*n_leaves], d_values float[512*n_leaves], d_masks
+ * uint32[16*n_leaves]) and its active tiles as bs_volume_export_tiles gives
+ * them (d_tile_origins int32[3*n_tiles], d_tile_sizes int32[n_tiles],
+ * d_tile_values float[n_tiles]; n_tiles 0 and NULL arrays for a volume without
+ * tiles).  Passing every tile of the volume gives exactly bs_dual_contour's
+ * triangles; leaving tiles out gives the triangles of a volume without them.
+ * Output: up to `capacity` triangles (9 floats each) in d_tris, the count in
+ * *n_tris (also when the capacity is too small, which returns
+ * BS_ERR_CAPACITY).  Work runs on `stream` (a cudaStream_t, NULL for the
+ * legacy default stream) and the call returns after synchronising it; the
+ * calling thread's current device is restored before the call returns.
  * Working memory is one static 32 MiB device array per GPU, held from module
- * load until exit; limits: 2048 leaves, 393216 sign-change edges, 393216
- * vertex cells; larger inputs return BS_ERR_CAPACITY.  All calls on a device
- * share that array: calls that overlap on the GPU race and must be
- * serialised.  The first call on a device resolves the array's address and
- * must come before any stream capture. */
+ * load until exit; limits: 2048 leaves, 2^20 tiles in at most 256 nodes of
+ * 128^3 (8^3 tiles) and 16 nodes of 4096^3 (128^3 tiles), 393216 sign-change
+ * edges and 393216 vertex cells; larger inputs return BS_ERR_CAPACITY.  All
+ * calls on a device share that array: calls that overlap on the GPU race and
+ * must be serialised.  The first call on a device resolves the array's
+ * address and must come before any stream capture; after cudaDeviceReset on
+ * that device the entry point must not be used again in the process. */
 bs_status bs_dual_contour_noalloc(int device, void* stream, const int32_t* d_origins, const float* d_values,
-                                  const uint32_t* d_masks, uint64_t n_leaves, float voxel_size, float* d_tris,
-                                  uint64_t capacity, uint64_t* n_tris);
+                                  const uint32_t* d_masks, uint64_t n_leaves, const int32_t* d_tile_origins,
+                                  const int32_t* d_tile_sizes, const float* d_tile_values, uint64_t n_tiles,
+                                  float voxel_size, float* d_tris, uint64_t capacity, uint64_t* n_tris);
 
 /* ------------------------------------------------------- CornerTable ---- */
 typedef struct bs_corner_table bs_corner_table;

@@ -132,4 +132,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_reference_kats.py /path/to/baby_shark")
+    main(sys.argv[1])
