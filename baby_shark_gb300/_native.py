@@ -23,7 +23,7 @@ PP = C.POINTER(C.c_void_p)
 
 class M2VParams(C.Structure):
     _fields_ = [("voxel_size", C.c_float), ("band_width", C.c_int32), ("wn_beta", C.c_float),
-                ("wn_threshold", C.c_float), ("wn_order", C.c_int32)]
+                ("wn_threshold", C.c_float), ("wn_order", C.c_int32), ("wn_tree", C.c_int32)]
 
 
 SIGNATURES = {
@@ -56,6 +56,7 @@ SIGNATURES = {
     "bs_diag_fp32_peak": (i32, [vp, C.POINTER(C.c_double)]),
     "bs_winding_numbers_exact": (i32, [vp, vp, u64, vp, u64, vp, u64, vp]),
     "bs_winding_numbers_build": (i32, [vp, vp, u64, vp, u64, i32, PP]),
+    "bs_winding_numbers_build_ex": (i32, [vp, vp, u64, vp, u64, i32, i32, PP]),
     "bs_winding_numbers_approximate": (i32, [vp, vp, vp, u64, f32, vp]),
     "bs_winding_numbers_free": (i32, [vp]),
     "bs_m2v_params_default": (None, [C.POINTER(M2VParams)]),

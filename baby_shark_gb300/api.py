@@ -315,8 +315,20 @@ class MeshToVolume:
         return self.with_narrow_band_width(width)
 
     def with_winding_number_order(self, order):
-        """Far-field order of the sign pass: 2 as the reference, or 3 (extension)."""
+        """Far-field order of the sign pass: 2 as the reference, or 3 (an
+        extension, evaluated over the library's own tree)."""
         self.params.wn_order = int(order)
+        if int(order) == 3:
+            self.params.wn_tree = 1
+        return self
+
+    def with_sign_tree(self, tree):
+        """Tree of the sign pass: "reference" (default; the reference's SAH
+        tree and summation order, bit-exact signs) or "fast" (the library's
+        PLOC tree with a warp-coherent traversal)."""
+        if tree not in ("reference", "fast"):
+            raise ValueError("tree must be 'reference' or 'fast'")
+        self.params.wn_tree = 0 if tree == "reference" else 1
         return self
 
     def convert(self, mesh):
@@ -377,7 +389,10 @@ class WindingNumbers:
             self.h = None
 
     @staticmethod
-    def from_mesh(mesh, order=2, ctx=None):
+    def from_mesh(mesh, order=2, ctx=None, tree="fast"):
+        """tree="reference": the reference's own SAH tree, traversed once per
+        point in its summation order (order 2 only); "fast": the library's
+        PLOC tree with warp-coherent traversal."""
         import torch
         ctx = ctx or default_context()
         v, f = _mesh_arrays(mesh)
@@ -385,8 +400,10 @@ class WindingNumbers:
         df = torch.from_numpy(f.astype(np.int32)).cuda()
         torch.cuda.synchronize()
         out = C.c_void_p()
-        N.check(N.load().bs_winding_numbers_build(ctx.h, dv.data_ptr(), len(v), df.data_ptr(), len(f), int(order),
-                                                  C.byref(out)), ctx.h)
+        if tree not in ("reference", "fast"):
+            raise ValueError("tree must be 'reference' or 'fast'")
+        N.check(N.load().bs_winding_numbers_build_ex(ctx.h, dv.data_ptr(), len(v), df.data_ptr(), len(f), int(order),
+                                                     0 if tree == "reference" else 1, C.byref(out)), ctx.h)
         return WindingNumbers(out, ctx)
 
     def approximate(self, points, accuracy_scale=2.0):

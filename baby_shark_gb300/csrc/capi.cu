@@ -243,6 +243,7 @@ void bs_m2v_params_default(bs_m2v_params* p) {
   p->wn_beta = 2.0f;      // mesh_to_volume.rs:264
   p->wn_threshold = 0.2f; // mesh_to_volume.rs:266
   p->wn_order = 2;
+  p->wn_tree = 0;         // the reference's tree and summation order
 }
 
 bs_status bs_mesh_to_volume_device(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri,

@@ -22,9 +22,11 @@
 #include <climits>
 #include <cmath>
 #include <exception>
+#include <memory>
 #include <vector>
 
 #include "bs_internal.cuh"
+#include "ref_tree.cuh"
 
 namespace bs {
 
@@ -661,6 +663,31 @@ __global__ void k_brick_popcount(const uint32_t* __restrict__ masks, uint64_t nb
 #pragma unroll
   for (int w = 0; w < 16; ++w) c += __popc(masks[b * 16 + w]);
   cnt[b] = c;
+}
+
+// Bricks whose every candidate distance is NaN (the closest-point formula
+// divides 0 by 0 on some degenerate sub-triangles) hold no active voxel; the
+// reference inserts only distances below the running value
+// (mesh_to_volume.rs:183-190), so it never creates their leaves.  keep[b]:
+// brick b has an active voxel (keep[nb] = 0 for the scan's total).
+__global__ void k_brick_keep(const uint32_t* __restrict__ cnt, uint64_t nb, uint32_t* __restrict__ keep) {
+  const uint64_t b = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (b <= nb) keep[b] = (b < nb && cnt[b] > 0) ? 1u : 0u;
+}
+__global__ void k_brick_compact(const uint32_t* __restrict__ keep, const uint32_t* __restrict__ pos, uint64_t nb,
+                                const int4* __restrict__ org, const float* __restrict__ val,
+                                const uint32_t* __restrict__ msk, int4* __restrict__ org2, float* __restrict__ val2,
+                                uint32_t* __restrict__ msk2) {
+  const uint64_t b = blockIdx.x;
+  if (b >= nb || !keep[b]) return;
+  const uint64_t d = pos[b];
+  if (threadIdx.x == 0) org2[d] = org[b];
+  for (int k = threadIdx.x; k < 512; k += blockDim.x) val2[d * 512 + k] = val[b * 512 + k];
+  if (threadIdx.x < 16) msk2[d * 16 + threadIdx.x] = msk[b * 16 + threadIdx.x];
+}
+__global__ void k_remap_base(uint32_t* __restrict__ base, int K, const uint32_t* __restrict__ pos) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m <= K) base[m] = pos[base[m]];
 }
 
 // One warp per brick; active voxels are listed in Morton order inside the
@@ -1785,6 +1812,10 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
     if (!(p.voxel_size > 0.f) || !std::isfinite(p.voxel_size)) fail(BS_ERR_INVALID_ARG, "voxel_size must be > 0");
     if (p.band_width < 0 || p.band_width > 1000000) fail(BS_ERR_INVALID_ARG, "band_width out of range");
     if (p.wn_order != 2 && p.wn_order != 3) fail(BS_ERR_INVALID_ARG, "wn_order must be 2 or 3");
+    if (p.wn_tree != 0 && p.wn_tree != 1) fail(BS_ERR_INVALID_ARG, "wn_tree must be 0 or 1");
+    if (p.wn_tree == 0 && p.wn_order != 2)
+      fail(BS_ERR_INVALID_ARG, "the reference's tree has the order-2 far field only (order 3 needs wn_tree 1)");
+    if (p.wn_tree != params[0].wn_tree) fail(BS_ERR_INVALID_ARG, "all meshes of a batch need the same wn_tree");
     if (n_tri[m]) {
       MeshInfo q{};
       q.h = p.voxel_size;
@@ -1897,7 +1928,8 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
     q_pairs[m] = hst[m].n_pairs;
   }
   check_limit(q_pairs, which, K_all, 4294967296.0, "more than 2^32 brick/sub-triangle pairs");
-  const uint64_t nb = nb_np[0], np = nb_np[1];
+  uint64_t nb = nb_np[0];
+  const uint64_t np = nb_np[1];
   if (nb >= (1ull << 23)) {  // active voxels are listed as brick << 9 | voxel in 32 bits
     std::vector<uint32_t> lb(K + 1);
     read_back(ctx, lb.data(), leaf_base.p, (K + 1) * sizeof(uint32_t));
@@ -1937,16 +1969,43 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   // one tree per mesh over its original triangles, built on the side stream
   // while the distance pass runs (the build's own syncs wait for it alone)
   const bool any3 = std::any_of(mi.begin(), mi.end(), [](const MeshInfo& q) { return q.order >= 3; });
+  // wn_tree 0: the reference's SAH tree, traversed per voxel in its summation
+  // order (ref_tree.cu); 1: this library's PLOC tree, traversed per warp
+  const bool ref_tree = params[size_t(which[0])].wn_tree == 0;
   DBuf<float4> leaf, inode, leaf3, inode3;
+  RefTrees rt;
   {
     SideStream side(ctx);
     BS_CUDA(cudaStreamWaitEvent(ctx->stream, gathered.e, 0));
-    build_trees(ctx, T.p, nt, K, d_tb.p, d_ib.p, st.p, any3, leaf, inode, leaf3, inode3);
+    if (ref_tree)
+      build_ref_trees(ctx, T.p, nt, K, tri_base.data(), rt);
+    else
+      build_trees(ctx, T.p, nt, K, d_tb.p, d_ib.p, st.p, any3, leaf, inode, leaf3, inode3);
     BS_CUDA(cudaEventRecord(built.e, ctx->stream));
   }
 
   DBuf<uint32_t> vc(ctx, nb + 1), voff(ctx, nb + 1);
   BS_KERNEL(ctx, "k_brick_popcount", (k_brick_popcount<<<blocks(nb + 1, 256), 256, 0, s>>>(masks.p, nb, vc.p)));
+  {
+    DBuf<uint32_t> keep(ctx, nb + 1), kpos(ctx, nb + 1);
+    BS_KERNEL(ctx, "k_brick_keep", (k_brick_keep<<<blocks(nb + 1, 256), 256, 0, s>>>(vc.p, nb, keep.p)));
+    exclusive_scan(ctx, keep.p, kpos.p, nb + 1);
+    uint32_t kept = 0;
+    read_back(ctx, &kept, kpos.p + nb, sizeof kept);
+    if (kept < nb) {
+      DBuf<int4> o2(ctx, kept);
+      DBuf<float> v2(ctx, uint64_t(kept) * 512);
+      DBuf<uint32_t> m2(ctx, uint64_t(kept) * 16);
+      BS_KERNEL(ctx, "k_brick_compact", (k_brick_compact<<<unsigned(nb), 128, 0, s>>>(keep.p, kpos.p, nb, origins.p, values.p, masks.p,
+                                                                                  o2.p, v2.p, m2.p)));
+      BS_KERNEL(ctx, "k_remap_base", (k_remap_base<<<blocks(K + 1, 128), 128, 0, s>>>(leaf_base.p, K, kpos.p)));
+      origins = std::move(o2);
+      values = std::move(v2);
+      masks = std::move(m2);
+      nb = kept;
+      BS_KERNEL(ctx, "k_brick_popcount", (k_brick_popcount<<<blocks(nb + 1, 256), 256, 0, s>>>(masks.p, nb, vc.p)));
+    }
+  }
   exclusive_scan(ctx, vc.p, voff.p, nb + 1);
   BS_KERNEL(ctx, "k_act_starts", (k_act_starts<<<blocks(K + 1, 128), 128, 0, s>>>(voff.p, leaf_base.p, K, act_base.p)));
   std::vector<uint32_t> h_leaf_base(K + 1), h_act_base(K + 1);
@@ -1958,14 +2017,25 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   DBuf<uint32_t> d_wb(ctx, K + 1);
   BS_CUDA(cudaMemcpyAsync(d_wb.p, warp_base.data(), (K + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
   DBuf<uint32_t> act(ctx, std::max<uint64_t>(na, 1));
-  BS_KERNEL(ctx, "k_emit_active", (k_emit_active<<<blocks(nb * 32, 256), 256, 0, s>>>(masks.p, voff.p, nb, act.p)));
+  if (nb) BS_KERNEL(ctx, "k_emit_active", (k_emit_active<<<blocks(nb * 32, 256), 256, 0, s>>>(masks.p, voff.p, nb, act.p)));
   vc.reset();
   voff.reset();
 
   // join the tree build; the triangles are freed after it
   BS_CUDA(cudaStreamWaitEvent(s, built.e, 0));
   T.reset();
-  if (na > 0) {
+  unsigned long long rt_cnt[4] = {0, 0, 0, 0};
+  if (na > 0 && ref_tree) {
+    std::vector<RefSignMesh> rm(K);
+    for (int m = 0; m < K; ++m) rm[m] = RefSignMesh{rt.h_roots[m], mi[m].h, mi[m].beta, mi[m].thresh};
+    DBuf<RefSignMesh> d_rm(ctx, K);
+    DBuf<unsigned long long> d_cnt(ctx, 4);
+    BS_CUDA(cudaMemcpyAsync(d_rm.p, rm.data(), K * sizeof(RefSignMesh), cudaMemcpyHostToDevice, s));
+    BS_CUDA(cudaMemsetAsync(d_cnt.p, 0, 4 * sizeof(unsigned long long), s));
+    ref_tree_sign(ctx, rt, act.p, act_base.p, d_wb.p, warp_base[K], K, d_rm.p, origins.p, values.p, d_cnt.p);
+    read_back(ctx, rt_cnt, d_cnt.p, sizeof rt_cnt);
+    if (rt_cnt[3]) fail(BS_ERR_CAPACITY, "winding-number traversal stack overflow");
+  } else if (na > 0) {
     const uint64_t n_warps = warp_base[K];
 #define BS_WN1(O, WP, I3, L3)                                                                                   \
   BS_KERNEL(ctx, "k_wn_sign", (k_wn_sign<O, WP><<<blocks(na, 32 * WP), 32 * WP, 0, s>>>(                      \
@@ -2006,6 +2076,11 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
     visits += hst[m].wn_visits;
     far += hst[m].wn_far;
     exact += hst[m].wn_exact;
+  }
+  if (ref_tree) {  // per voxel rather than per warp
+    visits = rt_cnt[0];
+    far = rt_cnt[1];
+    exact = rt_cnt[2];
   }
   ctx->last_stats[0] = nt;
   ctx->last_stats[1] = ns;
@@ -2096,21 +2171,25 @@ struct bs_wn_tree {
     bs::dfree(ctx, inode);
     bs::dfree(ctx, leaf3);
     bs::dfree(ctx, inode3);
+    delete ref;
     bs_ctx_release(ctx);
   }
   bs_ctx* ctx;
   uint64_t nt = 0;
   int order = 2;
   float4 *leaf = nullptr, *inode = nullptr, *leaf3 = nullptr, *inode3 = nullptr;
+  bs::RefTrees* ref = nullptr;  // the reference's tree (tree kind 0)
 };
 
 namespace bs {
 
 static bs_wn_tree* wn_tree_build(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
-                                 int order) {
+                                 int order, int kind = 1) {
   if (nt == 0) fail(BS_ERR_EMPTY, "mesh has no triangles");
   if (nt >= (1ull << 31)) fail(BS_ERR_CAPACITY, "more than 2^31 triangles");
   if (order != 2 && order != 3) fail(BS_ERR_INVALID_ARG, "order must be 2 or 3");
+  if (kind != 0 && kind != 1) fail(BS_ERR_INVALID_ARG, "tree must be 0 or 1");
+  if (kind == 0 && order != 2) fail(BS_ERR_INVALID_ARG, "the reference's tree has the order-2 far field only");
   cudaStream_t s = ctx->stream;
   DBuf<float4> T(ctx, 3 * nt);
   DBuf<M2VStats> st(ctx, 1);
@@ -2126,6 +2205,18 @@ static bs_wn_tree* wn_tree_build(bs_ctx* ctx, const float* d_xyz, uint64_t nv, c
   BS_CUDA(cudaMemcpyAsync(d_tb.p, tb, sizeof tb, cudaMemcpyHostToDevice, s));
   BS_CUDA(cudaMemcpyAsync(d_ib.p, ibase, sizeof ibase, cudaMemcpyHostToDevice, s));
   DBuf<float4> leaf, inode, leaf3, inode3;
+  if (kind == 0) {
+    M2VStats hs;
+    read_back(ctx, &hs, st.p, sizeof hs);
+    if (hs.error == 1) fail(BS_ERR_INVALID_ARG, "triangle vertex index out of range");
+    std::unique_ptr<RefTrees> rt(new RefTrees);
+    build_ref_trees(ctx, T.p, nt, 1, tb, *rt);
+    bs_wn_tree* t = new bs_wn_tree(ctx);
+    t->nt = nt;
+    t->order = 2;
+    t->ref = rt.release();
+    return t;
+  }
   build_trees(ctx, T.p, nt, 1, d_tb.p, d_ib.p, st.p, order >= 3, leaf, inode, leaf3, inode3);
   M2VStats hs;
   read_back(ctx, &hs, st.p, sizeof hs);
@@ -2144,6 +2235,18 @@ static void wn_tree_approximate(bs_ctx* ctx, const bs_wn_tree* t, const float* d
                                 float* d_out) {
   if (np == 0) return;
   cudaStream_t s = ctx->stream;
+  if (t->ref) {  // one traversal per point, in the caller's order
+    DBuf<unsigned long long> cnt(ctx, 4);
+    BS_CUDA(cudaMemsetAsync(cnt.p, 0, 4 * sizeof(unsigned long long), s));
+    ref_tree_points(ctx, *t->ref, d_pts, np, beta, d_out, cnt.p);
+    unsigned long long h[4];
+    read_back(ctx, h, cnt.p, sizeof h);
+    if (h[3]) fail(BS_ERR_CAPACITY, "winding-number traversal stack overflow");
+    ctx->last_stats[6] = h[0];
+    ctx->last_stats[7] = (h[1] & 0xffffffffull) | (h[2] << 32);
+    ctx->last_stats[8] = BS_STATS_WINDING_NUMBERS;
+    return;
+  }
   DBuf<M2VStats> st(ctx, 1);
   BS_CUDA(cudaMemsetAsync(st.p, 0, sizeof(M2VStats), s));
   // from 2^20 points on, traverse a Morton-sorted copy and scatter back
@@ -2193,6 +2296,22 @@ bs_status bs_winding_numbers_build(bs_ctx* ctx, const float* d_xyz, uint64_t nv,
   try {
     BS_CUDA(cudaSetDevice(ctx->device));
     *out = bs::wn_tree_build(ctx, d_xyz, nv, d_tri, nt, order);
+    return BS_OK;
+  } catch (const bs::Error& e) {
+    ctx->last_error = e.msg;
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    return BS_ERR_OOM;
+  }
+}
+
+bs_status bs_winding_numbers_build_ex(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri,
+                                      uint64_t nt, int order, int tree, bs_wn_tree** out) {
+  if (!ctx || !out || (nt && (!d_xyz || !d_tri))) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  try {
+    BS_CUDA(cudaSetDevice(ctx->device));
+    *out = bs::wn_tree_build(ctx, d_xyz, nv, d_tri, nt, order, tree);
     return BS_OK;
   } catch (const bs::Error& e) {
     ctx->last_error = e.msg;

@@ -121,10 +121,18 @@ typedef struct bs_m2v_params {
   float wn_beta;       /* far-field accuracy scale; the reference uses 2.0 (mesh_to_volume.rs:264) */
   float wn_threshold;  /* wn < threshold => outside; the reference uses 0.2 (mesh_to_volume.rs:266) */
   int32_t wn_order;    /* far-field expansion order: 2 as the reference (aabb_tree.rs:662-691), or 3
-                          (the third-order term the reference leaves undone, aabb_tree.rs:706) */
+                          (the third-order term the reference leaves undone, aabb_tree.rs:706; needs
+                          wn_tree 1) */
+  int32_t wn_tree;     /* 0: the reference's own tree — the top-down SAH build of AABBTree::top_down::<Area>
+                          with 3 triangles per leaf (aabb_tree.rs:118-199, 422-514, 636-644), one traversal
+                          per voxel summing wn(left) + wn(right) as fast_wn recurses (aabb_tree.rs:662-691):
+                          signs equal the reference's bit for bit.  1: this library's PLOC tree with a
+                          warp-coherent traversal (faster; signs differ only where the winding number is
+                          within the far-field approximation error of the threshold).  All meshes of a
+                          batch use the same value. */
 } bs_m2v_params;
 
-/* Fills `p` with the reference's defaults (voxel 1, band 0, beta 2, threshold 0.2). */
+/* Fills `p` with the reference's defaults (voxel 1, band 0, beta 2, threshold 0.2, the reference's tree). */
 void bs_m2v_params_default(bs_m2v_params* p);
 
 /* MeshToVolume::convert (mesh_to_volume.rs:52-73) on an indexed triangle mesh
@@ -205,6 +213,15 @@ typedef struct bs_wn_tree bs_wn_tree;
  * reference's SAH split. */
 bs_status bs_winding_numbers_build(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
                                    int order, bs_wn_tree** out);
+/* WindingNumbers::from_mesh with a choice of tree: tree 0 is the reference's
+ * own (AABBTree::top_down::<Area> with 3 triangles per leaf,
+ * aabb_tree.rs:636-644; order 2 only), and bs_winding_numbers_approximate then
+ * traverses it once per point, summing as fast_wn recurses
+ * (aabb_tree.rs:662-691), so values equal the reference's float32 results bit
+ * for bit but for last-place differences of atan2f; tree 1 is the PLOC tree
+ * of bs_winding_numbers_build. */
+bs_status bs_winding_numbers_build_ex(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri,
+                                      uint64_t nt, int order, int tree, bs_wn_tree** out);
 /* WindingNumbers::approximate(point, accuracy_scale) (aabb_tree.rs:654-660) at
  * n_points device points (3 floats each) into d_out; beta = accuracy_scale.
  * From 2^20 points on the call traverses a Morton-sorted copy of the points
