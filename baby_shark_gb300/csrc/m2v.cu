@@ -1977,10 +1977,13 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   {
     SideStream side(ctx);
     BS_CUDA(cudaStreamWaitEvent(ctx->stream, gathered.e, 0));
-    if (ref_tree)
-      build_ref_trees(ctx, T.p, nt, K, tri_base.data(), rt);
-    else
+    if (ref_tree) {
+      std::vector<float> betas(K);
+      for (int m = 0; m < K; ++m) betas[m] = mi[m].beta;
+      build_ref_trees(ctx, T.p, nt, K, tri_base.data(), betas, rt);
+    } else {
       build_trees(ctx, T.p, nt, K, d_tb.p, d_ib.p, st.p, any3, leaf, inode, leaf3, inode3);
+    }
     BS_CUDA(cudaEventRecord(built.e, ctx->stream));
   }
 
@@ -2210,7 +2213,7 @@ static bs_wn_tree* wn_tree_build(bs_ctx* ctx, const float* d_xyz, uint64_t nv, c
     read_back(ctx, &hs, st.p, sizeof hs);
     if (hs.error == 1) fail(BS_ERR_INVALID_ARG, "triangle vertex index out of range");
     std::unique_ptr<RefTrees> rt(new RefTrees);
-    build_ref_trees(ctx, T.p, nt, 1, tb, *rt);
+    build_ref_trees(ctx, T.p, nt, 1, tb, std::vector<float>(1, 2.0f), *rt);
     bs_wn_tree* t = new bs_wn_tree(ctx);
     t->nt = nt;
     t->order = 2;
@@ -2231,7 +2234,7 @@ static bs_wn_tree* wn_tree_build(bs_ctx* ctx, const float* d_xyz, uint64_t nv, c
   return t;
 }
 
-static void wn_tree_approximate(bs_ctx* ctx, const bs_wn_tree* t, const float* d_pts, uint64_t np, float beta,
+static void wn_tree_approximate(bs_ctx* ctx, bs_wn_tree* t, const float* d_pts, uint64_t np, float beta,
                                 float* d_out) {
   if (np == 0) return;
   cudaStream_t s = ctx->stream;
@@ -2326,7 +2329,8 @@ bs_status bs_winding_numbers_approximate(bs_ctx* ctx, const bs_wn_tree* t, const
   if (!ctx || !t || t->ctx != ctx || (n_points && (!d_points || !d_out)) || !(beta > 0.f)) return BS_ERR_INVALID_ARG;
   try {
     BS_CUDA(cudaSetDevice(ctx->device));
-    bs::wn_tree_approximate(ctx, t, d_points, n_points, beta, d_out);
+    // the reference tree caches its far thresholds for the last beta (stream-ordered state)
+    bs::wn_tree_approximate(ctx, const_cast<bs_wn_tree*>(t), d_points, n_points, beta, d_out);
     return BS_OK;
   } catch (const bs::Error& e) {
     ctx->last_error = e.msg;

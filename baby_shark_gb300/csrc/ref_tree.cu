@@ -777,9 +777,10 @@ __device__ __forceinline__ Init load_init(const float4* d) {
 // NodeData of compute_node_data (aabb_tree.rs:723-747): dipole centre,
 // radius to the farther box corner, order-1 = area-weighted normal, order-2
 // = o1 - dipole * awn^T.
-__device__ __forceinline__ void store_record(float4* r, const Init& d, F3 dip) {
+__device__ __forceinline__ void store_record(float4* r, float* rad, const Init& d, F3 dip) {
   const F3 a = sub3(d.lo, dip), b = sub3(d.hi, dip);
   const float radius = fsqrt(fmaxf(dot3(a, a), dot3(b, b)));
+  *rad = radius;
   const float aw[3] = {d.awn.x, d.awn.y, d.awn.z}, dp[3] = {dip.x, dip.y, dip.z};
   float o2[9];
   for (int j = 0; j < 3; ++j)
@@ -796,7 +797,8 @@ __device__ __forceinline__ void store_record(float4* r, const Init& d, F3 dip) {
 __global__ void k_rt_refit(uint64_t nt, const uint32_t* __restrict__ leaf_cnt, const float4* __restrict__ tri,
                            const int2* __restrict__ topo, const int* __restrict__ par_i,
                            const int* __restrict__ par_l, int* __restrict__ flags, float4* __restrict__ ld_i,
-                           float4* __restrict__ ld_l, float4* __restrict__ rec_i, float4* __restrict__ rec_l) {
+                           float4* __restrict__ ld_l, float4* __restrict__ rec_i, float4* __restrict__ rec_l,
+                           float* __restrict__ rad_i, float* __restrict__ rad_l) {
   const uint64_t p = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
   if (p >= nt) return;
   const uint32_t c = leaf_cnt[p];
@@ -837,7 +839,7 @@ __global__ void k_rt_refit(uint64_t nt, const uint32_t* __restrict__ leaf_cnt, c
   }
   F3 dip = f3(fdiv(d.awc.x, d.area), fdiv(d.awc.y, d.area), fdiv(d.awc.z, d.area));
   store_init(ld_l + 6 * p, d);
-  store_record(rec_l + 4 * p, d, dip);
+  store_record(rec_l + 4 * p, rad_l + p, d, dip);
   __threadfence();
   int par = par_l[p];
   for (int guard = 0; par >= 0 && guard <= MAX_DEPTH + 1; ++guard) {
@@ -856,10 +858,39 @@ __global__ void k_rt_refit(uint64_t nt, const uint32_t* __restrict__ leaf_cnt, c
     const F3 s = add3(l.awc, r.awc);
     dip = f3(fdiv(s.x, m.area), fdiv(s.y, m.area), fdiv(s.z, m.area));
     store_init(ld_i + 6 * uint64_t(par), m);
-    store_record(rec_i + 4 * uint64_t(par), m, dip);
+    store_record(rec_i + 4 * uint64_t(par), rad_i + par, m, dip);
     __threadfence();
     par = __ldcg(par_i + par);
   }
+}
+
+// The far test |q - p| > beta r (aabb_tree.rs:665-666) without the square
+// root: for t = RN(r * beta) >= 0 and t+ the next float above t,
+// RN(sqrt(x)) > t exactly when sqrt(x) exceeds the midpoint m = (t + t+) / 2
+// (sqrt(x) never equals m: m has 25 significant bits, so m^2 is no float),
+// that is when x > m^2, and for a float x when x > RD(m^2).  m^2 is exact in
+// double.  The record's .w holds this threshold for the call's beta.
+__device__ __forceinline__ float far_tau(float radius, float beta) {
+  const float t = fmul(radius, beta);
+  if (t != t) return t;                                   // NaN radius: never far
+  if (t < 0.0f) return -1.0f;                             // every |q - p| exceeds t
+  if (t == __int_as_float(0x7f800000)) return t;          // never far
+  const float tp = nextafterf(t, __int_as_float(0x7f800000));
+  if (tp == __int_as_float(0x7f800000)) return 3.40282347e+38f;  // only an infinite x rounds above
+  const double m = (double(t) + double(tp)) * 0.5;
+  return __double2float_rd(m * m);
+}
+
+// Writes every node's far threshold for its mesh's beta into its record.
+__global__ void k_rt_tau(uint64_t nt, const uint32_t* __restrict__ tb, int K, const float* __restrict__ beta,
+                         const uint32_t* __restrict__ leaf_cnt, const int* __restrict__ flags,
+                         const float* __restrict__ rad_i, const float* __restrict__ rad_l, float4* __restrict__ rec_i,
+                         float4* __restrict__ rec_l) {
+  const uint64_t p = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (p >= nt) return;
+  const float b = beta[K > 1 ? mesh_of(tb, K, p) : 0];
+  if (leaf_cnt[p]) rec_l[4 * p].w = far_tau(rad_l[p], b);
+  if (flags[p] == 2) rec_i[4 * p].w = far_tau(rad_i[p], b);  // internal node p (both children combined)
 }
 
 // ------------------------------------------------------------ traversal ---
@@ -880,8 +911,9 @@ __device__ __forceinline__ float solid_angle(float4 A, float4 Bv, float4 C, F3 q
 // Far field of a node at q (aabb_tree.rs:666-671 with hessians, 803-816):
 // r = p - q, the order-1 term a . r / (4 pi |r|^3) and the Frobenius product
 // of the order-2 coefficients with I / (4 pi |r|^3) - 3 r r^T / (4 pi |r|^5).
-__device__ __forceinline__ float far_field(const float4* R, float4 P, F3 q, float r2, float r1) {
+__device__ __forceinline__ float far_field(const float4* R, float4 P, F3 q, float r2) {
   const float4 c1 = R[1], c2 = R[2], c3 = R[3];
+  const float r1 = fsqrt(r2);  // |q - p| (norm, aabb_tree.rs:665; r1 of hessians, 806)
   const float r[3] = {fsub(P.x, q.x), fsub(P.y, q.y), fsub(P.z, q.z)};
   const float r3 = fmul(r2, r1);
   const float inv = fdiv(1.0f, fmul(FOUR_PI_F, r3));
@@ -906,96 +938,122 @@ struct Counts {
 
 // fast_wn (aabb_tree.rs:662-691) at the 32 points of a warp, each lane
 // with its own cut of the tree and its own sums in the recursion's order.
-// The warp walks the union of the lanes' recursions depth first: at a node,
-// the lanes still inside it (`active`) take its far field when it is far for
-// them, its triangles when it is a leaf, and the rest open it, so the warp
-// descends only for those.  A lane's value for a node is therefore exactly
-// its recursion's wn(node): far field, leaf sum, or wn(left) + wn(right)
-// added when the right child returns.  Node records are read once per warp
+// The warp walks the union of the lanes' recursions depth first.  Each step
+// opens one node for the lanes that open it and tests both children for
+// them: a lane takes a child's far field when it is far for it, a leaf
+// child's triangles, and opens the others, so the warp descends only where
+// some lane opens a child.  A lane's value for a node is therefore exactly
+// its recursion's wn(node) — far field, leaf sum, or wn(left) + wn(right)
+// added once both children are known.  Node records are read once per warp
 // (uniform addresses); only the far-field and leaf arithmetic diverges.
-// Per level of the walk the warp keeps the right child, the lanes that
-// opened the node and the lanes that were inside it (shared memory); each
-// lane keeps the pending left sum and, for lanes that did not open the node,
-// the value they took there.
+// Per opened level the warp keeps the right child, the lanes opening each
+// child and the lanes that opened the node (shared memory); each lane keeps
+// its two child values.
 struct WarpStack {
   int right[STACK];
-  unsigned open[STACK];
+  unsigned open_l[STACK], open_r[STACK];
   unsigned act[STACK];
 };
 
+// The lanes in `lanes` meet `node`: far field or leaf sum into v; returns the
+// lanes that open it (an internal node near for them).
+__device__ __forceinline__ unsigned resolve(int node, unsigned lanes, F3 q, const float4* __restrict__ rec_i,
+                                            const float4* __restrict__ rec_l, const uint32_t* __restrict__ leaf_cnt,
+                                            const float4* __restrict__ tri, float& v, Counts& cnt) {
+  const unsigned me = 1u << (threadIdx.x & 31);
+  const float4* R = node >= 0 ? rec_i + 4 * node : rec_l + 4 * (~node);
+  const float4 P = __ldg(R);
+  const float dx = fsub(q.x, P.x), dy = fsub(q.y, P.y), dz = fsub(q.z, P.z);
+  const float r2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
+  const unsigned farm = __ballot_sync(FULL, r2 > P.w) & lanes;  // |q - p| > beta r
+  const unsigned rest = lanes & ~farm;
+  ++cnt.visits;
+  if (farm & me) {
+    ++cnt.far;
+    v = far_field(R, P, q, r2);
+  }
+  if (node >= 0) return rest;
+  if (rest & me) {
+    const uint32_t p = ~node, c = __ldg(leaf_cnt + p);
+    float w = 0.0f;
+    for (uint32_t k = 0; k < c; ++k)
+      w = fadd(w, solid_angle(__ldg(tri + 3 * (p + k)), __ldg(tri + 3 * (p + k) + 1), __ldg(tri + 3 * (p + k) + 2), q));
+    cnt.exact += c;
+    v = fdiv(w, FOUR_PI_F);  // winding_number (aabb_tree.rs:617-628)
+  }
+  return 0u;
+}
+
 __device__ float ref_wn_warp(F3 q, unsigned valid, int root, const float4* __restrict__ rec_i,
                              const int2* __restrict__ topo, const float4* __restrict__ rec_l,
-                             const uint32_t* __restrict__ leaf_cnt, const float4* __restrict__ tri, float beta,
-                             WarpStack& ws, Counts& cnt) {
+                             const uint32_t* __restrict__ leaf_cnt, const float4* __restrict__ tri, WarpStack& ws,
+                             Counts& cnt) {
   const int lane = threadIdx.x & 31;
   const unsigned me = 1u << lane;
-  float lval[STACK], nval[STACK];
-  unsigned active = valid;
-  int node = root, d = 0;
-  uint64_t phase = 0;  // bit f: the left child of level f has returned
+  float lval[STACK], rval[STACK];
   float v = 0.0f;
+  unsigned open = resolve(root, valid, q, rec_i, rec_l, leaf_cnt, tri, v, cnt);
+  if (!open) return v;
+  const float v_root = v;  // lanes for which the root itself is far (or a leaf)
+  const bool root_open = (open & me) != 0;
+  int node = root, d = 0;
+  uint64_t phase = 0;  // bit f: level f is descending its right child
   for (uint32_t guard = 0; guard < (1u << 30); ++guard) {
-    const float4* R = node >= 0 ? rec_i + 4 * node : rec_l + 4 * (~node);
-    const float4 P = __ldg(R);
-    const float dx = fsub(q.x, P.x), dy = fsub(q.y, P.y), dz = fsub(q.z, P.z);
-    const float r2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
-    const float dist = fsqrt(r2);
-    const unsigned farm = __ballot_sync(FULL, dist > fmul(P.w, beta)) & active;
-    const unsigned rest = active & ~farm;
-    ++cnt.visits;
-    if (farm & me) {
-      ++cnt.far;
-      v = far_field(R, P, q, r2, dist);
-    }
-    if (node < 0) {
-      if (rest & me) {
-        const uint32_t p = ~node, c = __ldg(leaf_cnt + p);
-        float w = 0.0f;
-        for (uint32_t k = 0; k < c; ++k)
-          w = fadd(w, solid_angle(__ldg(tri + 3 * (p + k)), __ldg(tri + 3 * (p + k) + 1),
-                                  __ldg(tri + 3 * (p + k) + 2), q));
-        cnt.exact += c;
-        v = fdiv(w, FOUR_PI_F);  // winding_number (aabb_tree.rs:617-628)
-      }
-    } else if (rest) {
+    // open `node` for the lanes in `open`
+    const int2 ch = __ldg(topo + node);
+    float vl = 0.0f, vr = 0.0f;
+    const unsigned ol = resolve(ch.x, open, q, rec_i, rec_l, leaf_cnt, tri, vl, cnt);
+    const unsigned orr = resolve(ch.y, open, q, rec_i, rec_l, leaf_cnt, tri, vr, cnt);
+    if (ol | orr) {
       if (d >= STACK) {
         cnt.overflow = true;
         return 0.0f;
       }
-      nval[d] = v;  // the value of lanes that did not open this node
-      const int2 ch = __ldg(topo + node);
+      lval[d] = vl;
+      rval[d] = vr;
       __syncwarp();  // every lane has read the entries this push may replace
       if (lane == 0) {
         ws.right[d] = ch.y;
-        ws.open[d] = rest;
-        ws.act[d] = active;
+        ws.open_l[d] = ol;
+        ws.open_r[d] = orr;
+        ws.act[d] = open;
       }
       __syncwarp();
-      phase &= ~(1ull << d);
+      if (ol) {
+        phase &= ~(1ull << d);
+        node = ch.x;
+        open = ol;
+      } else {
+        phase |= 1ull << d;
+        node = ch.y;
+        open = orr;
+      }
       ++d;
-      active = rest;
-      node = ch.x;
       continue;
     }
-    // `node` is done for every lane in `active`: fold it into the pending sums
+    v = fadd(vl, vr);  // left_wn + right_wn
+    // `node` is done for every lane in `open`: fold it into the pending sums
     bool next = false;
     while (d > 0) {
       const int f = d - 1;
-      const unsigned op = ws.open[f];
-      if (!((phase >> f) & 1ull)) {
-        if (op & me) lval[f] = v;
-        phase |= 1ull << f;
-        node = ws.right[f];
-        active = op;
-        next = true;
-        break;
+      if (!((phase >> f) & 1ull)) {  // its left child returned
+        if (ws.open_l[f] & me) lval[f] = v;
+        const unsigned r = ws.open_r[f];
+        if (r) {
+          phase |= 1ull << f;
+          node = ws.right[f];
+          open = r;
+          next = true;
+          break;
+        }
+      } else if (ws.open_r[f] & me) {  // its right child returned
+        rval[f] = v;
       }
-      if (op & me) v = fadd(lval[f], v);  // left_wn + right_wn
-      else v = nval[f];
-      active = ws.act[f];
+      v = fadd(lval[f], rval[f]);  // left_wn + right_wn
+      open = ws.act[f];
       --d;
     }
-    if (!next) return v;
+    if (!next) return root_open ? v : v_root;
   }
   cnt.overflow = true;
   return 0.0f;
@@ -1043,7 +1101,7 @@ __global__ void __launch_bounds__(32 * SIGN_WARPS) k_rt_sign(const uint32_t* __r
   const F3 q = f3(fmul(__int2float_rn(org.x + int(o >> 6)), M.h), fmul(__int2float_rn(org.y + int((o >> 3) & 7)), M.h),
                   fmul(__int2float_rn(org.z + int(o & 7)), M.h));
   Counts c;
-  const float wn = ref_wn_warp(q, __ballot_sync(FULL, ok), M.root, rec_i, topo, rec_l, leaf_cnt, tri, M.beta, ws[w], c);
+  const float wn = ref_wn_warp(q, __ballot_sync(FULL, ok), M.root, rec_i, topo, rec_l, leaf_cnt, tri, ws[w], c);
   if (ok) {
     const float d = values[uint64_t(b) * 512 + o];
     values[uint64_t(b) * 512 + o] = (wn < M.thresh) ? copysignf(d, 1.0f) : copysignf(d, -1.0f);
@@ -1052,7 +1110,7 @@ __global__ void __launch_bounds__(32 * SIGN_WARPS) k_rt_sign(const uint32_t* __r
 }
 
 __global__ void __launch_bounds__(32 * SIGN_WARPS) k_rt_points(const float* __restrict__ pts, uint64_t np, int root,
-                                                               float beta, const float4* __restrict__ rec_i,
+                                                               const float4* __restrict__ rec_i,
                                                                const int2* __restrict__ topo,
                                                                const float4* __restrict__ rec_l,
                                                                const uint32_t* __restrict__ leaf_cnt,
@@ -1067,7 +1125,7 @@ __global__ void __launch_bounds__(32 * SIGN_WARPS) k_rt_points(const float* __re
   const uint64_t j = ok ? i : np - 1;
   const F3 q = f3(pts[3 * j], pts[3 * j + 1], pts[3 * j + 2]);
   Counts c;
-  const float wn = ref_wn_warp(q, __ballot_sync(FULL, ok), root, rec_i, topo, rec_l, leaf_cnt, tri, beta, ws[w], c);
+  const float wn = ref_wn_warp(q, __ballot_sync(FULL, ok), root, rec_i, topo, rec_l, leaf_cnt, tri, ws[w], c);
   if (ok) out[i] = wn;
   flush_counts(c, counters);
 }
@@ -1076,7 +1134,8 @@ inline unsigned nblk(uint64_t n, unsigned t) { return unsigned((n + t - 1) / t);
 
 }  // namespace
 
-void build_ref_trees(bs_ctx* ctx, const float4* T, uint64_t nt, int K, const uint32_t* h_tb, RefTrees& out) {
+void build_ref_trees(bs_ctx* ctx, const float4* T, uint64_t nt, int K, const uint32_t* h_tb,
+                     const std::vector<float>& h_beta, RefTrees& out) {
   if (nt == 0 || K <= 0) fail(BS_ERR_EMPTY, "mesh has no triangles");
   if (nt >= (1ull << 31)) fail(BS_ERR_CAPACITY, "more than 2^31 triangles");
   cudaStream_t s = ctx->stream;
@@ -1168,15 +1227,31 @@ void build_ref_trees(bs_ctx* ctx, const float4* T, uint64_t nt, int K, const uin
   BS_KERNEL(ctx, "k_rt_tri", (k_rt_tri<<<nblk(nt, 256), 256, 0, s>>>(T, perm.p, nt, out.tri.p)));
   out.rec_i = DBuf<float4>(ctx, 4 * nt);
   out.rec_l = DBuf<float4>(ctx, 4 * nt);
+  out.rad_i = DBuf<float>(ctx, nt);
+  out.rad_l = DBuf<float>(ctx, nt);
+  out.flags = DBuf<int>(ctx, nt);
   {
     DBuf<float4> ld_i(ctx, 6 * nt), ld_l(ctx, 6 * nt);
-    DBuf<int> flags(ctx, nt);
-    BS_CUDA(cudaMemsetAsync(flags.p, 0, nt * sizeof(int), s));
-    BS_KERNEL(ctx, "k_rt_refit", (k_rt_refit<<<nblk(nt, 128), 128, 0, s>>>(nt, out.leaf_cnt.p, out.tri.p, out.topo.p, par_i.p, par_l.p, flags.p,
-                                                                         ld_i.p, ld_l.p, out.rec_i.p, out.rec_l.p)));
+    BS_CUDA(cudaMemsetAsync(out.flags.p, 0, nt * sizeof(int), s));
+    BS_KERNEL(ctx, "k_rt_refit", (k_rt_refit<<<nblk(nt, 128), 128, 0, s>>>(nt, out.leaf_cnt.p, out.tri.p, out.topo.p, par_i.p, par_l.p,
+                                                                         out.flags.p, ld_i.p, ld_l.p, out.rec_i.p, out.rec_l.p,
+                                                                         out.rad_i.p, out.rad_l.p)));
     out.h_roots.resize(K);
     read_back(ctx, out.h_roots.data(), out.roots.p, K * sizeof(int));
   }
+  out.tb = std::move(d_tb);
+  out.h_beta.clear();
+  ref_tree_set_beta(ctx, out, h_beta);
+}
+
+void ref_tree_set_beta(bs_ctx* ctx, RefTrees& t, const std::vector<float>& beta) {
+  if (int(beta.size()) != t.K) fail(BS_ERR_INVALID_ARG, "one beta per mesh");
+  if (beta == t.h_beta) return;
+  DBuf<float> d_beta(ctx, t.K);
+  BS_CUDA(cudaMemcpyAsync(d_beta.p, beta.data(), t.K * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  BS_KERNEL(ctx, "k_rt_tau", (k_rt_tau<<<nblk(t.nt, 256), 256, 0, ctx->stream>>>(t.nt, t.tb.p, t.K, d_beta.p, t.leaf_cnt.p, t.flags.p,
+                                                                             t.rad_i.p, t.rad_l.p, t.rec_i.p, t.rec_l.p)));
+  t.h_beta = beta;
 }
 
 void ref_tree_sign(bs_ctx* ctx, const RefTrees& t, const uint32_t* act, const uint32_t* d_act_base,
@@ -1188,11 +1263,12 @@ void ref_tree_sign(bs_ctx* ctx, const RefTrees& t, const uint32_t* act, const ui
                                   t.rec_l.p, t.leaf_cnt.p, t.tri.p, d_counters)));
 }
 
-void ref_tree_points(bs_ctx* ctx, const RefTrees& t, const float* d_pts, uint64_t np, float beta, float* d_out,
+void ref_tree_points(bs_ctx* ctx, RefTrees& t, const float* d_pts, uint64_t np, float beta, float* d_out,
                      unsigned long long* d_counters) {
   if (np == 0) return;
+  ref_tree_set_beta(ctx, t, std::vector<float>(1, beta));
   BS_KERNEL(ctx, "k_rt_points", (k_rt_points<<<nblk(np, 32 * SIGN_WARPS), 32 * SIGN_WARPS, 0, ctx->stream>>>(
-                                    d_pts, np, t.h_roots[0], beta, t.rec_i.p, t.topo.p, t.rec_l.p, t.leaf_cnt.p,
+                                    d_pts, np, t.h_roots[0], t.rec_i.p, t.topo.p, t.rec_l.p, t.leaf_cnt.p,
                                     t.tri.p, d_out, d_counters)));
 }
 
