@@ -54,6 +54,7 @@ SIGNATURES = {
     "bs_ctx_memory": (i32, [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
     "bs_ctx_memory_reset": (i32, [vp, C.c_int]),
     "bs_diag_fp32_peak": (i32, [vp, C.POINTER(C.c_double)]),
+    "bs_diag_check_division": (i32, [vp, C.c_uint32, C.POINTER(u64), C.POINTER(u64)]),
     "bs_winding_numbers_exact": (i32, [vp, vp, u64, vp, u64, vp, u64, vp]),
     "bs_winding_numbers_build": (i32, [vp, vp, u64, vp, u64, i32, PP]),
     "bs_winding_numbers_build_ex": (i32, [vp, vp, u64, vp, u64, i32, i32, PP]),

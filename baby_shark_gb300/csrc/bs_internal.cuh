@@ -196,6 +196,25 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
 
+// Quotient a / b, correctly rounded, from y = RN(1/b) (computed once and
+// shared by every division by b): Markstein's division (P. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Develop. 34(1), 1990): q0 = RN(a y), the remainder
+// r = a - b q0 exact through a fused multiply-add, q1 = RN(q0 + r y).  Valid
+// where a, b and a / b stay clear of overflow and underflow (callers keep
+// |a| and |b| in [2^-60, 2^60]); each step then scales exactly with the
+// operands' exponents, so it equals IEEE division everywhere in that range
+// when it does on every pair of significands — bs_diag_check_division checks
+// all 2^46 pairs against __fdiv_rn.  For a = -0 it returns +0 (IEEE: -0).
+__device__ __forceinline__ float mdiv(float a, float b, float y) {
+  const float q0 = __fmul_rn(a, y);
+  return __fmaf_rn(__fmaf_rn(-b, q0, a), y, q0);
+}
+__device__ __forceinline__ bool mdiv_range(float x) {  // |x| in [2^-60, 2^60]
+  const float ax = fabsf(x);
+  return ax >= 0x1p-60f && ax <= 0x1p60f;
+}
+
 struct F3 {
   float x, y, z;
 };

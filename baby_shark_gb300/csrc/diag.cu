@@ -47,3 +47,42 @@ extern "C" bs_status bs_diag_fp32_peak(bs_ctx* ctx, double* tflops) {
     return e.status;
   }
 }
+
+// Every pair of significands (a, b in [1, 2)): Markstein's division with a
+// shared reciprocal (bs_internal.cuh, mdiv) against CUDA's IEEE division.
+__global__ void k_div_check(uint32_t b_stride, unsigned long long* bad, unsigned long long* tested) {
+  const uint32_t mb = blockIdx.x * b_stride;
+  if (mb >= (1u << 23)) return;
+  const float b = __uint_as_float((127u << 23) | mb);
+  const float y = __frcp_rn(b);
+  uint32_t nbad = 0;
+  for (uint32_t ma = threadIdx.x; ma < (1u << 23); ma += blockDim.x) {
+    const float a = __uint_as_float((127u << 23) | ma);
+    nbad += (bs::mdiv(a, b, y) != __fdiv_rn(a, b)) ? 1u : 0u;
+  }
+  const uint32_t w = __reduce_add_sync(0xffffffffu, nbad);
+  if ((threadIdx.x & 31) == 0) {
+    if (w) atomicAdd(bad, (unsigned long long)w);
+    atomicAdd(tested, 32ull * ((1u << 23) / blockDim.x));
+  }
+}
+
+extern "C" bs_status bs_diag_check_division(bs_ctx* ctx, uint32_t b_stride, uint64_t* mismatches, uint64_t* tested) {
+  if (!ctx || !mismatches || !tested || b_stride == 0) return BS_ERR_INVALID_ARG;
+  try {
+    BS_CUDA(cudaSetDevice(ctx->device));
+    bs::DBuf<unsigned long long> c(ctx, 2);
+    BS_CUDA(cudaMemsetAsync(c.p, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    const unsigned nb = unsigned(((1u << 23) + b_stride - 1) / b_stride);
+    k_div_check<<<nb, 256, 0, ctx->stream>>>(b_stride, c.p, c.p + 1);
+    BS_CHECK_LAUNCH(ctx);
+    unsigned long long h[2];
+    bs::read_back(ctx, h, c.p, sizeof h);
+    *mismatches = h[0];
+    *tested = h[1];
+    return BS_OK;
+  } catch (const bs::Error& e) {
+    ctx->last_error = e.msg;
+    return e.status;
+  }
+}

@@ -894,14 +894,27 @@ __global__ void k_rt_tau(uint64_t nt, const uint32_t* __restrict__ tb, int K, co
 }
 
 // ------------------------------------------------------------ traversal ---
+// v / len for the three components of v, correctly rounded, with one
+// reciprocal (mdiv) where the operands allow it.
+__device__ __forceinline__ F3 div3(F3 v, float len) {
+  if (mdiv_range(len) && (v.x == 0.0f || mdiv_range(v.x)) && (v.y == 0.0f || mdiv_range(v.y)) &&
+      (v.z == 0.0f || mdiv_range(v.z))) {
+    const float y = __frcp_rn(len);
+    // a zero component keeps its sign (0 / len = 0 * (1 / len))
+    return f3(v.x == 0.0f ? fmul(v.x, y) : mdiv(v.x, len, y), v.y == 0.0f ? fmul(v.y, y) : mdiv(v.y, len, y),
+              v.z == 0.0f ? fmul(v.z, y) : mdiv(v.z, len, y));
+  }
+  return f3(fdiv(v.x, len), fdiv(v.y, len), fdiv(v.z, len));
+}
+
 // solid_angle (aabb_tree.rs:582-615): Van Oosterom–Strackee, unfused.
 __device__ __forceinline__ float solid_angle(float4 A, float4 Bv, float4 C, F3 q) {
   F3 qa = sub3(f3(A.x, A.y, A.z), q), qb = sub3(f3(Bv.x, Bv.y, Bv.z), q), qc = sub3(f3(C.x, C.y, C.z), q);
   const float la = fsqrt(dot3(qa, qa)), lb = fsqrt(dot3(qb, qb)), lc = fsqrt(dot3(qc, qc));
   if (la == 0.f || lb == 0.f || lc == 0.f) return 0.f;
-  qa = f3(fdiv(qa.x, la), fdiv(qa.y, la), fdiv(qa.z, la));
-  qb = f3(fdiv(qb.x, lb), fdiv(qb.y, lb), fdiv(qb.z, lb));
-  qc = f3(fdiv(qc.x, lc), fdiv(qc.y, lc), fdiv(qc.z, lc));
+  qa = div3(qa, la);
+  qb = div3(qb, lb);
+  qc = div3(qc, lc);
   const float num = dot3(qa, cross3(sub3(qb, qa), sub3(qc, qa)));
   if (num == 0.f) return 0.f;
   const float den = fadd(fadd(fadd(1.0f, dot3(qa, qb)), dot3(qa, qc)), dot3(qb, qc));
@@ -911,6 +924,11 @@ __device__ __forceinline__ float solid_angle(float4 A, float4 Bv, float4 C, F3 q
 // Far field of a node at q (aabb_tree.rs:666-671 with hessians, 803-816):
 // r = p - q, the order-1 term a . r / (4 pi |r|^3) and the Frobenius product
 // of the order-2 coefficients with I / (4 pi |r|^3) - 3 r r^T / (4 pi |r|^5).
+// The nine quotients by 4 pi |r|^5 share one reciprocal (mdiv) when every
+// component of r is 0 or within [2^-28, 2^28] and 4 pi |r|^5 within
+// [2^-60, 2^60]: every dividend (3 r_i) r_j is then 0 or within [2^-60, 2^60].
+// A dividend of -0 gives +0 there, which the following id - quotient turns
+// into the same +0 or id that IEEE division's -0 gives.
 __device__ __forceinline__ float far_field(const float4* R, float4 P, F3 q, float r2) {
   const float4 c1 = R[1], c2 = R[2], c3 = R[3];
   const float r1 = fsqrt(r2);  // |q - p| (norm, aabb_tree.rs:665; r1 of hessians, 806)
@@ -922,12 +940,25 @@ __device__ __forceinline__ float far_field(const float4* R, float4 P, F3 q, floa
   const float t[3] = {fmul(3.0f, r[0]), fmul(3.0f, r[1]), fmul(3.0f, r[2])};
   const float B[9] = {c1.w, c2.x, c2.y, c2.z, c2.w, c3.x, c3.y, c3.z, c3.w};
   const float v1 = fadd(fadd(fmul(c1.x, fmul(r[0], inv)), fmul(c1.y, fmul(r[1], inv))), fmul(c1.z, fmul(r[2], inv)));
+  auto comp_ok = [](float x) {
+    const float ax = fabsf(x);
+    return ax == 0.0f || (ax >= 0x1p-28f && ax <= 0x1p28f);
+  };
   float v2 = 0.0f;
-  for (int j = 0; j < 3; ++j)
-    for (int i = 0; i < 3; ++i) {
-      const float id = fmul(i == j ? 1.0f : 0.0f, inv);
-      v2 = fadd(v2, fmul(B[3 * j + i], fsub(id, fdiv(fmul(t[i], r[j]), d5))));
-    }
+  if (mdiv_range(d5) && comp_ok(r[0]) && comp_ok(r[1]) && comp_ok(r[2])) {
+    const float y = __frcp_rn(d5);
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i) {
+        const float id = fmul(i == j ? 1.0f : 0.0f, inv);
+        v2 = fadd(v2, fmul(B[3 * j + i], fsub(id, mdiv(fmul(t[i], r[j]), d5, y))));
+      }
+  } else {
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i) {
+        const float id = fmul(i == j ? 1.0f : 0.0f, inv);
+        v2 = fadd(v2, fmul(B[3 * j + i], fsub(id, fdiv(fmul(t[i], r[j]), d5))));
+      }
+  }
   return fadd(v1, v2);
 }
 

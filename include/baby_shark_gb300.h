@@ -106,6 +106,12 @@ bs_status bs_ctx_memory_reset(bs_ctx* ctx, int trim);
 /* Measured FP32 FMA throughput of the context's device in TFLOP/s (a timed
  * FFMA loop over all SMs); the denominator of FP32-bound roofline fractions. */
 bs_status bs_diag_fp32_peak(bs_ctx* ctx, double* tflops);
+/* Checks the shared-reciprocal division of the winding-number kernels
+ * (Markstein's: q0 = RN(a * RN(1/b)), one fused correction) against CUDA's
+ * IEEE division on every pair of significands a, b in [1, 2) — every
+ * b_stride-th divisor, every dividend; b_stride 1 covers all 2^46 pairs —
+ * and returns the number of differing quotients and of pairs tested. */
+bs_status bs_diag_check_division(bs_ctx* ctx, uint32_t b_stride, uint64_t* mismatches, uint64_t* tested);
 /* Exact generalised winding numbers of n_points points (device float3) with
  * respect to a mesh (device arrays): the direct sum over every triangle of
  * the solid angle of aabb_tree.rs:582-615, summed in double into d_out.  A
