@@ -120,6 +120,11 @@ class Context:
         out["wn_warp_visits"] = a[6]
         out["wn_warp_far"] = a[7] & 0xffffffff
         out["wn_warp_exact"] = a[7] >> 32
+        out["wn_far"] = a[10]
+        out["wn_exact"] = a[11]
+        out["wn_tree"] = "reference" if a[12] == 0 else "fast"
+        out["wn_far_warp_sections"] = a[13]
+        out["wn_exact_warp_sections"] = a[14]
         return out
 
 

@@ -2027,14 +2027,14 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   // join the tree build; the triangles are freed after it
   BS_CUDA(cudaStreamWaitEvent(s, built.e, 0));
   T.reset();
-  unsigned long long rt_cnt[4] = {0, 0, 0, 0};
+  unsigned long long rt_cnt[6] = {0, 0, 0, 0, 0, 0};
   if (na > 0 && ref_tree) {
     std::vector<RefSignMesh> rm(K);
     for (int m = 0; m < K; ++m) rm[m] = RefSignMesh{rt.h_roots[m], mi[m].h, mi[m].beta, mi[m].thresh};
     DBuf<RefSignMesh> d_rm(ctx, K);
-    DBuf<unsigned long long> d_cnt(ctx, 4);
+    DBuf<unsigned long long> d_cnt(ctx, 6);
     BS_CUDA(cudaMemcpyAsync(d_rm.p, rm.data(), K * sizeof(RefSignMesh), cudaMemcpyHostToDevice, s));
-    BS_CUDA(cudaMemsetAsync(d_cnt.p, 0, 4 * sizeof(unsigned long long), s));
+    BS_CUDA(cudaMemsetAsync(d_cnt.p, 0, 6 * sizeof(unsigned long long), s));
     ref_tree_sign(ctx, rt, act.p, act_base.p, d_wb.p, warp_base[K], K, d_rm.p, origins.p, values.p, d_cnt.p);
     read_back(ctx, rt_cnt, d_cnt.p, sizeof rt_cnt);
     if (rt_cnt[3]) fail(BS_ERR_CAPACITY, "winding-number traversal stack overflow");
@@ -2095,6 +2095,11 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
   ctx->last_stats[7] = (far & 0xffffffffull) | (exact << 32);
   ctx->last_stats[8] = BS_STATS_MESH_TO_VOLUME;
   ctx->last_stats[9] = n_ev;
+  ctx->last_stats[10] = far;  // full width (per voxel for the reference's tree)
+  ctx->last_stats[11] = exact;
+  ctx->last_stats[12] = ref_tree ? 0 : 1;
+  ctx->last_stats[13] = ref_tree ? rt_cnt[4] : 0;
+  ctx->last_stats[14] = ref_tree ? rt_cnt[5] : 0;
 
   // hand out the volumes
   std::vector<bs_volume*> vols(K, nullptr);
@@ -2239,15 +2244,18 @@ static void wn_tree_approximate(bs_ctx* ctx, bs_wn_tree* t, const float* d_pts, 
   if (np == 0) return;
   cudaStream_t s = ctx->stream;
   if (t->ref) {  // one traversal per point, in the caller's order
-    DBuf<unsigned long long> cnt(ctx, 4);
-    BS_CUDA(cudaMemsetAsync(cnt.p, 0, 4 * sizeof(unsigned long long), s));
+    DBuf<unsigned long long> cnt(ctx, 6);
+    BS_CUDA(cudaMemsetAsync(cnt.p, 0, 6 * sizeof(unsigned long long), s));
     ref_tree_points(ctx, *t->ref, d_pts, np, beta, d_out, cnt.p);
-    unsigned long long h[4];
+    unsigned long long h[6];
     read_back(ctx, h, cnt.p, sizeof h);
     if (h[3]) fail(BS_ERR_CAPACITY, "winding-number traversal stack overflow");
     ctx->last_stats[6] = h[0];
     ctx->last_stats[7] = (h[1] & 0xffffffffull) | (h[2] << 32);
     ctx->last_stats[8] = BS_STATS_WINDING_NUMBERS;
+    ctx->last_stats[10] = h[1];
+    ctx->last_stats[11] = h[2];
+    ctx->last_stats[12] = 0;
     return;
   }
   DBuf<M2VStats> st(ctx, 1);
@@ -2286,6 +2294,9 @@ static void wn_tree_approximate(bs_ctx* ctx, bs_wn_tree* t, const float* d_pts, 
   ctx->last_stats[6] = hs.wn_visits;
   ctx->last_stats[7] = (hs.wn_far & 0xffffffffull) | (hs.wn_exact << 32);
   ctx->last_stats[8] = BS_STATS_WINDING_NUMBERS;
+  ctx->last_stats[10] = hs.wn_far;
+  ctx->last_stats[11] = hs.wn_exact;
+  ctx->last_stats[12] = 1;
 }
 
 }  // namespace bs
@@ -2372,7 +2383,9 @@ bs_status bs_autotune_mesh_to_volume(bs_ctx* ctx, const float* d_xyz, uint64_t n
         ctx->stages.clear();
         bs::volume_release(bs::mesh_to_volume_impl(ctx, d_xyz, nv, d_tri, nt, *p));
         bs_ctx_resolve_stages(ctx);
-        const auto d = ctx->stages.find("k_brick_distance"), w = ctx->stages.find("k_wn_sign");
+        const auto d = ctx->stages.find("k_brick_distance");
+        auto w = ctx->stages.find("k_wn_sign");
+        if (w == ctx->stages.end()) w = ctx->stages.find("k_rt_sign");  // the reference's tree
         if (d != ctx->stages.end()) best[c][0] = std::min(best[c][0], d->second.ms);
         if (w != ctx->stages.end()) best[c][1] = std::min(best[c][1], w->second.ms);
       }

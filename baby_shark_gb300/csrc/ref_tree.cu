@@ -946,11 +946,14 @@ __device__ __forceinline__ float far_field(const float4* R, float4 P, F3 q, floa
   };
   float v2 = 0.0f;
   if (mdiv_range(d5) && comp_ok(r[0]) && comp_ok(r[1]) && comp_ok(r[2])) {
+    // inv is then positive and finite, so the identity's entries are inv
+    // and +0, and +0 - x = -x up to the sign of a zero, which no sum here
+    // can see: v2 starts at +0 and x + (+-0) is x, +0 for x = +-0
     const float y = __frcp_rn(d5);
     for (int j = 0; j < 3; ++j)
       for (int i = 0; i < 3; ++i) {
-        const float id = fmul(i == j ? 1.0f : 0.0f, inv);
-        v2 = fadd(v2, fmul(B[3 * j + i], fsub(id, mdiv(fmul(t[i], r[j]), d5, y))));
+        const float qt = mdiv(fmul(t[i], r[j]), d5, y);
+        v2 = fadd(v2, fmul(B[3 * j + i], i == j ? fsub(inv, qt) : -qt));
       }
   } else {
     for (int j = 0; j < 3; ++j)
@@ -964,6 +967,7 @@ __device__ __forceinline__ float far_field(const float4* R, float4 P, F3 q, floa
 
 struct Counts {
   uint32_t visits = 0, far = 0, exact = 0;
+  uint32_t far_sec = 0, exact_sec = 0;  // warp-level: far-field sections run, leaf triangles run
   bool overflow = false;
 };
 
@@ -999,11 +1003,13 @@ __device__ __forceinline__ unsigned resolve(int node, unsigned lanes, F3 q, cons
   const unsigned farm = __ballot_sync(FULL, r2 > P.w) & lanes;  // |q - p| > beta r
   const unsigned rest = lanes & ~farm;
   ++cnt.visits;
+  if (farm) ++cnt.far_sec;
   if (farm & me) {
     ++cnt.far;
     v = far_field(R, P, q, r2);
   }
   if (node >= 0) return rest;
+  if (rest) cnt.exact_sec += __ldg(leaf_cnt + ~node);
   if (rest & me) {
     const uint32_t p = ~node, c = __ldg(leaf_cnt + p);
     float w = 0.0f;
@@ -1098,6 +1104,8 @@ __device__ __forceinline__ void flush_counts(const Counts& c, unsigned long long
     atomicAdd(counters + 1, (unsigned long long)f);
     atomicAdd(counters + 2, (unsigned long long)e);
     if (ov) atomicAdd(counters + 3, 1ull);
+    atomicAdd(counters + 4, (unsigned long long)c.far_sec);
+    atomicAdd(counters + 5, (unsigned long long)c.exact_sec);
   }
 }
 
@@ -1105,7 +1113,9 @@ constexpr int SIGN_WARPS = 4;
 
 // One warp per 32 consecutive band voxels of one mesh (mesh_to_volume.rs:
 // 245-280): warps are numbered per mesh (warp_base[m] .. warp_base[m+1]).
-__global__ void __launch_bounds__(32 * SIGN_WARPS) k_rt_sign(const uint32_t* __restrict__ act,
+// WARPS per block: 2, 4 or 8 (the context's tuned launch shape).
+template <int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_rt_sign(const uint32_t* __restrict__ act,
                                                              const uint32_t* __restrict__ act_base,
                                                              const uint32_t* __restrict__ warp_base, int K,
                                                              const RefSignMesh* __restrict__ meshes,
@@ -1117,9 +1127,9 @@ __global__ void __launch_bounds__(32 * SIGN_WARPS) k_rt_sign(const uint32_t* __r
                                                              const uint32_t* __restrict__ leaf_cnt,
                                                              const float4* __restrict__ tri,
                                                              unsigned long long* __restrict__ counters) {
-  __shared__ WarpStack ws[SIGN_WARPS];
+  __shared__ WarpStack ws[WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const uint64_t gw = blockIdx.x * uint64_t(SIGN_WARPS) + w;
+  const uint64_t gw = blockIdx.x * uint64_t(WARPS) + w;
   if (gw >= warp_base[K]) return;  // whole warp
   const int m = K > 1 ? mesh_of(warp_base, K, gw) : 0;
   const uint64_t a1 = act_base[m + 1];
@@ -1289,9 +1299,17 @@ void ref_tree_sign(bs_ctx* ctx, const RefTrees& t, const uint32_t* act, const ui
                    const uint32_t* d_warp_base, uint64_t n_warps, int K, const RefSignMesh* d_meshes,
                    const int4* origins, float* values, unsigned long long* d_counters) {
   if (n_warps == 0) return;
-  BS_KERNEL(ctx, "k_rt_sign", (k_rt_sign<<<nblk(n_warps, SIGN_WARPS), 32 * SIGN_WARPS, 0, ctx->stream>>>(
-                                  act, d_act_base, d_warp_base, K, d_meshes, origins, values, t.rec_i.p, t.topo.p,
-                                  t.rec_l.p, t.leaf_cnt.p, t.tri.p, d_counters)));
+#define BS_RT_SIGN(W)                                                                                        \
+  BS_KERNEL(ctx, "k_rt_sign", (k_rt_sign<W><<<nblk(n_warps, W), 32 * W, 0, ctx->stream>>>(                   \
+                                  act, d_act_base, d_warp_base, K, d_meshes, origins, values, t.rec_i.p, t.topo.p, \
+                                  t.rec_l.p, t.leaf_cnt.p, t.tri.p, d_counters)))
+  if (ctx->tune_wn_warps == 2)
+    BS_RT_SIGN(2);
+  else if (ctx->tune_wn_warps == 8)
+    BS_RT_SIGN(8);
+  else
+    BS_RT_SIGN(4);
+#undef BS_RT_SIGN
 }
 
 void ref_tree_points(bs_ctx* ctx, RefTrees& t, const float* d_pts, uint64_t np, float beta, float* d_out,

@@ -51,9 +51,10 @@ struct RefSignMesh {
 // owns act[act_base[m], act_base[m+1]) and warps warp_base[m] ..
 // warp_base[m+1] of 32 voxels each) with the winding number of their grid
 // points: values[v] = +|d| when wn < thresh, else -|d|
-// (mesh_to_volume.rs:245-280).  counters (device, 4 x u64, accumulated):
+// (mesh_to_volume.rs:245-280).  counters (device, 6 x u64, accumulated):
 // warp node visits, far-field evaluations, exact solid angles, stack
-// overflows.
+// overflows, far-field evaluations and exact solid angles as the warps run
+// them (a section any lane needs runs for the whole warp).
 void ref_tree_sign(bs_ctx* ctx, const RefTrees& t, const uint32_t* act, const uint32_t* d_act_base,
                    const uint32_t* d_warp_base, uint64_t n_warps, int K, const RefSignMesh* d_meshes,
                    const int4* origins, float* values, unsigned long long* d_counters);

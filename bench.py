@@ -19,10 +19,13 @@ Synthetic, seeded (baby_shark_gb300.synthetic).
   cpu_baseline: the oracle (CPU restatement of the reference path, OpenMP,
           all host cores) on a bounded sample of the same workload.
 
-Beside the headline line (default run): the boolean / offset / meshing tail
-on those volumes (`pipeline`), the order-3 far field at accuracy scale 1.5
-(`order3_beta1.5`), the 256-mesh uneven batch (`batched`) and the launch
-shapes the autotuner picked during warm-up (`autotuned_launch_shape`).
+The headline signs on the reference's own tree (the library's default, bit-exact
+signs).  Beside it (default run): the boolean / offset / meshing tail on
+those volumes (`pipeline`), the library's faster PLOC tree at the reference's
+parameters (`fast_tree`) and with the order-3 far field at accuracy scale 1.5
+(`order3_beta1.5`), each with its sign differences from the headline, the
+256-mesh uneven batch (`batched`) and the launch shapes the autotuner picked
+during warm-up (`autotuned_launch_shape`).
 
 Other workloads (`--workload`): `open-icosphere` (4.7 M triangles with
 holes, voxel 0.001, signs of a sample checked against exact winding
@@ -61,11 +64,13 @@ WN_FLOP_PER_VOXEL = int(round(WN_FAR_PER_VOXEL * WN_FLOP_FAR + WN_EXACT_PER_VOXE
 # dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture of
 # the half-ring case (k_wn_sign 322 MB for 17,900,503 band voxels,
 # k_brick_distance 716 MB for 3,416,413,115 voxel pairs), scaled to a full
-# torus by the units processed (35,669,277 voxels; 6,848,421,294 pairs)
-TRAFFIC_PER_LAUNCH = {"k_wn_sign": 642e6, "k_brick_distance": 1436e6}
+# torus by the units processed (35,669,277 voxels; 6,848,421,294 pairs);
+# k_rt_sign captured on one full torus (548.3 MB read + 373.5 MB written)
+TRAFFIC_PER_LAUNCH = {"k_wn_sign": 642e6, "k_brick_distance": 1436e6, "k_rt_sign": 921.8e6}
 METRIC = "band voxels/s mesh→SDF+sign: learned/batched vs plain GPU, 0 sign flips"
 UNIT = "band_voxels/s"
-WORKLOAD = "two displaced tori, 1,048,576 triangles each, voxel 0.002, band 3: mesh->SDF+sign (plain GPU path)"
+WORKLOAD = ("two displaced tori, 1,048,576 triangles each, voxel 0.002, band 3: mesh->SDF+sign (plain GPU path; "
+            "signs on the reference's own SAH tree, bit-exact)")
 
 
 def rank_info():
@@ -368,6 +373,19 @@ def run_ours(args):
                 % (FLOP_PER_PAIR, ev, CULL_FLOP_PER_PAIR, stats["voxel_pairs"]))
         extra["reference_equivalent_tflops"] = FLOP_PER_PAIR * stats["voxel_pairs"] / per_launch_s / 1e12
         extra["pairs_evaluated_fraction"] = ev / max(1, stats["voxel_pairs"])
+    elif name == "k_rt_sign":
+        flops = WN_FLOP_PER_VOXEL * stats["active_voxels"]
+        # one traversal per voxel of the reference's own tree: the executed
+        # far-field and exact counts are the reference's (per voxel)
+        executed = WN_FLOP_FAR * stats["wn_far"] + WN_FLOP_EXACT * stats["wn_exact"]
+        extra["executed_tflops"] = executed / per_launch_s / 1e12
+        extra["executed_flop_per_launch"] = executed
+        extra["far_per_voxel"] = stats["wn_far"] / max(1, stats["active_voxels"])
+        extra["exact_per_voxel"] = stats["wn_exact"] / max(1, stats["active_voxels"])
+        algo = ("%d FLOP per band voxel (the reference's own traversal: %.0f far-field nodes x %d FLOP + "
+                "%.0f exact triangles x %d FLOP, counted by the oracle) x %d voxels per launch"
+                % (WN_FLOP_PER_VOXEL, WN_FAR_PER_VOXEL, WN_FLOP_FAR, WN_EXACT_PER_VOXEL, WN_FLOP_EXACT,
+                   stats["active_voxels"]))
     elif name == "k_wn_sign":
         flops = WN_FLOP_PER_VOXEL * stats["active_voxels"]
         # what the warp-coherent traversal executes: every lane of a warp evaluates
@@ -396,7 +414,8 @@ def run_ours(args):
     roof["launch_ms"] = tot_ms / nl
 
     pipe = pipeline_secondary(ctx, params, dev, L, N, bs, C) if args.pipeline else None
-    fast3 = order3_secondary(ctx, params, dev, L, N, bs, C, args) if args.order3 else None
+    fast_tree = variant_secondary(ctx, params, dev, L, N, bs, C, args) if args.order3 else None
+    fast3 = variant_secondary(ctx, params, dev, L, N, bs, C, args, order=3, beta=1.5) if args.order3 else None
     batch = batch_secondary(ctx, L, N, bs, C, args.batch_meshes) if args.batch_meshes else None
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -416,6 +435,7 @@ def run_ours(args):
             "pipeline": pipe,
             "batched": batch,
             "autotuned_launch_shape": tuned,
+            "fast_tree": fast_tree,
             "order3_beta1.5": fast3}
     if rank == 0:
         if world == 1:
@@ -456,6 +476,8 @@ def run_open(args):
     params.band_width = BAND
     params.wn_order = args.wn_order
     params.wn_beta = args.wn_beta
+    if args.wn_order == 3:
+        params.wn_tree = 1  # the third-order term lives on the library's tree
     stream = torch.cuda.ExternalStream(ctx.stream)
 
     def step():
@@ -507,16 +529,18 @@ def run_open(args):
     print(json.dumps(line))
 
 
-def order3_secondary(ctx, params, dev, L, N, bs, C, args):
-    """The same conversion with the order-3 far field at accuracy scale 1.5
-    (not the reference's order 2 / scale 2): band voxels/s, and how many band
-    voxel signs differ from the reference-parameter result."""
+def variant_secondary(ctx, params, dev, L, N, bs, C, args, tree=1, order=2, beta=2.0):
+    """The same conversion with another sign tree / far-field order /
+    accuracy scale: band voxels/s, and how many band voxel signs differ from
+    the headline (the reference's tree, order 2, scale 2).  tree 1 is the
+    library's PLOC tree with its warp-coherent traversal."""
     import copy
 
     import torch
     p3 = copy.copy(params)
-    p3.wn_order = 3
-    p3.wn_beta = 1.5
+    p3.wn_tree = tree
+    p3.wn_order = order
+    p3.wn_beta = beta
     stream = torch.cuda.ExternalStream(ctx.stream)
 
     def conv(p):
@@ -546,7 +570,8 @@ def order3_secondary(ctx, params, dev, L, N, bs, C, args):
         act = np.unpackbits(ma.view(np.uint8), bitorder="little").reshape(len(ma), 512).astype(bool)
         diff += int(np.sum(np.signbit(va[act]) != np.signbit(vb[act])))
     return {"value": band / (min(ms) / 1000.0), "unit": UNIT, "ms_per_step": min(ms),
-            "sign_differences_vs_reference_parameters": diff, "band_voxels": int(band)}
+            "sign_differences_vs_headline": diff, "band_voxels": int(band),
+            "tree": "PLOC (warp-coherent traversal)" if tree == 1 else "reference SAH", "order": order, "beta": beta}
 
 
 def run_learned(args):

@@ -87,7 +87,12 @@ bs_status bs_ctx_last_stats(const bs_ctx* ctx, uint64_t* out8);
 /* The same counters and more: [0..7] as above, [8] which call wrote them
  * (bs_stats_kind), [9] (voxel, sub-triangle) pairs whose exact distance a
  * mesh -> volume call evaluated after culling (the rest provably could not
- * lower their voxel's minimum), [10..15] zero. */
+ * lower their voxel's minimum), [10] far-field evaluations and [11] exact
+ * solid angles of the winding-number pass in 64 bits (per voxel or point on
+ * the reference's tree, per warp on the library's PLOC tree), [12] which tree
+ * (0 the reference's, 1 PLOC), [13] and [14] on the reference's tree the
+ * far-field evaluations and solid angles as its warps execute them (a
+ * section that any lane of a warp needs runs for all 32), [15] zero. */
 enum bs_stats_kind {
   BS_STATS_NONE = 0,
   BS_STATS_MESH_TO_VOLUME = 1,
