@@ -65,6 +65,7 @@ SIGNATURES = {
     "bs_mesh_to_volume_device": (i32, [vp, vp, u64, vp, u64, C.POINTER(M2VParams), PP]),
     "bs_mesh_to_volume_batch": (i32, [vp, u64, vp, vp, vp, vp, C.POINTER(M2VParams), vp]),
     "bs_mesh_to_volume_batch_device": (i32, [vp, u64, vp, vp, vp, vp, C.POINTER(M2VParams), vp]),
+    "bs_volume_create": (i32, [vp, f32, PP]),
     "bs_volume_free": (i32, [vp]),
     "bs_volume_voxel_size": (i32, [vp, C.POINTER(C.c_float)]),
     "bs_volume_clone": (i32, [vp, vp, PP]),

@@ -193,6 +193,14 @@ class Volume:
         self.h = handle
         self.ctx = ctx
 
+    @staticmethod
+    def with_voxel_size(voxel_size, ctx=None):
+        """Volume::with_voxel_size (volume/mod.rs:17-24): an empty volume."""
+        ctx = ctx or default_context()
+        out = C.c_void_p()
+        N.check(N.load().bs_volume_create(ctx.h, C.c_float(voxel_size), C.byref(out)), ctx.h)
+        return Volume(out, ctx)
+
     def __del__(self):
         if getattr(self, "h", None) is not None and self.h.value:
             try:

@@ -6,6 +6,8 @@
 #include <iterator>
 #include <new>
 
+#include <cmath>
+
 #include "bs_internal.cuh"
 
 namespace bs {
@@ -312,6 +314,16 @@ bs_status bs_winding_numbers_exact(bs_ctx* ctx, const float* d_xyz, uint64_t nv,
                                    uint64_t nt, const float* d_points, uint64_t n_points, double* d_out) {
   if (!ctx || (nt && (!d_xyz || !d_tri)) || (n_points && (!d_points || !d_out))) return BS_ERR_INVALID_ARG;
   return guarded(ctx, [&] { bs::exact_winding_numbers_impl(ctx, d_xyz, nv, d_tri, nt, d_points, n_points, d_out); });
+}
+
+bs_status bs_volume_create(bs_ctx* ctx, float voxel_size, bs_volume** out) {
+  if (!ctx || !out || !(voxel_size > 0.f) || !std::isfinite(voxel_size)) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  return guarded(ctx, [&] {
+    bs_volume* v = new bs_volume(ctx);  // no leaves, no tiles, no internal nodes
+    v->h = voxel_size;
+    *out = v;
+  });
 }
 
 bs_status bs_volume_free(bs_volume* v) {

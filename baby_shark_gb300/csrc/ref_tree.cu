@@ -893,6 +893,24 @@ __global__ void k_rt_tau(uint64_t nt, const uint32_t* __restrict__ tb, int K, co
   if (flags[p] == 2) rec_i[4 * p].w = far_tau(rad_i[p], b);  // internal node p (both children combined)
 }
 
+// Opening record of every internal node: both children's dipole centre and
+// far threshold (copied from their records) and their references and leaf
+// triangle counts, so a warp opening a node reads three float4 at once.
+__global__ void k_rt_open(uint64_t nt, const int* __restrict__ flags, const int2* __restrict__ topo,
+                          const uint32_t* __restrict__ leaf_cnt, const float4* __restrict__ rec_i,
+                          const float4* __restrict__ rec_l, float4* __restrict__ open) {
+  const uint64_t p = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (p >= nt || flags[p] != 2) return;
+  const int2 ch = topo[p];
+  const float4 hl = ch.x >= 0 ? rec_i[4 * uint64_t(ch.x)] : rec_l[4 * uint64_t(~ch.x)];
+  const float4 hr = ch.y >= 0 ? rec_i[4 * uint64_t(ch.y)] : rec_l[4 * uint64_t(~ch.y)];
+  open[3 * p] = hl;
+  open[3 * p + 1] = hr;
+  open[3 * p + 2] = make_float4(__int_as_float(ch.x), __int_as_float(ch.y),
+                                __uint_as_float(ch.x < 0 ? leaf_cnt[~ch.x] : 0u),
+                                __uint_as_float(ch.y < 0 ? leaf_cnt[~ch.y] : 0u));
+}
+
 // ------------------------------------------------------------ traversal ---
 // v / len for the three components of v, correctly rounded, with one
 // reciprocal (mdiv) where the operands allow it.
@@ -965,9 +983,12 @@ __device__ __forceinline__ float far_field(const float4* R, float4 P, F3 q, floa
   return fadd(v1, v2);
 }
 
+// Work counters, the same in every lane of a warp (computed from ballot
+// masks): far-field evaluations and exact solid angles its lanes need, and
+// the far-field and leaf sections the warp runs for them.
 struct Counts {
-  uint32_t visits = 0, far = 0, exact = 0;
-  uint32_t far_sec = 0, exact_sec = 0;  // warp-level: far-field sections run, leaf triangles run
+  uint32_t iters = 0, far = 0, exact = 0;
+  uint32_t far_sec = 0, exact_sec = 0;
   bool overflow = false;
 };
 
@@ -990,46 +1011,47 @@ struct WarpStack {
   unsigned act[STACK];
 };
 
-// The lanes in `lanes` meet `node`: far field or leaf sum into v; returns the
-// lanes that open it (an internal node near for them).
-__device__ __forceinline__ unsigned resolve(int node, unsigned lanes, F3 q, const float4* __restrict__ rec_i,
-                                            const float4* __restrict__ rec_l, const uint32_t* __restrict__ leaf_cnt,
+// The lanes in `lanes` meet node `ref` (header H: dipole centre, far
+// threshold; c: its leaf triangle count): far field or leaf sum into v;
+// returns the lanes that open it (an internal node near for them).
+__device__ __forceinline__ unsigned resolve(int ref, uint32_t c, float4 H, unsigned lanes, F3 q,
+                                            const float4* __restrict__ rec_i, const float4* __restrict__ rec_l,
                                             const float4* __restrict__ tri, float& v, Counts& cnt) {
   const unsigned me = 1u << (threadIdx.x & 31);
-  const float4* R = node >= 0 ? rec_i + 4 * node : rec_l + 4 * (~node);
-  const float4 P = __ldg(R);
-  const float dx = fsub(q.x, P.x), dy = fsub(q.y, P.y), dz = fsub(q.z, P.z);
+  const float dx = fsub(q.x, H.x), dy = fsub(q.y, H.y), dz = fsub(q.z, H.z);
   const float r2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz));
-  const unsigned farm = __ballot_sync(FULL, r2 > P.w) & lanes;  // |q - p| > beta r
+  const unsigned farm = __ballot_sync(FULL, r2 > H.w) & lanes;  // |q - p| > beta r
   const unsigned rest = lanes & ~farm;
-  ++cnt.visits;
-  if (farm) ++cnt.far_sec;
-  if (farm & me) {
-    ++cnt.far;
-    v = far_field(R, P, q, r2);
+  if (farm) {
+    cnt.far += __popc(farm);
+    ++cnt.far_sec;
+    if (farm & me) v = far_field(ref >= 0 ? rec_i + 4 * ref : rec_l + 4 * (~ref), H, q, r2);
   }
-  if (node >= 0) return rest;
-  if (rest) cnt.exact_sec += __ldg(leaf_cnt + ~node);
-  if (rest & me) {
-    const uint32_t p = ~node, c = __ldg(leaf_cnt + p);
-    float w = 0.0f;
-    for (uint32_t k = 0; k < c; ++k)
-      w = fadd(w, solid_angle(__ldg(tri + 3 * (p + k)), __ldg(tri + 3 * (p + k) + 1), __ldg(tri + 3 * (p + k) + 2), q));
-    cnt.exact += c;
-    v = fdiv(w, FOUR_PI_F);  // winding_number (aabb_tree.rs:617-628)
+  if (ref >= 0) return rest;
+  if (rest) {
+    cnt.exact += __popc(rest) * c;
+    cnt.exact_sec += c;
+    if (rest & me) {
+      const uint32_t p = ~ref;
+      float w = 0.0f;
+      for (uint32_t k = 0; k < c; ++k)
+        w = fadd(w, solid_angle(__ldg(tri + 3 * (p + k)), __ldg(tri + 3 * (p + k) + 1), __ldg(tri + 3 * (p + k) + 2), q));
+      v = fdiv(w, FOUR_PI_F);  // winding_number (aabb_tree.rs:617-628)
+    }
   }
   return 0u;
 }
 
 __device__ float ref_wn_warp(F3 q, unsigned valid, int root, const float4* __restrict__ rec_i,
-                             const int2* __restrict__ topo, const float4* __restrict__ rec_l,
+                             const float4* __restrict__ opn, const float4* __restrict__ rec_l,
                              const uint32_t* __restrict__ leaf_cnt, const float4* __restrict__ tri, WarpStack& ws,
                              Counts& cnt) {
   const int lane = threadIdx.x & 31;
   const unsigned me = 1u << lane;
   float lval[STACK], rval[STACK];
   float v = 0.0f;
-  unsigned open = resolve(root, valid, q, rec_i, rec_l, leaf_cnt, tri, v, cnt);
+  const float4 Hroot = __ldg(root >= 0 ? rec_i + 4 * root : rec_l + 4 * (~root));
+  unsigned open = resolve(root, root >= 0 ? 0u : __ldg(leaf_cnt + ~root), Hroot, valid, q, rec_i, rec_l, tri, v, cnt);
   if (!open) return v;
   const float v_root = v;  // lanes for which the root itself is far (or a leaf)
   const bool root_open = (open & me) != 0;
@@ -1037,10 +1059,12 @@ __device__ float ref_wn_warp(F3 q, unsigned valid, int root, const float4* __res
   uint64_t phase = 0;  // bit f: level f is descending its right child
   for (uint32_t guard = 0; guard < (1u << 30); ++guard) {
     // open `node` for the lanes in `open`
-    const int2 ch = __ldg(topo + node);
+    const float4 HL = __ldg(opn + 3 * node), HR = __ldg(opn + 3 * node + 1), M = __ldg(opn + 3 * node + 2);
+    const int2 ch = make_int2(__float_as_int(M.x), __float_as_int(M.y));
     float vl = 0.0f, vr = 0.0f;
-    const unsigned ol = resolve(ch.x, open, q, rec_i, rec_l, leaf_cnt, tri, vl, cnt);
-    const unsigned orr = resolve(ch.y, open, q, rec_i, rec_l, leaf_cnt, tri, vr, cnt);
+    ++cnt.iters;
+    const unsigned ol = resolve(ch.x, __float_as_uint(M.z), HL, open, q, rec_i, rec_l, tri, vl, cnt);
+    const unsigned orr = resolve(ch.y, __float_as_uint(M.w), HR, open, q, rec_i, rec_l, tri, vr, cnt);
     if (ol | orr) {
       if (d >= STACK) {
         cnt.overflow = true;
@@ -1097,12 +1121,11 @@ __device__ float ref_wn_warp(F3 q, unsigned valid, int root, const float4* __res
 }
 
 __device__ __forceinline__ void flush_counts(const Counts& c, unsigned long long* counters) {
-  const uint32_t f = __reduce_add_sync(FULL, c.far), e = __reduce_add_sync(FULL, c.exact);
   const unsigned ov = __ballot_sync(FULL, c.overflow);
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(counters, (unsigned long long)c.visits);  // warp-level visits (uniform)
-    atomicAdd(counters + 1, (unsigned long long)f);
-    atomicAdd(counters + 2, (unsigned long long)e);
+  if ((threadIdx.x & 31) == 0) {  // the counters are warp-uniform
+    atomicAdd(counters, 1ull + 2ull * c.iters);  // node visits: the root, then two children per opening
+    atomicAdd(counters + 1, (unsigned long long)c.far);
+    atomicAdd(counters + 2, (unsigned long long)c.exact);
     if (ov) atomicAdd(counters + 3, 1ull);
     atomicAdd(counters + 4, (unsigned long long)c.far_sec);
     atomicAdd(counters + 5, (unsigned long long)c.exact_sec);
@@ -1122,7 +1145,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_rt_sign(const uint32_t* __restri
                                                              const int4* __restrict__ origins,
                                                              float* __restrict__ values,
                                                              const float4* __restrict__ rec_i,
-                                                             const int2* __restrict__ topo,
+                                                             const float4* __restrict__ opn,
                                                              const float4* __restrict__ rec_l,
                                                              const uint32_t* __restrict__ leaf_cnt,
                                                              const float4* __restrict__ tri,
@@ -1142,7 +1165,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_rt_sign(const uint32_t* __restri
   const F3 q = f3(fmul(__int2float_rn(org.x + int(o >> 6)), M.h), fmul(__int2float_rn(org.y + int((o >> 3) & 7)), M.h),
                   fmul(__int2float_rn(org.z + int(o & 7)), M.h));
   Counts c;
-  const float wn = ref_wn_warp(q, __ballot_sync(FULL, ok), M.root, rec_i, topo, rec_l, leaf_cnt, tri, ws[w], c);
+  const float wn = ref_wn_warp(q, __ballot_sync(FULL, ok), M.root, rec_i, opn, rec_l, leaf_cnt, tri, ws[w], c);
   if (ok) {
     const float d = values[uint64_t(b) * 512 + o];
     values[uint64_t(b) * 512 + o] = (wn < M.thresh) ? copysignf(d, 1.0f) : copysignf(d, -1.0f);
@@ -1152,7 +1175,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_rt_sign(const uint32_t* __restri
 
 __global__ void __launch_bounds__(32 * SIGN_WARPS) k_rt_points(const float* __restrict__ pts, uint64_t np, int root,
                                                                const float4* __restrict__ rec_i,
-                                                               const int2* __restrict__ topo,
+                                                               const float4* __restrict__ opn,
                                                                const float4* __restrict__ rec_l,
                                                                const uint32_t* __restrict__ leaf_cnt,
                                                                const float4* __restrict__ tri, float* __restrict__ out,
@@ -1166,7 +1189,7 @@ __global__ void __launch_bounds__(32 * SIGN_WARPS) k_rt_points(const float* __re
   const uint64_t j = ok ? i : np - 1;
   const F3 q = f3(pts[3 * j], pts[3 * j + 1], pts[3 * j + 2]);
   Counts c;
-  const float wn = ref_wn_warp(q, __ballot_sync(FULL, ok), root, rec_i, topo, rec_l, leaf_cnt, tri, ws[w], c);
+  const float wn = ref_wn_warp(q, __ballot_sync(FULL, ok), root, rec_i, opn, rec_l, leaf_cnt, tri, ws[w], c);
   if (ok) out[i] = wn;
   flush_counts(c, counters);
 }
@@ -1292,6 +1315,9 @@ void ref_tree_set_beta(bs_ctx* ctx, RefTrees& t, const std::vector<float>& beta)
   BS_CUDA(cudaMemcpyAsync(d_beta.p, beta.data(), t.K * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
   BS_KERNEL(ctx, "k_rt_tau", (k_rt_tau<<<nblk(t.nt, 256), 256, 0, ctx->stream>>>(t.nt, t.tb.p, t.K, d_beta.p, t.leaf_cnt.p, t.flags.p,
                                                                              t.rad_i.p, t.rad_l.p, t.rec_i.p, t.rec_l.p)));
+  if (!t.open.p) t.open = DBuf<float4>(ctx, 3 * t.nt);
+  BS_KERNEL(ctx, "k_rt_open", (k_rt_open<<<nblk(t.nt, 256), 256, 0, ctx->stream>>>(t.nt, t.flags.p, t.topo.p, t.leaf_cnt.p, t.rec_i.p,
+                                                                               t.rec_l.p, t.open.p)));
   t.h_beta = beta;
 }
 
@@ -1301,7 +1327,7 @@ void ref_tree_sign(bs_ctx* ctx, const RefTrees& t, const uint32_t* act, const ui
   if (n_warps == 0) return;
 #define BS_RT_SIGN(W)                                                                                        \
   BS_KERNEL(ctx, "k_rt_sign", (k_rt_sign<W><<<nblk(n_warps, W), 32 * W, 0, ctx->stream>>>(                   \
-                                  act, d_act_base, d_warp_base, K, d_meshes, origins, values, t.rec_i.p, t.topo.p, \
+                                  act, d_act_base, d_warp_base, K, d_meshes, origins, values, t.rec_i.p, t.open.p, \
                                   t.rec_l.p, t.leaf_cnt.p, t.tri.p, d_counters)))
   if (ctx->tune_wn_warps == 2)
     BS_RT_SIGN(2);
@@ -1317,7 +1343,7 @@ void ref_tree_points(bs_ctx* ctx, RefTrees& t, const float* d_pts, uint64_t np, 
   if (np == 0) return;
   ref_tree_set_beta(ctx, t, std::vector<float>(1, beta));
   BS_KERNEL(ctx, "k_rt_points", (k_rt_points<<<nblk(np, 32 * SIGN_WARPS), 32 * SIGN_WARPS, 0, ctx->stream>>>(
-                                    d_pts, np, t.h_roots[0], t.rec_i.p, t.topo.p, t.rec_l.p, t.leaf_cnt.p,
+                                    d_pts, np, t.h_roots[0], t.rec_i.p, t.open.p, t.rec_l.p, t.leaf_cnt.p,
                                     t.tri.p, d_out, d_counters)));
 }
 

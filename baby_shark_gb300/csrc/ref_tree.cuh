@@ -19,6 +19,8 @@ namespace bs {
 struct RefTrees {
   DBuf<float4> rec_i;       // [n] 4 float4 per internal node: dipole xyz + far threshold, order-1 xyz + B0, B1..B4, B5..B8
   DBuf<int2> topo;          // [n] children of internal nodes
+  DBuf<float4> open;        // [n] 3 float4 per internal node: both children's dipole + far threshold,
+                            //     then (left ref, right ref, left leaf count, right leaf count) as int bits
   DBuf<float4> rec_l;       // [n] 4 float4 per leaf, at its first position
   DBuf<uint32_t> leaf_cnt;  // [n] triangles of the leaf starting at a position (0: none starts there)
   DBuf<float4> tri;         // [3n] triangles in leaf order

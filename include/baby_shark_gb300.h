@@ -185,6 +185,11 @@ bs_status bs_autotune_mesh_to_volume(bs_ctx* ctx, const float* d_xyz, uint64_t n
 /* Sets the launch shapes directly (0 keeps the current value). */
 bs_status bs_ctx_set_launch_shape(bs_ctx* ctx, int32_t dist_threads, int32_t wn_warps);
 /* ------------------------------------------------------------- volumes --- */
+/* Volume::with_voxel_size (volume/mod.rs:17-24): an empty volume (no leaves,
+ * tiles or internal nodes).  It takes part in booleans as the reference's
+ * empty grid does (root_node/csg.rs:9-58): union and subtraction of it leave
+ * the other operand (flood filled), intersection with it is empty. */
+bs_status bs_volume_create(bs_ctx* ctx, float voxel_size, bs_volume** out);
 /* Dropping a Volume (its Box<VolumeGrid>, volume/mod.rs:10-14). */
 bs_status bs_volume_free(bs_volume* v);
 /* Volume::voxel_size (volume/mod.rs:31-34). */

@@ -99,3 +99,40 @@ def test_consumed_operands():
     g = ga.union(gb)
     with pytest.raises(ValueError):
         ga.union(g)
+
+
+@pytest.mark.parametrize("op", ["union", "subtract", "intersect"])
+@pytest.mark.parametrize("empty_side", ["a", "b", "both"])
+def test_boolean_with_empty_volume(op, empty_side):
+    """Volume::with_voxel_size (volume/mod.rs:17-24) as either operand: the
+    reference's root-level CSG (root_node/csg.rs:9-58) keeps the other
+    operand's nodes for union (and for subtraction of an empty volume) and
+    nothing for intersection; every leaf, flood-filled value and tile equals
+    the oracle's."""
+    v, f = synthetic.icosphere(3, 0.6, 0.02, seed=11)
+    ctx = context()
+    h = 0.02
+    full_g = bs.MeshToVolume(ctx).with_voxel_size(h).with_narrow_band_width(2).convert((v, f))
+    full_o, _, _ = ob.mesh_to_volume(v, f, h, 2)
+    empty_g = lambda: bs.Volume.with_voxel_size(h, ctx)  # noqa: E731
+    empty_o = lambda: ob.volume_from_leaves(np.zeros((0, 3), np.int32), np.zeros((0, 512), np.float32),  # noqa: E731
+                                            np.zeros((0, 16), np.uint32), h)
+    ga, gb = (empty_g(), full_g) if empty_side == "a" else (full_g, empty_g()) if empty_side == "b" else \
+        (empty_g(), empty_g())
+    oa, obb = (empty_o(), full_o) if empty_side == "a" else (full_o, empty_o()) if empty_side == "b" else \
+        (empty_o(), empty_o())
+    g = getattr(ga, op)(gb)
+    o = getattr(oa, op)(obb)
+    rep = compare_volumes(g.export(), o.export(), check_inactive=True)
+    assert rep["leaf_set_equal"] and rep["mask_mismatch_leaves"] == 0, rep
+    assert rep["value_mismatch"] == 0 and rep["sign_mismatch"] == 0 and rep["inactive_mismatch"] == 0, rep
+    go, gs, gt = g.tiles()
+    oo, os_, ot = o.tiles()
+    assert sorted(zip(map(tuple, go.tolist()), gs.tolist())) == sorted(zip(map(tuple, oo.tolist()), os_.tolist()))
+    expect_full = (op == "union" and empty_side != "both") or (op == "subtract" and empty_side == "b")
+    assert (g.counts()["leaves"] > 0) == expect_full
+    # the empty volume through the rest of the path
+    e = bs.Volume.with_voxel_size(h, ctx)
+    e.offset(0.05)
+    assert e.counts()["leaves"] == 0
+    assert bs.DualContouringMesher().with_voxel_size(h).mesh(e).size == 0
