@@ -65,8 +65,8 @@ WN_FLOP_PER_VOXEL = int(round(WN_FAR_PER_VOXEL * WN_FLOP_FAR + WN_EXACT_PER_VOXE
 # the half-ring case (k_wn_sign 322 MB for 17,900,503 band voxels,
 # k_brick_distance 716 MB for 3,416,413,115 voxel pairs), scaled to a full
 # torus by the units processed (35,669,277 voxels; 6,848,421,294 pairs);
-# k_rt_sign captured on one full torus (548.3 MB read + 373.5 MB written)
-TRAFFIC_PER_LAUNCH = {"k_wn_sign": 642e6, "k_brick_distance": 1436e6, "k_rt_sign": 921.8e6}
+# k_rt_sign captured on one full torus (582.8 MB read + 272.0 MB written)
+TRAFFIC_PER_LAUNCH = {"k_wn_sign": 642e6, "k_brick_distance": 1436e6, "k_rt_sign": 854.8e6}
 METRIC = "band voxels/s mesh→SDF+sign: learned/batched vs plain GPU, 0 sign flips"
 UNIT = "band_voxels/s"
 WORKLOAD = ("two displaced tori, 1,048,576 triangles each, voxel 0.002, band 3: mesh->SDF+sign (plain GPU path; "
