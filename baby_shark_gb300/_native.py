@@ -41,7 +41,7 @@ SIGNATURES = {
     "bs_ctx_last_stats": (i32, [vp, C.POINTER(u64)]),
     "bs_ctx_last_counters": (i32, [vp, C.POINTER(u64)]),
     "bs_autotune_mesh_to_volume": (i32, [vp, vp, u64, vp, u64, vp, vp, vp]),
-    "bs_ctx_set_launch_shape": (i32, [vp, C.c_int32, C.c_int32]),
+    "bs_ctx_set_launch_shape": (i32, [vp, C.c_int32, C.c_int32, C.c_int32]),
     "bs_mlp_num_params": (i32, []),
     "bs_mlp_create": (i32, [vp, vp, f32, vp, vp, C.POINTER(vp)]),
     "bs_mlp_free": (i32, [vp]),

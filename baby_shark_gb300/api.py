@@ -81,16 +81,17 @@ class Context:
         self._lib.bs_m2v_params_default(C.byref(P))
         P.voxel_size = float(voxel_size)
         P.band_width = int(band_width)
-        ch = (C.c_int32 * 2)()
-        ms = (C.c_float * 6)()
+        ch = (C.c_int32 * 3)()
+        ms = (C.c_float * 11)()
         N.check(self._lib.bs_autotune_mesh_to_volume(self.h, dv.data_ptr(), len(v), df.data_ptr(), len(f),
                                                      C.byref(P), ch, ms), self.h)
-        return {"dist_threads": ch[0], "wn_warps": ch[1],
-                "distance_ms": {64: ms[0], 128: ms[1], 256: ms[2]},
-                "sign_ms": {2: ms[3], 4: ms[4], 8: ms[5]}}
+        shapes = [(64, 8), (64, 16), (64, 32), (128, 8), (128, 16), (128, 32), (256, 8), (256, 16)]
+        return {"dist_threads": ch[0], "wn_warps": ch[1], "dist_tile": ch[2],
+                "distance_ms": {sh: ms[k] for k, sh in enumerate(shapes)},
+                "sign_ms": {2: ms[8], 4: ms[9], 8: ms[10]}}
 
-    def set_launch_shape(self, dist_threads=0, wn_warps=0):
-        N.check(self._lib.bs_ctx_set_launch_shape(self.h, int(dist_threads), int(wn_warps)), self.h)
+    def set_launch_shape(self, dist_threads=0, wn_warps=0, dist_tile=0):
+        N.check(self._lib.bs_ctx_set_launch_shape(self.h, int(dist_threads), int(wn_warps), int(dist_tile)), self.h)
 
     def memory(self):
         """Bytes of the context's device pool: in use, peak in use, reserved."""

@@ -465,9 +465,10 @@ __global__ void k_act_starts(const uint32_t* __restrict__ voff, const uint32_t* 
 // survivors go through a per-warp queue and are evaluated 32 at a time with
 // all lanes busy (the branching closest-point formula measured
 // faster here than a branch-free one with a single division).
-// Threads per brick of the distance pass: 64, 128 or 256 (bs_autotune_mesh_to_volume
-// picks one per context; 128 by default).
-constexpr int DIST_BATCH = 16;  // sub-triangles a warp stages at a time
+// Threads per brick of the distance pass: 64, 128 or 256, and sub-triangles
+// a warp stages at a time (the tile): 8, 16 or 32, except 32 with 256
+// threads (its shared memory would pass 48 KB); bs_autotune_mesh_to_volume
+// picks both per context (128 and 16 by default).
 constexpr int DIST_QUEUE = 32 + 8 * 32;  // < 32 left over + one column walk of 8 steps x 32 lanes
 
 struct __align__(16) BatchTri {
@@ -487,7 +488,7 @@ constexpr float CULL_SCALE = 1.0f - 0x1p-20f;
 
 __device__ __forceinline__ float box_d(float lo, float hi, float g) { return fmaxf(fmaxf(lo - g, g - hi), 0.0f); }
 
-template <int THREADS>
+template <int THREADS, int DIST_BATCH>
 __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_brick_distance(
     const int4* __restrict__ origins, const uint32_t* __restrict__ list_off, const uint32_t* __restrict__ list,
     const SubTri* __restrict__ S, const MeshInfo* __restrict__ mi, const uint32_t* __restrict__ leaf_base, int K,
@@ -1950,17 +1951,28 @@ static std::vector<bs_volume*> batch_core(bs_ctx* ctx, const float* d_xyz, const
     bidx.reset();
     BS_KERNEL(ctx, "k_fill_pairs", (k_fill_pairs<<<blocks(ns, 256), 256, 0, s>>>(S.p, ns, d_dirs.p, d_db.p, cnt.p, list.p)));
     cnt.reset();
-    const int dt = ctx->tune_dist_threads;
-#define BS_DIST(TH)                                                                                              \
-  BS_KERNEL(ctx, "k_brick_distance", (k_brick_distance<TH><<<unsigned(nb), TH, 0, s>>>(origins.p, list_off.p, list.p, \
-                                                                                        S.p, d_mi.p, leaf_base.p, K,   \
-                                                                                        values.p, masks.p, st.p)))
-    if (dt == 64)
-      BS_DIST(64);
+    const int dt = ctx->tune_dist_threads, db = ctx->tune_dist_batch;
+#define BS_DIST(TH, BA)                                                                                            \
+  BS_KERNEL(ctx, "k_brick_distance", (k_brick_distance<TH, BA><<<unsigned(nb), TH, 0, s>>>(origins.p, list_off.p,  \
+                                                                                            list.p, S.p, d_mi.p,     \
+                                                                                            leaf_base.p, K, values.p, \
+                                                                                            masks.p, st.p)))
+    if (dt == 64 && db == 8)
+      BS_DIST(64, 8);
+    else if (dt == 64 && db == 32)
+      BS_DIST(64, 32);
+    else if (dt == 64)
+      BS_DIST(64, 16);
+    else if (dt == 256 && db == 8)
+      BS_DIST(256, 8);
     else if (dt == 256)
-      BS_DIST(256);
+      BS_DIST(256, 16);
+    else if (db == 8)
+      BS_DIST(128, 8);
+    else if (db == 32)
+      BS_DIST(128, 32);
     else
-      BS_DIST(128);
+      BS_DIST(128, 16);
 #undef BS_DIST
   }
   S.reset();
@@ -2358,76 +2370,92 @@ bs_status bs_winding_numbers_free(bs_wn_tree* t) {
 }
 
 // Times the distance and sign passes of one mesh -> volume conversion under
-// each candidate launch shape (threads per brick 64 / 128 / 256 with 2 / 4 /
-// 8 warps per sign block; two rounds, best of each) and keeps the fastest of
-// each pass for the context's later calls.  h_choice: [threads per brick,
-// warps per sign block]; h_ms (optional, 6 floats): the distance then the
-// sign times per candidate.
+// each candidate: the distance pass with 64 / 128 / 256 threads per brick
+// and tiles of 8 / 16 / 32 sub-triangles per warp (8 shapes: 256 threads
+// take tiles of 8 or 16), the sign pass with 2 / 4 / 8 warps per block; two
+// rounds, best of each, and keeps the fastest of each pass for the context's
+// later calls.  h_choice: [threads per brick, warps per sign block, tile];
+// h_ms (optional, 11 floats): the 8 distance shapes in the order (64, 8),
+// (64, 16), (64, 32), (128, 8), (128, 16), (128, 32), (256, 8), (256, 16),
+// then the sign pass with 2, 4, 8 warps.
 bs_status bs_autotune_mesh_to_volume(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
                                      const bs_m2v_params* p, int32_t* h_choice, float* h_ms) {
   if (!ctx || !p || !h_choice || !d_xyz || !d_tri || !nt) return BS_ERR_INVALID_ARG;
   const bool timing0 = ctx->timing;
-  const int dt0 = ctx->tune_dist_threads, ww0 = ctx->tune_wn_warps;
+  const int dt0 = ctx->tune_dist_threads, ww0 = ctx->tune_wn_warps, db0 = ctx->tune_dist_batch;
+  auto restore = [&] {
+    ctx->timing = timing0;
+    ctx->tune_dist_threads = dt0;
+    ctx->tune_wn_warps = ww0;
+    ctx->tune_dist_batch = db0;
+  };
   try {
     BS_CUDA(cudaSetDevice(ctx->device));
     bs_ctx_resolve_stages(ctx);
     auto saved = ctx->stages;
-    const int cand[3][2] = {{64, 2}, {128, 4}, {256, 8}};
-    double best[3][2] = {{1e30, 1e30}, {1e30, 1e30}, {1e30, 1e30}};
+    const int dist_cand[8][2] = {{64, 8}, {64, 16}, {64, 32}, {128, 8}, {128, 16}, {128, 32}, {256, 8}, {256, 16}};
+    const int wn_cand[3] = {2, 4, 8};
+    double best_d[8], best_w[3];
+    for (double& b : best_d) b = 1e30;
+    for (double& b : best_w) b = 1e30;
     bs::volume_release(bs::mesh_to_volume_impl(ctx, d_xyz, nv, d_tri, nt, *p));  // warm-up
     ctx->timing = true;
     for (int round = 0; round < 2; ++round) {
-      for (int c = 0; c < 3; ++c) {
-        ctx->tune_dist_threads = cand[c][0];
-        ctx->tune_wn_warps = cand[c][1];
+      for (int c = 0; c < 8; ++c) {
+        ctx->tune_dist_threads = dist_cand[c][0];
+        ctx->tune_dist_batch = dist_cand[c][1];
+        ctx->tune_wn_warps = wn_cand[c % 3];
         ctx->stages.clear();
         bs::volume_release(bs::mesh_to_volume_impl(ctx, d_xyz, nv, d_tri, nt, *p));
         bs_ctx_resolve_stages(ctx);
         const auto d = ctx->stages.find("k_brick_distance");
         auto w = ctx->stages.find("k_wn_sign");
         if (w == ctx->stages.end()) w = ctx->stages.find("k_rt_sign");  // the reference's tree
-        if (d != ctx->stages.end()) best[c][0] = std::min(best[c][0], d->second.ms);
-        if (w != ctx->stages.end()) best[c][1] = std::min(best[c][1], w->second.ms);
+        if (d != ctx->stages.end()) best_d[c] = std::min(best_d[c], d->second.ms);
+        if (w != ctx->stages.end()) best_w[c % 3] = std::min(best_w[c % 3], w->second.ms);
       }
     }
-    int bd = 1, bw = 1;
-    for (int c = 0; c < 3; ++c) {
-      if (best[c][0] < best[bd][0]) bd = c;
-      if (best[c][1] < best[bw][1]) bw = c;
-    }
-    ctx->tune_dist_threads = cand[bd][0];
-    ctx->tune_wn_warps = cand[bw][1];
+    int bd = 4, bw = 1;
+    for (int c = 0; c < 8; ++c)
+      if (best_d[c] < best_d[bd]) bd = c;
+    for (int c = 0; c < 3; ++c)
+      if (best_w[c] < best_w[bw]) bw = c;
     ctx->stages = saved;
     ctx->timing = timing0;
+    ctx->tune_dist_threads = dist_cand[bd][0];
+    ctx->tune_dist_batch = dist_cand[bd][1];
+    ctx->tune_wn_warps = wn_cand[bw];
     h_choice[0] = ctx->tune_dist_threads;
     h_choice[1] = ctx->tune_wn_warps;
-    if (h_ms)
-      for (int c = 0; c < 3; ++c) {
-        h_ms[c] = float(best[c][0]);
-        h_ms[3 + c] = float(best[c][1]);
-      }
+    h_choice[2] = ctx->tune_dist_batch;
+    if (h_ms) {
+      for (int c = 0; c < 8; ++c) h_ms[c] = float(best_d[c]);
+      for (int c = 0; c < 3; ++c) h_ms[8 + c] = float(best_w[c]);
+    }
     return BS_OK;
   } catch (const bs::Error& e) {
-    ctx->timing = timing0;
-    ctx->tune_dist_threads = dt0;
-    ctx->tune_wn_warps = ww0;
+    restore();
     ctx->last_error = e.msg;
     return e.status;
   } catch (const std::bad_alloc&) {
-    ctx->timing = timing0;
-    ctx->tune_dist_threads = dt0;
-    ctx->tune_wn_warps = ww0;
+    restore();
     return BS_ERR_OOM;
   }
 }
 
 // Sets the launch shapes directly (0 keeps a value): threads per brick of
-// the distance pass (64, 128, 256), warps per sign block (2, 4, 8).
-bs_status bs_ctx_set_launch_shape(bs_ctx* ctx, int32_t dist_threads, int32_t wn_warps) {
+// the distance pass (64, 128, 256), warps per sign block (2, 4, 8) and
+// sub-triangles per warp tile (8, 16, 32; not 32 with 256 threads).
+bs_status bs_ctx_set_launch_shape(bs_ctx* ctx, int32_t dist_threads, int32_t wn_warps, int32_t dist_tile) {
   if (!ctx) return BS_ERR_INVALID_ARG;
   if (dist_threads && dist_threads != 64 && dist_threads != 128 && dist_threads != 256) return BS_ERR_INVALID_ARG;
   if (wn_warps && wn_warps != 2 && wn_warps != 4 && wn_warps != 8) return BS_ERR_INVALID_ARG;
-  if (dist_threads) ctx->tune_dist_threads = dist_threads;
+  if (dist_tile && dist_tile != 8 && dist_tile != 16 && dist_tile != 32) return BS_ERR_INVALID_ARG;
+  const int th = dist_threads ? dist_threads : ctx->tune_dist_threads;
+  const int ti = dist_tile ? dist_tile : ctx->tune_dist_batch;
+  if (th == 256 && ti == 32) return BS_ERR_INVALID_ARG;
+  ctx->tune_dist_threads = th;
+  ctx->tune_dist_batch = ti;
   if (wn_warps) ctx->tune_wn_warps = wn_warps;
   return BS_OK;
 }

@@ -24,8 +24,10 @@ signs).  Beside it (default run): the boolean / offset / meshing tail on
 those volumes (`pipeline`), the library's faster PLOC tree at the reference's
 parameters (`fast_tree`) and with the order-3 far field at accuracy scale 1.5
 (`order3_beta1.5`), each with its sign differences from the headline, the
-256-mesh uneven batch (`batched`) and the launch shapes the autotuner picked
-during warm-up (`autotuned_launch_shape`).
+256-mesh uneven batch (`batched`), the learned far field against the plain
+traversal on 16 M points around the holed subdivision-9 icosphere, training
+time included (`learned`), and the launch shapes the autotuner picked during
+warm-up (`autotuned_launch_shape`).
 
 Other workloads (`--workload`): `open-icosphere` (4.7 M triangles with
 holes, voxel 0.001, signs of a sample checked against exact winding
@@ -244,8 +246,8 @@ def run_ours(args):
     L.bs_m2v_params_default(C.byref(params))
     params.voxel_size = H
     params.band_width = BAND
-    tune_choice = (C.c_int32 * 2)()
-    tune_ms = (C.c_float * 6)()
+    tune_choice = (C.c_int32 * 3)()
+    tune_ms = (C.c_float * 11)()
     if args.pipeline_only:
         params.voxel_size = args.voxel_size
         # the boolean / offset / dual-contouring tail alone, once (a profiling case)
@@ -307,9 +309,11 @@ def run_ours(args):
     if args.autotune:
         N.check(L.bs_autotune_mesh_to_volume(ctx.h, dev[0][0].data_ptr(), dev[0][0].shape[0], dev[0][1].data_ptr(),
                                              dev[0][1].shape[0], C.byref(params), tune_choice, tune_ms), ctx.h)
+        shapes = ["64x8", "64x16", "64x32", "128x8", "128x16", "128x32", "256x8", "256x16"]
         tuned = {"dist_threads": int(tune_choice[0]), "wn_warps": int(tune_choice[1]),
-                 "distance_ms_64_128_256": [round(float(x), 2) for x in tune_ms[:3]],
-                 "sign_ms_2_4_8_warps": [round(float(x), 2) for x in tune_ms[3:]]}
+                 "dist_tile": int(tune_choice[2]),
+                 "distance_ms_threads_x_tile": {k: round(float(x), 2) for k, x in zip(shapes, tune_ms[:8])},
+                 "sign_ms_2_4_8_warps": [round(float(x), 2) for x in tune_ms[8:]]}
     for _ in range(args.warmup):
         step_device()
     ctx.synchronize()
@@ -417,6 +421,13 @@ def run_ours(args):
     fast_tree = variant_secondary(ctx, params, dev, L, N, bs, C, args) if args.order3 else None
     fast3 = variant_secondary(ctx, params, dev, L, N, bs, C, args, order=3, beta=1.5) if args.order3 else None
     batch = batch_secondary(ctx, L, N, bs, C, args.batch_meshes) if args.batch_meshes else None
+    learned = None
+    if args.learned_queries:
+        from baby_shark_gb300 import synthetic as syn
+        vl, fl = syn.open_icosphere()
+        learned = learned_secondary(ctx, vl, fl, args.learned_queries, steps=2, warmup=1, validation=100000)
+        learned["workload"] = ("subdivision-9 icosphere with holes (%d triangles), %d points uniform in the box "
+                               "padded by 10 %%" % (len(fl), args.learned_queries))
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -436,6 +447,7 @@ def run_ours(args):
             "batched": batch,
             "autotuned_launch_shape": tuned,
             "fast_tree": fast_tree,
+            "learned": learned,
             "order3_beta1.5": fast3}
     if rank == 0:
         if world == 1:
@@ -574,30 +586,24 @@ def variant_secondary(ctx, params, dev, L, N, bs, C, args, tree=1, order=2, beta
             "tree": "PLOC (warp-coherent traversal)" if tree == 1 else "reference SAH", "order": order, "beta": beta}
 
 
-def run_learned(args):
-    """The learned far field on the non-watertight workload (subdivision-9
-    icosphere, 4.7 M triangles, 4-octave noise 0.1, 10 % of faces removed):
-    winding numbers (signs at the 0.2 threshold) of a query set of points
-    uniform in the padded bounding box.  Plain = the tree traversal (the
-    reference's order-2 far field, accuracy scale 2) for every point;
-    learned = train a network (band volume, sampling, traversal labels,
-    training, calibration: all timed) and answer the points outside the band
-    whose prediction is confident from the network, the rest from the same
-    traversal.  Both include the tree build.  Reports both times, the share
-    of points the network answered, sign differences between the two, and
-    signs of a seeded sample against exact winding numbers."""
+def learned_secondary(ctx, v, f, n_q, steps=2, warmup=1, validation=200000, seed=12345):
+    """The learned far field against the plain traversal on one mesh:
+    winding numbers (signs at the 0.2 threshold) of n_q points uniform in the
+    bounding box padded by 10 %.  Plain = the tree traversal (the reference's
+    order-2 far field, accuracy scale 2, the library's PLOC tree with
+    Morton-sorted queries) for every point; learned = train a network (band
+    volume, sampling, traversal labels, training, calibration: all timed) and
+    answer the points outside the band whose prediction is confident from the
+    network, the rest from the same traversal.  Both include the tree build.
+    Returns both times, their ratio, the share of points the network
+    answered, the sign differences between the two, and signs of a seeded
+    sample against exact winding numbers."""
     import torch
 
     import baby_shark_gb300 as bs
-    from baby_shark_gb300 import build as bs_build
-    from baby_shark_gb300 import synthetic
 
-    bs_build.build()
-    ctx = bs.Context(0)
-    v, f = synthetic.open_icosphere()
-    n_q = args.queries
     gen = torch.Generator(device="cuda")
-    gen.manual_seed(12345)
+    gen.manual_seed(seed)
     lo = torch.from_numpy(v.min(axis=0)).cuda()
     hi = torch.from_numpy(v.max(axis=0)).cuda()
     ext = hi - lo
@@ -625,15 +631,15 @@ def run_learned(args):
         ctx.synchronize()
         return time.perf_counter() - t0, time.perf_counter() - t1, out, n_trav, lf
 
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, warmup)):
         plain()
         learned()
-    tp, wp = min((plain() for _ in range(max(1, args.steps))), key=lambda r: r[0])
-    runs = [learned() for _ in range(max(1, args.steps))]
+    tp, wp = min((plain() for _ in range(max(1, steps))), key=lambda r: r[0])
+    runs = [learned() for _ in range(max(1, steps))]
     tl, tq, wl, n_trav, lf = min(runs, key=lambda r: r[0])
     diff = int((wp > 0.2).ne(wl > 0.2).sum().item())
     # exact check on a seeded sample
-    idx = torch.randperm(n_q, generator=gen, device="cuda")[:args.validation]
+    idx = torch.randperm(n_q, generator=gen, device="cuda")[:validation]
     exact = bs.winding_numbers_exact(v, f, q[idx], ctx=ctx)
     ex = (exact > 0.2).cpu().numpy()
     mism_plain = int(np.sum(ex != (wp[idx] > 0.2).cpu().numpy()))
@@ -642,23 +648,40 @@ def run_learned(args):
     # tensor-core work of the network (forward 2 (64 x 64 + 64 x 64 + 64) FLOP a sample, training about 3x)
     fwd_flop = 2 * (64 * 64 + 64 * 64 + 64)
     train_samples = 2_000_000 * 16
-    line = {"metric": "winding numbers / s of points in the padded box (learned far field vs traversal)",
-            "value": n_q / tl, "unit": "points/s", "n_gpus": 1, "steps": len(runs), "warmup": args.warmup,
-            "higher_is_better": True, "dtype": "bf16 network, f32 traversal", "data": "synthetic",
-            "config": {"workload": "subdivision-9 icosphere, 4-octave noise 0.1, 10 %% of faces removed (%d "
-                                   "triangles); %d query points uniform in the box padded by 10 %%" % (len(f), n_q),
-                       "parallelism": "single GPU"},
+    return {"points": n_q, "triangles": int(len(f)),
             "plain_s": tp, "plain_points_per_s": n_q / tp,
-            "learned_s": tl, "learned_over_plain": tp / tl,
+            "learned_s": tl, "learned_points_per_s": n_q / tl, "learned_over_plain": tp / tl,
             "learned_breakdown_s": dict(lf.timings, classify_s=tq),
             "network_answered_fraction": answered,
             "sign_differences_learned_vs_plain": diff,
-            "validation": {"points": int(args.validation), "plain_vs_exact": mism_plain,
+            "validation": {"points": int(validation), "plain_vs_exact": mism_plain,
                            "learned_vs_exact": mism_learned},
             "calibration": lf.calibration, "margin": lf.margin,
             "epoch_loss": [float(x) for x in lf.epoch_loss],
             "network_tflops": {"training": 3 * fwd_flop * train_samples / lf.timings["training_s"] / 1e12,
                                "inference_in_classify": fwd_flop * n_q / tq / 1e12}}
+
+
+def run_learned(args):
+    """The learned far field on the non-watertight workload (subdivision-9
+    icosphere, 4.7 M triangles, 4-octave noise 0.1, 10 % of faces removed):
+    learned_secondary on --queries points."""
+    import baby_shark_gb300 as bs
+    from baby_shark_gb300 import build as bs_build
+    from baby_shark_gb300 import synthetic
+
+    bs_build.build()
+    ctx = bs.Context(0)
+    v, f = synthetic.open_icosphere()
+    r = learned_secondary(ctx, v, f, args.queries, args.steps, args.warmup, args.validation)
+    line = {"metric": "winding numbers / s of points in the padded box (learned far field vs traversal)",
+            "value": r["learned_points_per_s"], "unit": "points/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "dtype": "bf16 network, f32 traversal",
+            "data": "synthetic",
+            "config": {"workload": "subdivision-9 icosphere, 4-octave noise 0.1, 10 %% of faces removed (%d "
+                                   "triangles); %d query points uniform in the box padded by 10 %%"
+                                   % (len(f), args.queries), "parallelism": "single GPU"},
+            **r}
     print(json.dumps(line), flush=True)
 
 
@@ -923,6 +946,8 @@ def main():
                     help="far-field order of the sign pass for --workload open-icosphere (2 = the reference's)")
     ap.add_argument("--wn-beta", type=float, default=2.0,
                     help="accuracy scale of the sign pass for --workload open-icosphere (2 = the reference's)")
+    ap.add_argument("--learned-queries", type=int, default=16_000_000,
+                    help="points of the learned-vs-plain comparison beside the headline (0: skip it)")
     ap.add_argument("--queries", type=int, default=16_000_000,
                     help="query points of --workload learned")
     ap.add_argument("--validation", type=int, default=200000,

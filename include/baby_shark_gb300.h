@@ -173,17 +173,20 @@ bs_status bs_mesh_to_volume_batch_device(bs_ctx* ctx, uint64_t n_meshes, const f
                                          const uint64_t* triangle_counts, const bs_m2v_params* params,
                                          bs_volume** out);
 /* Autotuner (no reference counterpart): converts the given mesh (device
- * arrays) once per candidate launch shape — 64 / 128 / 256 threads per brick
- * in the distance pass with 2 / 4 / 8 warps per block in the sign pass, two
- * rounds — and keeps the fastest shape of each pass for the context's later
- * conversions (results do not depend on the shape).  h_choice[2]: the
- * chosen threads per brick and warps per block; h_ms (optional, 6 floats):
- * the best distance-pass then sign-pass times per candidate, in ms.  The
- * brick stays 8^3 (the reference's leaf) and the sub-triangle tile 16. */
+ * arrays) once per candidate — the distance pass with 64 / 128 / 256 threads
+ * per brick and tiles of 8 / 16 / 32 sub-triangles per warp (256 threads take
+ * tiles of 8 or 16), the sign pass with 2 / 4 / 8 warps per block, two rounds
+ * — and keeps the fastest of each pass for the context's later conversions
+ * (results do not depend on them).  h_choice[3]: the chosen threads per
+ * brick, warps per sign block and tile; h_ms (optional, 11 floats): the best
+ * distance-pass times of the shapes (64, 8), (64, 16), (64, 32), (128, 8),
+ * (128, 16), (128, 32), (256, 8), (256, 16), then the sign-pass times with
+ * 2, 4, 8 warps, in ms.  The brick stays 8^3: it is the reference's leaf, the
+ * unit of every later boolean, offset and mesher. */
 bs_status bs_autotune_mesh_to_volume(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
                                      const bs_m2v_params* p, int32_t* h_choice, float* h_ms);
 /* Sets the launch shapes directly (0 keeps the current value). */
-bs_status bs_ctx_set_launch_shape(bs_ctx* ctx, int32_t dist_threads, int32_t wn_warps);
+bs_status bs_ctx_set_launch_shape(bs_ctx* ctx, int32_t dist_threads, int32_t wn_warps, int32_t dist_tile);
 /* ------------------------------------------------------------- volumes --- */
 /* Volume::with_voxel_size (volume/mod.rs:17-24): an empty volume (no leaves,
  * tiles or internal nodes).  It takes part in booleans as the reference's

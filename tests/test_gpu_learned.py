@@ -92,3 +92,24 @@ def test_training_lowers_loss_and_classification_keeps_signs():
     # the network answers a part of the uniform-plus-near-surface sample (the
     # margin follows the worst wrong-side calibration point, so the share varies)
     assert answered.mean() > 0.1, (answered.mean(), lf.calibration, lf.margin)
+
+
+def test_learned_against_plain_ratio_is_the_measured_one():
+    """bench.learned_secondary (the comparison the benchmark reports beside
+    its headline) on a smaller holed icosphere: the reported learned / plain
+    ratio is the ratio of the two measured wall times, the learned time
+    includes every stage of its set-up (tree, band, sampling, labels,
+    training, calibration) and its classification, and the learned signs
+    match exact winding numbers as well as the plain traversal's do, up to a
+    rare point answered by the network."""
+    import bench
+
+    v, f = synthetic.open_icosphere(subdiv=6, amplitude=0.1, octaves=4, remove=0.1, seed=3)
+    r = bench.learned_secondary(context(), v, f, 2_000_000, steps=1, warmup=1, validation=50_000)
+    print({k: r[k] for k in ("plain_s", "learned_s", "learned_over_plain", "network_answered_fraction")})
+    assert r["learned_over_plain"] == pytest.approx(r["plain_s"] / r["learned_s"], rel=1e-12)
+    assert r["learned_s"] >= r["learned_breakdown_s"]["total_s"]  # tree, band, sampling, labels, training, calibration
+    assert r["learned_s"] >= r["learned_breakdown_s"]["classify_s"]
+    assert 0.0 < r["network_answered_fraction"] < 1.0
+    val = r["validation"]
+    assert val["learned_vs_exact"] <= val["plain_vs_exact"] + 3

@@ -360,20 +360,26 @@ def test_distance_error_vs_float64_fine_voxel():
 
 
 def test_launch_shapes_give_identical_volumes_and_autotune_picks_one():
-    """Every launch shape the autotuner chooses from gives the same volume,
-    bit for bit; the autotuner returns one of them."""
+    """Every launch shape and tile the autotuner chooses from gives the same
+    volume, bit for bit, on both sign trees; the autotuner returns one of
+    them."""
     ctx = bs.Context(0)
     v, f = synthetic.torus(1.0, 0.3, 96, 48, 0.02, seed=5)
-    ref = None
-    for dt, ww in ((64, 2), (128, 4), (256, 8), (64, 8), (256, 2)):
-        ctx.set_launch_shape(dt, ww)
-        vol = bs.MeshToVolume(ctx).with_voxel_size(0.01).with_narrow_band_width(2).convert((v, f))
-        o, val, m = vol.export()
-        if ref is None:
-            ref = (o, val, m)
-        else:
-            assert np.array_equal(o, ref[0]) and np.array_equal(m, ref[2])
-            assert np.array_equal(val.view(np.uint32), ref[1].view(np.uint32))
+    for tree in ("reference", "fast"):
+        ref = None
+        for dt, ww, ti in ((64, 2, 8), (128, 4, 16), (256, 8, 16), (64, 8, 32), (256, 2, 8), (128, 2, 32)):
+            ctx.set_launch_shape(dt, ww, ti)
+            vol = bs.MeshToVolume(ctx).with_voxel_size(0.01).with_narrow_band_width(2).with_sign_tree(tree).convert(
+                (v, f))
+            o, val, m = vol.export()
+            if ref is None:
+                ref = (o, val, m)
+            else:
+                assert np.array_equal(o, ref[0]) and np.array_equal(m, ref[2])
+                assert np.array_equal(val.view(np.uint32), ref[1].view(np.uint32))
+    with pytest.raises(bs.BsError):
+        ctx.set_launch_shape(256, 0, 32)
     choice = ctx.autotune((v, f), 0.01, 2)
     assert choice["dist_threads"] in (64, 128, 256) and choice["wn_warps"] in (2, 4, 8)
+    assert choice["dist_tile"] in (8, 16, 32)
     assert all(t > 0 for t in choice["distance_ms"].values())
