@@ -5,10 +5,10 @@
 //    points (-0 == +0, NaN never equal) get one vertex, numbered in order of
 //    first appearance — three stable radix sorts on the coordinate bits, a
 //    group scan, and a scan over the first occurrences;
-//  * the indexed build (builder.rs:168-262) on the host: faces in order, a
-//    face that repeats a directed edge is skipped, then isolated vertices are
-//    deleted and every extra corner fan of a vertex gets its own copy.  This
-//    step is order dependent by definition and touches a few bytes per face.
+//  * the indexed build (builder.rs:168-262) on the GPU: faces in order, a
+//    face that repeats a directed edge of an earlier taken face is skipped,
+//    then isolated vertices are deleted and every extra corner fan of a
+//    vertex gets its own copy (see corner_table_from_device_soup).
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -92,12 +92,11 @@ __global__ void k_unique_points(const float* __restrict__ p, const uint32_t* __r
   out[3 * uint64_t(d) + 2] = p[3 * j + 2];
 }
 
-// merge_points on device points d_p[n][3]: ids[n] (host) and unique points (host).
-static void merge_points_gpu(bs_ctx* ctx, const float* d_p, uint64_t n, std::vector<uint32_t>& ids,
-                             std::vector<float>& uniq) {
+// merge_points on device points d_p[n][3]: ids[n] and the nu unique points, on the device.
+static void merge_points_gpu(bs_ctx* ctx, const float* d_p, uint64_t n, DBuf<uint32_t>& ids, DBuf<float>& uniq,
+                             uint32_t& nu) {
   cudaStream_t s = ctx->stream;
-  ids.assign(n, 0);
-  uniq.clear();
+  nu = 0;
   if (n == 0) return;
   if (n >= (1ull << 31)) fail(BS_ERR_CAPACITY, "more than 2^31 soup points");
   DBuf<uint32_t> key(ctx, n), key2(ctx, n), idx(ctx, n), idx2(ctx, n);
@@ -128,163 +127,412 @@ static void merge_points_gpu(bs_ctx* ctx, const float* d_p, uint64_t n, std::vec
   }
   BS_KERNEL(ctx, "k_group_first", (k_group_first<<<nbc(n, 256), 256, 0, s>>>(idx.p, start.p, gid.p, n, group_rep.p)));
   BS_KERNEL(ctx, "k_point_ids", (k_point_ids<<<nbc(n, 256), 256, 0, s>>>(idx.p, gid.p, group_rep.p, newid.p, n, id.p)));
-  uint32_t nu = 0;
   read_back(ctx, &nu, newid.p + n, sizeof(uint32_t));
   DBuf<float> up(ctx, uint64_t(nu) * 3);
   BS_KERNEL(ctx, "k_unique_points", (k_unique_points<<<nbc(n, 256), 256, 0, s>>>(d_p, is_rep.p, newid.p, n, up.p)));
-  uniq.resize(uint64_t(nu) * 3);
-  BS_CUDA(cudaMemcpyAsync(ids.data(), id.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  if (nu) BS_CUDA(cudaMemcpyAsync(uniq.data(), up.p, uint64_t(nu) * 3 * sizeof(float), cudaMemcpyDeviceToHost, s));
-  BS_CUDA(cudaStreamSynchronize(s));
+  ids = std::move(id);
+  uniq = std::move(up);
 }
 
-// ---------------------------------------------------- host indexed build ---
+// ------------------------------------------------------ indexed build ----
+// builder.rs:168-262 on the merged points, on the GPU.
+//
+// Faces are taken in order and a face is skipped when one of its directed
+// edges (v2, v3), (v3, v1), (v1, v2) already belongs to an earlier taken
+// face.  So a face is taken exactly when no earlier face sharing one of its
+// directed edges was taken: the lexicographically first maximal independent
+// set of the "shares a directed edge" graph.  The half-edges are sorted by
+// key (stable, so a key's run lists faces in order); a face none of whose
+// keys repeats is taken at once, the others decide in rounds — a face is
+// skipped as soon as an earlier face in one of its runs is taken, and taken
+// once every earlier face in its runs is skipped.  Each decision is final, so
+// the result does not depend on scheduling.  Taken faces get corners
+// 3r, 3r + 1, 3r + 2 (r their rank) with vertices v1, v2, v3, the
+// corner_from order; the corner opposite edge (x, y) pairs with the taken
+// half-edge (y, x) (for a key (x, x), only possible in a degenerate face, in
+// the chain the insertion order leaves: each with the next, the last with the
+// one before).  A vertex's corner is its highest (the last assigned); a
+// vertex without one is deleted.  Then per vertex the fan around its corner
+// stays, and every other fan, taken in order of its smallest corner, becomes
+// a new vertex (numbered after all earlier vertices' new ones, in vertex
+// order as the oracle's restatement numbers them).
 namespace {
 
-struct EdgeMap {  // directed edge (a, b) -> corner, open addressing
-  std::vector<uint64_t> keys;
-  std::vector<int32_t> vals;
-  uint64_t mask = 0;
-  static constexpr uint64_t EMPTY = ~0ull;
-  explicit EdgeMap(uint64_t n) {
-    uint64_t cap = 64;
-    while (cap < 2 * n + 16) cap <<= 1;
-    keys.assign(cap, EMPTY);
-    vals.assign(cap, -1);
-    mask = cap - 1;
+constexpr uint8_t F_OPEN = 0, F_TAKEN = 1, F_SKIPPED = 2;
+
+__device__ __forceinline__ int32_t cnext_d(int32_t c) { return (c % 3 == 2) ? c - 2 : c + 1; }
+__device__ __forceinline__ int32_t cprev_d(int32_t c) { return (c % 3 == 0) ? c + 2 : c - 1; }
+
+__global__ void k_half_keys(const uint32_t* __restrict__ ids, uint64_t nf, unsigned long long* __restrict__ key,
+                            uint32_t* __restrict__ half) {
+  const uint64_t f = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (f >= nf) return;
+  const uint32_t a = ids[3 * f], b = ids[3 * f + 1], c = ids[3 * f + 2];
+  const uint32_t x[3] = {b, c, a}, y[3] = {c, a, b};  // edges of corner_from(b,c,a), (c,a,b), (a,b,c)
+  for (int k = 0; k < 3; ++k) {
+    key[3 * f + k] = (static_cast<unsigned long long>(x[k]) << 32) | y[k];
+    half[3 * f + k] = uint32_t(3 * f + k);
   }
-  static uint64_t h(uint64_t k) {
-    k ^= k >> 31;
-    k *= 0x7fb5d329728ea185ull;
-    k ^= k >> 27;
-    k *= 0x81dadef4bc2dd44dull;
-    return k ^ (k >> 33);
-  }
-  int32_t* find(uint32_t a, uint32_t b) {
-    const uint64_t k = (uint64_t(a) << 32) | b;
-    for (uint64_t s = h(k) & mask;; s = (s + 1) & mask) {
-      if (keys[s] == k) return &vals[s];
-      if (keys[s] == EMPTY) return nullptr;
-    }
-  }
-  void put(uint32_t a, uint32_t b, int32_t v) {
-    const uint64_t k = (uint64_t(a) << 32) | b;
-    for (uint64_t s = h(k) & mask;; s = (s + 1) & mask) {
-      if (keys[s] == k || keys[s] == EMPTY) {
-        keys[s] = k;
-        vals[s] = v;
-        return;
-      }
-    }
-  }
+}
+
+// run_head[i]: i where a run of equal keys starts, else 0 (max-scanned into run starts)
+__global__ void k_half_runs(const unsigned long long* __restrict__ key, const uint32_t* __restrict__ half,
+                            uint64_t n, uint32_t* __restrict__ head, uint32_t* __restrict__ pos_of,
+                            uint8_t* __restrict__ shared_key) {
+  const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const bool first = i == 0 || key[i] != key[i - 1];
+  const bool last = i + 1 == n || key[i + 1] != key[i];
+  head[i] = first ? uint32_t(i) : 0u;
+  pos_of[half[i]] = uint32_t(i);
+  if (!(first && last)) shared_key[half[i] / 3] = 1;  // benign race: every writer writes 1
+}
+
+struct MaxU32 {
+  __device__ __forceinline__ uint32_t operator()(uint32_t a, uint32_t b) const { return a > b ? a : b; }
 };
 
-inline int32_t cnext(int32_t c) { return (c % 3 == 2) ? c - 2 : c + 1; }
-inline int32_t cprev(int32_t c) { return (c % 3 == 0) ? c + 2 : c - 1; }
+__global__ void k_face_init(const uint8_t* __restrict__ shared_key, uint64_t nf, uint8_t* __restrict__ state) {
+  const uint64_t f = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (f < nf) state[f] = shared_key[f] ? F_OPEN : F_TAKEN;
+}
 
-// traversal.rs:244-286
+// One round over the open faces.
+__global__ void k_face_round(const uint32_t* __restrict__ half, const uint32_t* __restrict__ run_start,
+                             const uint32_t* __restrict__ pos_of, uint64_t nf, uint8_t* __restrict__ state,
+                             unsigned long long* __restrict__ open_left) {
+  const uint64_t f = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (f >= nf) return;
+  if (__ldcg(state + f) != F_OPEN) return;
+  bool pending = false;
+  for (int k = 0; k < 3; ++k) {
+    const uint32_t i = pos_of[3 * f + k];
+    for (uint32_t j = run_start[i]; j < i; ++j) {
+      const uint64_t g = half[j] / 3;
+      if (g == f) continue;  // a face's own repeated key never excludes it
+      const uint8_t sg = __ldcg(state + g);
+      if (sg == F_TAKEN) {
+        state[f] = F_SKIPPED;
+        return;
+      }
+      if (sg == F_OPEN) pending = true;
+    }
+  }
+  if (pending) atomicAdd(open_left, 1ull);
+  else state[f] = F_TAKEN;
+}
+
+__global__ void k_taken_flags(const uint8_t* __restrict__ state, uint64_t nf, uint32_t* __restrict__ flag) {
+  const uint64_t f = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (f <= nf) flag[f] = (f < nf && state[f] == F_TAKEN) ? 1u : 0u;
+}
+
+__global__ void k_corner_vertices(const uint32_t* __restrict__ ids, const uint8_t* __restrict__ state,
+                                  const uint32_t* __restrict__ rank, uint64_t nf, int32_t* __restrict__ cvertex,
+                                  int32_t* __restrict__ vcorner) {
+  const uint64_t f = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (f >= nf || state[f] != F_TAKEN) return;
+  const uint64_t c0 = 3 * uint64_t(rank[f]);
+  for (int k = 0; k < 3; ++k) {
+    const uint32_t v = ids[3 * f + k];
+    cvertex[c0 + k] = int32_t(v);
+    atomicMax(vcorner + v, int32_t(c0 + k));  // the last corner assigned to the vertex
+  }
+}
+
+// First position of key k in the sorted keys, or n.
+__device__ __forceinline__ uint64_t lower_bound_key(const unsigned long long* __restrict__ key, uint64_t n,
+                                                    unsigned long long k) {
+  uint64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint64_t mid = (lo + hi) >> 1;
+    if (key[mid] < k) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_opposites(const unsigned long long* __restrict__ key, const uint32_t* __restrict__ half,
+                            const uint32_t* __restrict__ pos_of, const uint8_t* __restrict__ state,
+                            const uint32_t* __restrict__ rank, uint64_t nf, int32_t* __restrict__ copp) {
+  const uint64_t h = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (h >= 3 * nf) return;
+  const uint64_t f = h / 3;
+  if (state[f] != F_TAKEN) return;
+  const uint64_t n = 3 * nf;
+  const unsigned long long k = key[pos_of[h]];
+  const uint32_t x = uint32_t(k >> 32), y = uint32_t(k);
+  const int32_t me = int32_t(3 * uint64_t(rank[f]) + h % 3);
+  int32_t opp = -1;
+  if (x != y) {
+    const unsigned long long rk = (static_cast<unsigned long long>(y) << 32) | x;
+    for (uint64_t j = lower_bound_key(key, n, rk); j < n && key[j] == rk; ++j) {
+      const uint64_t g = half[j] / 3;
+      if (state[g] == F_TAKEN) {
+        opp = int32_t(3 * uint64_t(rank[g]) + half[j] % 3);
+        break;
+      }
+    }
+  } else {
+    // a self-reversed key: the taken half-edges of this run, in insertion order
+    int32_t prev = -1, next = -1;
+    bool seen_me = false;
+    for (uint64_t j = lower_bound_key(key, n, k); j < n && key[j] == k; ++j) {
+      const uint64_t g = half[j] / 3;
+      if (state[g] != F_TAKEN) continue;
+      const int32_t c = int32_t(3 * uint64_t(rank[g]) + half[j] % 3);
+      if (c == me) {
+        seen_me = true;
+        continue;
+      }
+      if (!seen_me) {
+        prev = c;
+      } else {
+        next = c;
+        break;
+      }
+    }
+    opp = next >= 0 ? next : prev;  // linked to the next one, the last to the one before
+  }
+  copp[me] = opp;
+}
+
+__global__ void k_deleted(const int32_t* __restrict__ vcorner, uint64_t nv, uint8_t* __restrict__ deleted) {
+  const uint64_t v = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (v < nv) deleted[v] = vcorner[v] < 0 ? 1 : 0;
+}
+
+// corners_around_vertex (traversal.rs:244-286) from corner c0: visit(c) for
+// every corner of the fan.  Every visited corner belongs to c0's vertex: a
+// corner's opposite lies across the same edge, reversed, or across the same
+// degenerate edge (x, x).  The walk's state is one of the vertex's corners, so
+// a walk that has not ended after deg + 1 steps is in a cycle that misses its
+// start and has already visited all it ever will: guard_max = deg + 2 visits
+// the same set as an unbounded walk.
 template <class F>
-void corners_around_vertex(const bs_corner_table& t, int32_t v, F visit) {
-  const size_t guard_max = t.cvertex.size() + 3;
-  int32_t w = cprev(t.vcorner[v]);
+__device__ void fan_around(const int32_t* __restrict__ copp, int32_t c0, uint32_t guard_max, F visit) {
+  int32_t w = cprev_d(c0);
   const int32_t started = w;
   bool border = false;
-  for (size_t g = 0; g < guard_max; ++g) {
-    visit(cnext(w));
-    w = cprev(w);
-    if (t.copp[w] < 0) {
+  for (uint32_t g = 0; g < guard_max; ++g) {
+    visit(cnext_d(w));
+    w = cprev_d(w);
+    if (copp[w] < 0) {
       border = true;
       break;
     }
-    w = t.copp[w];
+    w = copp[w];
     if (w == started) break;
   }
   w = started;
-  if (border && t.copp[w] >= 0) {
-    w = t.copp[w];
-    for (size_t g = 0; g < guard_max; ++g) {
-      visit(cprev(w));
-      w = cnext(w);
-      if (t.copp[w] < 0) break;
-      w = t.copp[w];
+  if (border && copp[w] >= 0) {
+    w = copp[w];
+    for (uint32_t g = 0; g < guard_max; ++g) {
+      visit(cprev_d(w));
+      w = cnext_d(w);
+      if (copp[w] < 0) break;
+      w = copp[w];
     }
   }
 }
 
-// builder.rs:168-262 on merged points.
-void indexed_build(bs_corner_table& t, const std::vector<float>& uniq, const std::vector<uint32_t>& ids) {
-  const uint64_t nv = uniq.size() / 3, nf = ids.size() / 3;
-  t.pos = uniq;
-  t.deleted.assign(nv, 0);
-  t.vcorner.assign(nv, -1);
-  t.cvertex.clear();
-  t.copp.clear();
-  t.cvertex.reserve(nf * 3);
-  t.copp.reserve(nf * 3);
-  EdgeMap em(nf * 3);
-  auto corner_from = [&](uint32_t a, uint32_t b, uint32_t vertex) {
-    const int32_t c = int32_t(t.cvertex.size());
-    t.cvertex.push_back(int32_t(vertex));
-    t.copp.push_back(-1);
-    if (int32_t* o = em.find(b, a)) {
-      t.copp[c] = *o;
-      t.copp[*o] = c;
-    }
-    em.put(a, b, c);
-    t.vcorner[vertex] = c;
-    return c;
-  };
-  for (uint64_t f = 0; f < nf; ++f) {
-    const uint32_t a = ids[3 * f], b = ids[3 * f + 1], c = ids[3 * f + 2];
-    // a face repeating a directed edge would be non-manifold: skipped (builder.rs:188-194)
-    if (em.find(b, c) || em.find(c, a) || em.find(a, b)) continue;
-    corner_from(b, c, a);
-    corner_from(c, a, b);
-    corner_from(a, b, c);
+// Pass 1 per vertex (builder.rs:224-262, finish): the fan around the vertex's
+// corner keeps the vertex (fan 0); then, while one of its corners is in no fan
+// yet, the smallest such corner seeds a new vertex and every corner of that
+// seed's fan moves to it, including corners an earlier fan had taken (a walk
+// around a non-manifold vertex can cross fans).  fan[c] = the last fan that
+// visited c; seed[vstart[v] + k - 1] = the corner of fan k, the new vertex's
+// corner.
+__global__ void k_fans(const int32_t* __restrict__ vcorner, const uint8_t* __restrict__ deleted,
+                       const uint32_t* __restrict__ vstart, const int32_t* __restrict__ vlist,
+                       const int32_t* __restrict__ copp, uint64_t nv, int32_t* __restrict__ fan,
+                       int32_t* __restrict__ seed, uint32_t* __restrict__ extra) {
+  const uint64_t v = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (v > nv) return;
+  if (v == nv) {
+    extra[nv] = 0;
+    return;
   }
-  // finish(): delete isolated vertices, split non-manifold vertices
-  for (uint64_t v = 0; v < nv; ++v)
-    if (t.vcorner[v] < 0) t.deleted[v] = 1;
-  // corners of every vertex in increasing corner order (BTreeSet)
-  std::vector<uint32_t> start(nv + 1, 0);
-  for (int32_t vx : t.cvertex) start[vx + 1]++;
-  for (uint64_t v = 0; v < nv; ++v) start[v + 1] += start[v];
-  std::vector<int32_t> corners(t.cvertex.size());
-  {
-    std::vector<uint32_t> fill(start.begin(), start.end() - 1);
-    for (int32_t c = 0; c < int32_t(t.cvertex.size()); ++c) corners[fill[t.cvertex[c]]++] = c;
-  }
-  std::vector<uint8_t> seen(t.cvertex.size(), 0);
-  for (uint64_t v = 0; v < nv; ++v) {
-    if (t.deleted[v]) continue;
-    corners_around_vertex(t, int32_t(v), [&](int32_t c) { seen[c] = 1; });
-    const float px = t.pos[3 * v], py = t.pos[3 * v + 1], pz = t.pos[3 * v + 2];
-    for (uint32_t k = start[v]; k < start[v + 1]; ++k) {
-      const int32_t ci = corners[k];
-      if (seen[ci]) continue;
-      const int32_t dup = int32_t(t.vcorner.size());
-      t.pos.push_back(px);
-      t.pos.push_back(py);
-      t.pos.push_back(pz);
-      t.deleted.push_back(0);
-      t.vcorner.push_back(ci);
-      seen[ci] = 1;
-      corners_around_vertex(t, dup, [&](int32_t c) {
-        t.cvertex[c] = dup;
-        seen[c] = 1;
-      });
+  uint32_t nfan = 0;
+  if (!deleted[v]) {
+    const uint32_t b = vstart[v], e = vstart[v + 1], guard = e - b + 2;
+    for (uint32_t j = b; j < e; ++j) fan[vlist[j]] = -1;
+    fan_around(copp, vcorner[v], guard, [&](int32_t c) { fan[c] = 0; });
+    for (uint32_t j = b; j < e; ++j) {
+      const int32_t ci = vlist[j];
+      if (fan[ci] >= 0) continue;
+      seed[b + nfan] = ci;
+      ++nfan;
+      fan_around(copp, ci, guard, [&](int32_t c) { fan[c] = int32_t(nfan); });
     }
   }
+  extra[v] = nfan;
+}
+
+// Pass 2 per vertex: the new vertices of its extra fans (builder.rs:247,
+// add_vertex at the vertex's position with the seed as its corner).
+__global__ void k_split(const uint8_t* deleted, const uint32_t* __restrict__ vstart,
+                        const int32_t* __restrict__ vlist, const int32_t* __restrict__ fan,
+                        const int32_t* __restrict__ seed, const uint32_t* __restrict__ extra_off, uint64_t nv,
+                        float* __restrict__ pos, int32_t* __restrict__ vcorner, uint8_t* del_out,
+                        int32_t* __restrict__ cvertex) {
+  const uint64_t v = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (v >= nv || deleted[v]) return;
+  const uint32_t base = uint32_t(nv) + extra_off[v], n_extra = extra_off[v + 1] - extra_off[v];
+  if (n_extra == 0) return;
+  for (uint32_t j = vstart[v]; j < vstart[v + 1]; ++j) {
+    const int32_t c = vlist[j];
+    const int32_t k = fan[c];
+    if (k > 0) cvertex[c] = int32_t(base + uint32_t(k) - 1);
+  }
+  for (uint32_t k = 0; k < n_extra; ++k) {
+    const uint32_t nvx = base + k;
+    vcorner[nvx] = seed[vstart[v] + k];
+    del_out[nvx] = 0;
+    pos[3 * uint64_t(nvx)] = pos[3 * v];
+    pos[3 * uint64_t(nvx) + 1] = pos[3 * v + 1];
+    pos[3 * uint64_t(nvx) + 2] = pos[3 * v + 2];
+  }
+}
+
+__global__ void k_corner_keys(const int32_t* __restrict__ cvertex, uint64_t nc, uint32_t* __restrict__ key,
+                              int32_t* __restrict__ val) {
+  const uint64_t c = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (c >= nc) return;
+  key[c] = uint32_t(cvertex[c]);
+  val[c] = int32_t(c);
+}
+
+__global__ void k_vertex_counts(const int32_t* __restrict__ cvertex, uint64_t nc, uint32_t* __restrict__ cnt) {
+  const uint64_t c = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  if (c < nc) atomicAdd(cnt + cvertex[c], 1u);
+}
+
+template <class T>
+void scan_ex(bs_ctx* ctx, const T* in, T* out, uint64_t n) {
+  size_t tmp = 0;
+  BS_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, in, out, n, ctx->stream));
+  DBuf<uint8_t> t(ctx, tmp);
+  BS_CUDA(cub::DeviceScan::ExclusiveSum(t.p, tmp, in, out, n, ctx->stream));
 }
 
 }  // namespace
 
 bs_corner_table* corner_table_from_device_soup(bs_ctx* ctx, const float* d_pts, uint64_t n_points) {
-  std::vector<uint32_t> ids;
-  std::vector<float> uniq;
-  merge_points_gpu(ctx, d_pts, n_points, ids, uniq);
+  cudaStream_t s = ctx->stream;
+  DBuf<uint32_t> ids;
+  DBuf<float> uniq;
+  uint32_t nu = 0;
+  merge_points_gpu(ctx, d_pts, n_points, ids, uniq, nu);
   auto* t = new bs_corner_table();
-  indexed_build(*t, uniq, ids);
+  const uint64_t nf = n_points / 3, nv = nu;
+  if (nf == 0) {
+    t->pos.resize(uint64_t(nu) * 3);
+    if (nu) BS_CUDA(cudaMemcpy(t->pos.data(), uniq.p, uint64_t(nu) * 3 * sizeof(float), cudaMemcpyDeviceToHost));
+    t->deleted.assign(nu, 1);
+    t->vcorner.assign(nu, -1);
+    return t;
+  }
+  const uint64_t nh = 3 * nf;
+  // faces taken or skipped (builder.rs:186-194)
+  DBuf<unsigned long long> key(ctx, nh), skey(ctx, nh);
+  DBuf<uint32_t> half(ctx, nh), shalf(ctx, nh);
+  BS_KERNEL(ctx, "k_half_keys", (k_half_keys<<<nbc(nf, 256), 256, 0, s>>>(ids.p, nf, key.p, half.p)));
+  {
+    size_t tmp = 0;
+    BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, key.p, skey.p, half.p, shalf.p, int(nh), 0, 64, s));
+    DBuf<uint8_t> tb(ctx, tmp);
+    BS_CUDA(cub::DeviceRadixSort::SortPairs(tb.p, tmp, key.p, skey.p, half.p, shalf.p, int(nh), 0, 64, s));
+  }
+  key.reset();
+  half.reset();
+  DBuf<uint32_t> head(ctx, nh), run_start(ctx, nh), pos_of(ctx, nh);
+  DBuf<uint8_t> shared_key(ctx, nf), state(ctx, nf);
+  BS_CUDA(cudaMemsetAsync(shared_key.p, 0, nf, s));
+  BS_KERNEL(ctx, "k_half_runs", (k_half_runs<<<nbc(nh, 256), 256, 0, s>>>(skey.p, shalf.p, nh, head.p, pos_of.p, shared_key.p)));
+  {
+    size_t tmp = 0;
+    BS_CUDA(cub::DeviceScan::InclusiveScan(nullptr, tmp, head.p, run_start.p, MaxU32(), nh, s));
+    DBuf<uint8_t> tb(ctx, tmp);
+    BS_CUDA(cub::DeviceScan::InclusiveScan(tb.p, tmp, head.p, run_start.p, MaxU32(), nh, s));
+  }
+  head.reset();
+  BS_KERNEL(ctx, "k_face_init", (k_face_init<<<nbc(nf, 256), 256, 0, s>>>(shared_key.p, nf, state.p)));
+  {
+    DBuf<unsigned long long> left(ctx, 1);
+    for (uint64_t round = 0;; ++round) {
+      if (round > nf + 1) fail(BS_ERR_CAPACITY, "corner table: face rounds did not settle");
+      BS_CUDA(cudaMemsetAsync(left.p, 0, sizeof(unsigned long long), s));
+      BS_KERNEL(ctx, "k_face_round", (k_face_round<<<nbc(nf, 256), 256, 0, s>>>(shalf.p, run_start.p, pos_of.p, nf, state.p, left.p)));
+      unsigned long long h = 0;
+      read_back(ctx, &h, left.p, sizeof h);
+      if (h == 0) break;
+    }
+  }
+  DBuf<uint32_t> flag(ctx, nf + 1), rank(ctx, nf + 1);
+  BS_KERNEL(ctx, "k_taken_flags", (k_taken_flags<<<nbc(nf + 1, 256), 256, 0, s>>>(state.p, nf, flag.p)));
+  scan_ex(ctx, flag.p, rank.p, nf + 1);
+  uint32_t n_taken = 0;
+  read_back(ctx, &n_taken, rank.p + nf, sizeof n_taken);
+  const uint64_t nc = 3 * uint64_t(n_taken);
+  // corners, opposites, vertex corners (builder.rs:196-208, corner_from)
+  DBuf<int32_t> cvertex(ctx, nc), copp(ctx, nc), vcorner(ctx, nv + nc);
+  BS_CUDA(cudaMemsetAsync(vcorner.p, 0xff, (nv + nc) * sizeof(int32_t), s));
+  if (nc) {
+    BS_KERNEL(ctx, "k_corner_vertices", (k_corner_vertices<<<nbc(nf, 256), 256, 0, s>>>(ids.p, state.p, rank.p, nf, cvertex.p, vcorner.p)));
+    BS_KERNEL(ctx, "k_opposites", (k_opposites<<<nbc(nh, 256), 256, 0, s>>>(skey.p, shalf.p, pos_of.p, state.p, rank.p, nf, copp.p)));
+  }
+  skey.reset();
+  shalf.reset();
+  pos_of.reset();
+  run_start.reset();
+  // finish (builder.rs:224-262): isolated vertices, extra fans
+  DBuf<uint8_t> deleted(ctx, nv + nc);
+  BS_KERNEL(ctx, "k_deleted", (k_deleted<<<nbc(nv, 256), 256, 0, s>>>(vcorner.p, nv, deleted.p)));
+  DBuf<float> pos(ctx, (nv + nc) * 3);
+  if (nv) BS_CUDA(cudaMemcpyAsync(pos.p, uniq.p, nv * 3 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  uint32_t n_extra = 0;
+  if (nc) {
+    DBuf<uint32_t> vcnt(ctx, nv + 1), vstart(ctx, nv + 1), ckey(ctx, nc), ckey2(ctx, nc);
+    DBuf<int32_t> cval(ctx, nc), vlist(ctx, nc), fan(ctx, nc);
+    // corners of every vertex in increasing order (a stable sort by vertex)
+    BS_CUDA(cudaMemsetAsync(vcnt.p, 0, (nv + 1) * sizeof(uint32_t), s));
+    BS_KERNEL(ctx, "k_vertex_counts", (k_vertex_counts<<<nbc(nc, 256), 256, 0, s>>>(cvertex.p, nc, vcnt.p)));
+    scan_ex(ctx, vcnt.p, vstart.p, nv + 1);
+    BS_KERNEL(ctx, "k_corner_keys", (k_corner_keys<<<nbc(nc, 256), 256, 0, s>>>(cvertex.p, nc, ckey.p, cval.p)));
+    {
+      int bits = 1;
+      while ((uint64_t(1) << bits) < nv) ++bits;
+      size_t tmp = 0;
+      BS_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, ckey.p, ckey2.p, cval.p, vlist.p, int(nc), 0, bits, s));
+      DBuf<uint8_t> tb(ctx, tmp);
+      BS_CUDA(cub::DeviceRadixSort::SortPairs(tb.p, tmp, ckey.p, ckey2.p, cval.p, vlist.p, int(nc), 0, bits, s));
+    }
+    DBuf<uint32_t> extra(ctx, nv + 1), extra_off(ctx, nv + 1);
+    BS_KERNEL(ctx, "k_fans", (k_fans<<<nbc(nv + 1, 128), 128, 0, s>>>(vcorner.p, deleted.p, vstart.p, vlist.p, copp.p, nv, fan.p,
+                                                                   cval.p, extra.p)));
+    scan_ex(ctx, extra.p, extra_off.p, nv + 1);
+    read_back(ctx, &n_extra, extra_off.p + nv, sizeof n_extra);
+    if (n_extra)
+      BS_KERNEL(ctx, "k_split", (k_split<<<nbc(nv, 128), 128, 0, s>>>(deleted.p, vstart.p, vlist.p, fan.p, cval.p, extra_off.p, nv, pos.p,
+                                                                    vcorner.p, deleted.p, cvertex.p)));
+  }
+  const uint64_t slots = nv + n_extra;
+  t->pos.resize(slots * 3);
+  t->deleted.resize(slots);
+  t->vcorner.resize(slots);
+  t->cvertex.resize(nc);
+  t->copp.resize(nc);
+  if (slots) {
+    BS_CUDA(cudaMemcpyAsync(t->pos.data(), pos.p, slots * 3 * sizeof(float), cudaMemcpyDeviceToHost, s));
+    BS_CUDA(cudaMemcpyAsync(t->deleted.data(), deleted.p, slots, cudaMemcpyDeviceToHost, s));
+    BS_CUDA(cudaMemcpyAsync(t->vcorner.data(), vcorner.p, slots * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  }
+  if (nc) {
+    BS_CUDA(cudaMemcpyAsync(t->cvertex.data(), cvertex.p, nc * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    BS_CUDA(cudaMemcpyAsync(t->copp.data(), copp.p, nc * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  }
+  BS_CUDA(cudaStreamSynchronize(s));
   return t;
 }
 
