@@ -10,12 +10,15 @@
 // sweep is a function of its own input, the outputs of the three neighbours
 // before it in the sweep order and the inputs of the three after it; leaves
 // it spawns lie after it.  The reference's result is therefore the unique
-// fixed point of that dependency order.  Here every leaf is swept at once,
-// and a leaf is swept again whenever a face it read from a before-neighbour
-// changes (k_relax), until nothing changes; a final check drops leaves that
-// only an unconverged pass asked for.  Inside a leaf the voxels go by
-// diagonal planes ux + uy + uz, which keeps their order.  So the sweeps are
-// bit-identical to the reference's sequential ones.
+// fixed point of that dependency order.  Here every leaf is queued at once
+// and one persistent kernel (k_relax_ring) keeps every resident warp taking
+// the next queued leaf; a leaf is queued again whenever a face it read from a
+// before-neighbour changes, until nothing is queued or being swept (no host
+// round trip per wave of sweeps); a final check drops leaves that only an
+// unconverged sweep asked for.  Inside a leaf the voxels go by diagonal
+// planes ux + uy + uz, which keeps their order.  So the sweeps are
+// bit-identical to the reference's sequential ones, in any order the queue
+// happens to take them.
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -158,6 +161,7 @@ struct Sweep {
   int* dirty;           // queued for a sweep
   int* nbr;             // [slot][6] slot of the face neighbour (-x, +x, -y, +y, -z, +z) or -1
   int* linked;          // nbr of the slot is filled in
+  int* busy;            // a warp is sweeping the slot (persistent relaxation)
   LeafHash hash;
   int* n_slots;
   uint64_t cap;
@@ -165,7 +169,18 @@ struct Sweep {
   int* changed;
   int sx, sy, sz, neg;
   float lim, h;
+  // work queue of the persistent relaxation (null: queue into lists)
+  unsigned long long* ring;  // entry: position << 32 | slot; RING_EMPTY when free
+  uint32_t ring_mask;
+  unsigned* qhead;           // next position to take
+  unsigned* qtail;           // next position to fill
+  int* pending;              // queued or being swept
+  int* qerr;                 // a bounded wait gave up
+  unsigned long long* n_sweeps;
 };
+
+constexpr unsigned long long RING_EMPTY = ~0ull;
+constexpr int RING_SPIN = 1 << 24;  // polls before a wait gives up (with back-off, seconds)
 
 constexpr int SW_WARPS = 4;
 constexpr int PAD = 10;  // a leaf with a one-voxel halo: 10 x 10 x 10
@@ -211,9 +226,33 @@ __device__ __forceinline__ int find_alive(const Sweep& S, int x, int y, int z) {
   return (l >= 0 && is_alive(S, l)) ? l : -1;
 }
 
-// Queues leaf l for the next pass unless it is queued already.
+// Appends slot l to the work queue.  pending counts it before it can be
+// taken, so pending reaches 0 only when no leaf is queued or being swept.
+// A leaf is queued at most once at a time (its dirty flag), so the ring,
+// larger than the slot count, never holds more entries than it has room for;
+// an entry is written only into a free cell (a bounded wait for the taker of
+// the cell's previous entry to clear it).
+__device__ void ring_push(const Sweep& S, int l) {
+  atomicAdd(S.pending, 1);
+  __threadfence();
+  const unsigned pos = atomicAdd(S.qtail, 1u);
+  unsigned long long* cell = S.ring + (pos & S.ring_mask);
+  const unsigned long long e = (uint64_t(pos) << 32) | uint32_t(l);
+  for (int it = 0; it < RING_SPIN; ++it) {
+    if (atomicCAS(cell, RING_EMPTY, e) == RING_EMPTY) return;
+    __nanosleep(64);
+  }
+  atomicExch(S.qerr, 1);
+}
+
+// Queues leaf l for a sweep unless it is queued already.
 __device__ __forceinline__ void mark_dirty(const Sweep& S, int l, int* list, int* cnt) {
-  if (atomicExch(&S.dirty[l], 1) == 0) list[atomicAdd(cnt, 1)] = l;
+  if (atomicExch(&S.dirty[l], 1) == 0) {
+    if (S.ring)
+      ring_push(S, l);
+    else
+      list[atomicAdd(cnt, 1)] = l;
+  }
 }
 
 // Brings back a leaf dropped earlier in the offset and queues it.
@@ -289,146 +328,222 @@ __device__ __forceinline__ void fill_order(const Sweep& S, uint32_t* order) {
 // is missing from it until that neighbour's first sweep links both ways; it
 // only matters as the target of a changed after-face, which falls back to the
 // hash.
-__global__ void __launch_bounds__(32 * SW_WARPS, 8) k_relax(Sweep S, const int* __restrict__ list, const int* __restrict__ n_list,
-                                                            int* __restrict__ next, int* __restrict__ n_next,
-                                                            int* __restrict__ n_clear) {
-  __shared__ float tile[SW_WARPS][PAD * PAD * PAD];
-  __shared__ float oldf[SW_WARPS][3 * 64];
-  __shared__ uint32_t oldm[SW_WARPS][6];
-  __shared__ uint32_t frz[SW_WARPS][16];
-  __shared__ uint32_t order[512];
-  if (blockIdx.x == 0 && threadIdx.x == 0) *n_clear = 0;  // the counter the pass after next fills
-  fill_order(S, order);
-  __syncthreads();
+// Sweeps one leaf from its input with its neighbours' current faces; an
+// after-face that changed queues the neighbour behind it, and a face that
+// asks for a missing neighbour creates it.  Repeated until nothing is queued,
+// the outputs reach the unique fixed point of the before/after dependency
+// order — the result of the reference's sequential sweep, whose queue pops
+// every before-neighbour first.
+//
+// Neighbours come from the slot's cached `nbr`.  A dropped neighbour reads as
+// empty (its faces are zero).  A neighbour created after the cache was filled
+// is missing from it until that neighbour's first sweep links both ways; it
+// only matters as the target of a changed after-face, which falls back to the
+// hash.
+struct RelaxSmem {
+  float tile[SW_WARPS][PAD * PAD * PAD];
+  float oldf[SW_WARPS][3 * 64];
+  uint32_t oldm[SW_WARPS][6];
+  uint32_t frz[SW_WARPS][16];
+  uint32_t order[512];
+};
+
+__device__ void relax_leaf(const Sweep& S, int leaf, RelaxSmem& sm, int* __restrict__ next,
+                           int* __restrict__ n_next) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  float* W = tile[w];
-  uint32_t* F = frz[w];
+  float* W = sm.tile[w];
+  uint32_t* F = sm.frz[w];
+  const uint32_t* order = sm.order;
+  float (*oldf)[3 * 64] = sm.oldf;
+  uint32_t (*oldm)[6] = sm.oldm;
   const int sdir[3] = {S.sx, S.sy, S.sz};
-  const int total = *n_list;
-  for (int item = blockIdx.x * SW_WARPS + w; item < total; item += gridDim.x * SW_WARPS) {
-    const int leaf = list[item];
-    int live = 0;
-    if (lane == 0) {
-      atomicExch(&S.dirty[leaf], 0);
-      __threadfence();
-      live = is_alive(S, leaf);
-    }
-    if (!__shfl_sync(0xffffffffu, live, 0)) continue;
-    const int4 org = S.org[leaf];
-    int nb = -1;
-    if (lane < 6) {
-      if (__ldcg(&S.linked[leaf])) {
-        nb = __ldcg(&S.nbr[uint64_t(leaf) * 6 + lane]);
-      } else {  // first sweep of a created slot: link both ways
-        const int ax = lane >> 1, step = (lane & 1) ? 8 : -8;
-        nb = S.hash.find(org.x + (ax == 0 ? step : 0), org.y + (ax == 1 ? step : 0), org.z + (ax == 2 ? step : 0));
-        S.nbr[uint64_t(leaf) * 6 + lane] = nb;
-        if (nb >= 0) S.nbr[uint64_t(nb) * 6 + (lane ^ 1)] = leaf;
-      }
-    }
-    const float* iv = S.in_val + uint64_t(leaf) * 512;
-    const uint32_t* im = S.in_msk + uint64_t(leaf) * 16;
-    for (int k = lane; k < 512; k += 32) {
-      const uint32_t m = im[k >> 5];
-      const float v = iv[k];
-      W[pad_idx(k >> 6, (k >> 3) & 7, k & 7)] = ((m >> lane) & 1u) ? v : INFINITY;
-    }
-    if (lane < 16) F[lane] = S.frz[uint64_t(leaf) * 16 + lane];
-    // this leaf's faces as published before: only this warp writes them in this pass
-    for (int k = lane; k < 3 * 64; k += 32) oldf[w][k] = __ldcg(&S.pub_val[uint64_t(leaf) * 192 + k]);
-    if (lane < 6) oldm[w][lane] = __ldcg(&S.pub_msk[uint64_t(leaf) * 6 + lane]);
-    // halo: all twelve loads of this lane first, then the tile writes
-    float hv[12];
-    uint32_t hm[12];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      const int n = __shfl_sync(0xffffffffu, nb, k);
-      const int ax = k >> 1, side = k & 1;
-      // the neighbour on the - side is before the leaf when the sweep goes +
-      const bool before = (side == 0) == (sdir[ax] > 0);
-      const float* fv = before ? S.pub_val : S.inf_val;
-      const uint32_t* fm = before ? S.pub_msk : S.inf_msk;
-#pragma unroll
-      for (int r = 0; r < 2; ++r) {
-        hv[2 * k + r] = INFINITY;
-        hm[2 * k + r] = 0u;
-        if (n >= 0) {
-          hv[2 * k + r] = __ldcg(&fv[(uint64_t(n) * 3 + ax) * 64 + lane + 32 * r]);
-          hm[2 * k + r] = __ldcg(&fm[(uint64_t(n) * 3 + ax) * 2 + r]);
-        }
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      const int ax = k >> 1, side = k & 1;
-#pragma unroll
-      for (int r = 0; r < 2; ++r) {
-        const int i = lane + 32 * r;
-        W[face_pad(ax, side ? 8 : -1, i)] = ((hm[2 * k + r] >> lane) & 1u) ? hv[2 * k + r] : INFINITY;
-      }
-    }
-    __syncwarp();
-    for (int q = 0; q < 22; ++q) {
-      const int beg = c_plane_off[q], end = c_plane_off[q + 1];
-      for (int k = beg + lane; k < end; k += 32) {
-        const uint32_t e = order[k];
-        const int o = int(e >> 16);
-        if (!bit(F, o)) sweep_voxel(W, int(e & 0xffffu), S.neg != 0, S.lim, S.h);
-      }
-      __syncwarp();
-    }
-    float* ov = S.out_val + uint64_t(leaf) * 512;
-    for (int k = lane; k < 512; k += 32) {
-      const float t = W[pad_idx(k >> 6, (k >> 3) & 7, k & 7)];
-      const bool on = t != INFINITY;
-      ov[k] = on ? t : iv[k];
-      const uint32_t mw = __ballot_sync(0xffffffffu, on);
-      if (lane == 0) S.out_msk[uint64_t(leaf) * 16 + (k >> 5)] = mw;
-    }
-    uint32_t flags = 0;  // bit ax: face changed, bit 3 + ax: face asks for the next leaf
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-      const int fl = sdir[ax] > 0 ? 7 : 0;
-      const uint64_t fb = uint64_t(leaf) * 3 + ax;
-      bool diff = false, any = false;
-#pragma unroll
-      for (int r = 0; r < 2; ++r) {
-        const int i = lane + 32 * r;
-        const float t = W[face_pad(ax, fl, i)];
-        const bool on = t != INFINITY;
-        const float v = on ? t : 0.f;
-        any |= spawns(S, on, v);
-        const uint32_t mw = __ballot_sync(0xffffffffu, on);
-        diff |= (mw != oldm[w][2 * ax + r]) || (__float_as_uint(oldf[w][ax * 64 + i]) != __float_as_uint(v));
-        S.pub_val[fb * 64 + i] = v;
-        if (lane == 0) S.pub_msk[fb * 2 + r] = mw;
-      }
-      if (__any_sync(0xffffffffu, diff)) flags |= 1u << ax;
-      if (__any_sync(0xffffffffu, any)) flags |= 8u << ax;
-    }
-    int after3[3];
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) after3[ax] = __shfl_sync(0xffffffffu, nb, 2 * ax + (sdir[ax] > 0 ? 1 : 0));
+  int live = 0;
+  if (lane == 0) {
+    atomicExch(&S.dirty[leaf], 0);
     __threadfence();
-    __syncwarp();
-    if (lane == 0) {
-      S.linked[leaf] = 1;
-      for (int ax = 0; ax < 3; ++ax) {
-        const bool chg = (flags >> ax) & 1u, spw = (flags >> (3 + ax)) & 1u;
-        if (!chg && !spw) continue;
-        const int x = org.x + (ax == 0 ? 8 * sdir[0] : 0), y = org.y + (ax == 1 ? 8 * sdir[1] : 0),
-                  z = org.z + (ax == 2 ? 8 * sdir[2] : 0);
-        int after = after3[ax];
-        if (after < 0) after = S.hash.find(x, y, z);  // created after the cache was filled
-        if (chg && after >= 0) mark_dirty(S, after, next, n_next);
-        if (spw) {
-          if (after < 0) request_leaf(S, x, y, z, next, n_next);
-          else revive_leaf(S, after, next, n_next);
-        }
+    live = is_alive(S, leaf);
+  }
+  if (!__shfl_sync(0xffffffffu, live, 0)) return;
+  const int4 org = S.org[leaf];
+  int nb = -1;
+  if (lane < 6) {
+    if (__ldcg(&S.linked[leaf])) {
+      nb = __ldcg(&S.nbr[uint64_t(leaf) * 6 + lane]);
+    } else {  // first sweep of a created slot: link both ways
+      const int ax = lane >> 1, step = (lane & 1) ? 8 : -8;
+      nb = S.hash.find(org.x + (ax == 0 ? step : 0), org.y + (ax == 1 ? step : 0), org.z + (ax == 2 ? step : 0));
+      S.nbr[uint64_t(leaf) * 6 + lane] = nb;
+      if (nb >= 0) S.nbr[uint64_t(nb) * 6 + (lane ^ 1)] = leaf;
+    }
+  }
+  const float* iv = S.in_val + uint64_t(leaf) * 512;
+  const uint32_t* im = S.in_msk + uint64_t(leaf) * 16;
+  for (int k = lane; k < 512; k += 32) {
+    const uint32_t m = im[k >> 5];
+    const float v = iv[k];
+    W[pad_idx(k >> 6, (k >> 3) & 7, k & 7)] = ((m >> lane) & 1u) ? v : INFINITY;
+  }
+  if (lane < 16) F[lane] = S.frz[uint64_t(leaf) * 16 + lane];
+  // this leaf's faces as published before: only this warp writes them in this pass
+  for (int k = lane; k < 3 * 64; k += 32) oldf[w][k] = __ldcg(&S.pub_val[uint64_t(leaf) * 192 + k]);
+  if (lane < 6) oldm[w][lane] = __ldcg(&S.pub_msk[uint64_t(leaf) * 6 + lane]);
+  // halo: all twelve loads of this lane first, then the tile writes
+  float hv[12];
+  uint32_t hm[12];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const int n = __shfl_sync(0xffffffffu, nb, k);
+    const int ax = k >> 1, side = k & 1;
+    // the neighbour on the - side is before the leaf when the sweep goes +
+    const bool before = (side == 0) == (sdir[ax] > 0);
+    const float* fv = before ? S.pub_val : S.inf_val;
+    const uint32_t* fm = before ? S.pub_msk : S.inf_msk;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      hv[2 * k + r] = INFINITY;
+      hm[2 * k + r] = 0u;
+      if (n >= 0) {
+        hv[2 * k + r] = __ldcg(&fv[(uint64_t(n) * 3 + ax) * 64 + lane + 32 * r]);
+        hm[2 * k + r] = __ldcg(&fm[(uint64_t(n) * 3 + ax) * 2 + r]);
       }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const int ax = k >> 1, side = k & 1;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int i = lane + 32 * r;
+      W[face_pad(ax, side ? 8 : -1, i)] = ((hm[2 * k + r] >> lane) & 1u) ? hv[2 * k + r] : INFINITY;
+    }
+  }
+  __syncwarp();
+  for (int q = 0; q < 22; ++q) {
+    const int beg = c_plane_off[q], end = c_plane_off[q + 1];
+    for (int k = beg + lane; k < end; k += 32) {
+      const uint32_t e = order[k];
+      const int o = int(e >> 16);
+      if (!bit(F, o)) sweep_voxel(W, int(e & 0xffffu), S.neg != 0, S.lim, S.h);
     }
     __syncwarp();
   }
+  float* ov = S.out_val + uint64_t(leaf) * 512;
+  for (int k = lane; k < 512; k += 32) {
+    const float t = W[pad_idx(k >> 6, (k >> 3) & 7, k & 7)];
+    const bool on = t != INFINITY;
+    ov[k] = on ? t : iv[k];
+    const uint32_t mw = __ballot_sync(0xffffffffu, on);
+    if (lane == 0) S.out_msk[uint64_t(leaf) * 16 + (k >> 5)] = mw;
+  }
+  uint32_t flags = 0;  // bit ax: face changed, bit 3 + ax: face asks for the next leaf
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    const int fl = sdir[ax] > 0 ? 7 : 0;
+    const uint64_t fb = uint64_t(leaf) * 3 + ax;
+    bool diff = false, any = false;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int i = lane + 32 * r;
+      const float t = W[face_pad(ax, fl, i)];
+      const bool on = t != INFINITY;
+      const float v = on ? t : 0.f;
+      any |= spawns(S, on, v);
+      const uint32_t mw = __ballot_sync(0xffffffffu, on);
+      diff |= (mw != oldm[w][2 * ax + r]) || (__float_as_uint(oldf[w][ax * 64 + i]) != __float_as_uint(v));
+      S.pub_val[fb * 64 + i] = v;
+      if (lane == 0) S.pub_msk[fb * 2 + r] = mw;
+    }
+    if (__any_sync(0xffffffffu, diff)) flags |= 1u << ax;
+    if (__any_sync(0xffffffffu, any)) flags |= 8u << ax;
+  }
+  int after3[3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) after3[ax] = __shfl_sync(0xffffffffu, nb, 2 * ax + (sdir[ax] > 0 ? 1 : 0));
+  __threadfence();
+  __syncwarp();
+  if (lane == 0) {
+    S.linked[leaf] = 1;
+    for (int ax = 0; ax < 3; ++ax) {
+      const bool chg = (flags >> ax) & 1u, spw = (flags >> (3 + ax)) & 1u;
+      if (!chg && !spw) continue;
+      const int x = org.x + (ax == 0 ? 8 * sdir[0] : 0), y = org.y + (ax == 1 ? 8 * sdir[1] : 0),
+                z = org.z + (ax == 2 ? 8 * sdir[2] : 0);
+      int after = after3[ax];
+      if (after < 0) after = S.hash.find(x, y, z);  // created after the cache was filled
+      if (chg && after >= 0) mark_dirty(S, after, next, n_next);
+      if (spw) {
+        if (after < 0) request_leaf(S, x, y, z, next, n_next);
+        else revive_leaf(S, after, next, n_next);
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// The queue of a persistent relaxation: the listed leaves, positions 0..n-1.
+__global__ void k_ring_start(Sweep S, const int* __restrict__ list, const int* __restrict__ n_list) {
+  const int n = *n_list;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) S.ring[i] = (uint64_t(i) << 32) | uint32_t(list[i]);
+  if (i == 0) {
+    *S.qhead = 0u;
+    *S.qtail = unsigned(n);
+    *S.pending = n;
+  }
+}
+
+// Persistent relaxation: every warp takes the next queued leaf, sweeps it
+// (queueing the leaves it changes) and takes another, until no leaf is
+// queued or being swept.  Waits are bounded; a wait that gives up sets qerr
+// and ends the warp (the offset then fails).
+__global__ void __launch_bounds__(32 * SW_WARPS, 8) k_relax_ring(Sweep S) {
+  __shared__ RelaxSmem sm;
+  fill_order(S, sm.order);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  unsigned long long swept = 0;
+  for (;;) {
+    int leaf = -1;
+    if (lane == 0) {
+      const unsigned pos = atomicAdd(S.qhead, 1u);
+      unsigned long long* cell = S.ring + (pos & S.ring_mask);
+      int it = 0;
+      for (; it < RING_SPIN; ++it) {
+        const unsigned long long e = atomicAdd(cell, 0ull);
+        if (e != RING_EMPTY && unsigned(e >> 32) == pos) {
+          atomicExch(cell, RING_EMPTY);
+          leaf = int(uint32_t(e));
+          break;
+        }
+        if ((it & 7) == 0 && atomicAdd(S.pending, 0) == 0) break;  // nothing left anywhere
+        __nanosleep(it < 64 ? 32 : 256);
+      }
+      if (it == RING_SPIN) atomicExch(S.qerr, 1);
+      __threadfence();
+    }
+    leaf = __shfl_sync(0xffffffffu, leaf, 0);
+    if (leaf < 0) break;
+    // a leaf queued again while it is being swept waits for that sweep
+    int got = 0;
+    if (lane == 0) {
+      for (int it = 0; it < RING_SPIN && !got; ++it) {
+        got = atomicCAS(&S.busy[leaf], 0, 1) == 0;
+        if (!got) __nanosleep(64);
+      }
+      if (!got) atomicExch(S.qerr, 1);
+      __threadfence();
+    }
+    if (__shfl_sync(0xffffffffu, got, 0)) {
+      relax_leaf(S, leaf, sm, nullptr, nullptr);
+      ++swept;
+    }
+    if (lane == 0) {
+      __threadfence();  // this sweep's writes and pushes before it stops counting
+      if (got) atomicExch(&S.busy[leaf], 0);
+      atomicSub(S.pending, 1);
+    }
+  }
+  if (lane == 0 && swept) atomicAdd(S.n_sweeps, swept);
 }
 
 // Neighbour cache of the leaves present when the offset starts.
@@ -604,7 +719,7 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   DBuf<float> val_a(ctx, cap * 512), val_b(ctx, cap * 512), pub_val(ctx, cap * 192), inf_val(ctx, cap * 192);
   DBuf<uint32_t> msk_a(ctx, cap * 16), msk_b(ctx, cap * 16), frz(ctx, cap * 16), pub_msk(ctx, cap * 6),
       inf_msk(ctx, cap * 6);
-  DBuf<int> flags(ctx, cap * 5), list_a(ctx, cap), list_b(ctx, cap), ctl(ctx, 8), nbr(ctx, cap * 6);
+  DBuf<int> flags(ctx, cap * 6), list_a(ctx, cap), list_b(ctx, cap), ctl(ctx, 16), nbr(ctx, cap * 6);
   // every spare slot is an empty leaf: zero inputs, outputs, faces and flags
   BS_CUDA(cudaMemsetAsync(val_a.p, 0, cap * 512 * sizeof(float), s));
   BS_CUDA(cudaMemsetAsync(val_b.p, 0, cap * 512 * sizeof(float), s));
@@ -615,8 +730,8 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   BS_CUDA(cudaMemsetAsync(pub_msk.p, 0, cap * 6 * sizeof(uint32_t), s));
   BS_CUDA(cudaMemsetAsync(inf_val.p, 0, cap * 192 * sizeof(float), s));
   BS_CUDA(cudaMemsetAsync(inf_msk.p, 0, cap * 6 * sizeof(uint32_t), s));
-  BS_CUDA(cudaMemsetAsync(flags.p, 0, cap * 5 * sizeof(int), s));
-  BS_CUDA(cudaMemsetAsync(ctl.p, 0, 8 * sizeof(int), s));
+  BS_CUDA(cudaMemsetAsync(flags.p, 0, cap * 6 * sizeof(int), s));
+  BS_CUDA(cudaMemsetAsync(ctl.p, 0, 16 * sizeof(int), s));
   int* alive = flags.p;
   BS_CUDA(cudaMemcpyAsync(org.p, v->d_origins, n0 * sizeof(int4), cudaMemcpyDeviceToDevice, s));
   BS_CUDA(cudaMemcpyAsync(val_a.p, v->d_values, n0 * 512 * sizeof(float), cudaMemcpyDeviceToDevice, s));
@@ -645,6 +760,7 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   S.wanted = flags.p + 2 * cap;
   S.dirty = flags.p + 3 * cap;
   S.linked = flags.p + 4 * cap;
+  S.busy = flags.p + 5 * cap;
   S.nbr = nbr.p;
   S.hash = hb.h;
   S.n_slots = ctl.p + 3;
@@ -654,6 +770,26 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   S.neg = signbit(limit) ? 1 : 0;
   S.lim = fabsf(limit);
   S.h = h;
+  S.ring = nullptr;
+  // persistent relaxation: one resident grid per phase, its queue in a ring
+  // with room for every slot and four claims per resident warp
+  int occ = 0, n_sm = 0;
+  BS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_relax_ring, 32 * SW_WARPS, 0));
+  BS_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
+  const unsigned ring_grid = unsigned(std::max(1, occ) * std::max(1, n_sm));
+  uint64_t rsize = 1024;
+  while (rsize < cap + 4ull * ring_grid * SW_WARPS) rsize <<= 1;
+  DBuf<unsigned long long> ring_buf(ctx, rsize), sweeps(ctx, 1);
+  BS_CUDA(cudaMemsetAsync(ring_buf.p, 0xff, rsize * sizeof(unsigned long long), s));
+  BS_CUDA(cudaMemsetAsync(sweeps.p, 0, sizeof(unsigned long long), s));
+  Sweep SR = S;  // the same state, queueing into the ring
+  SR.ring = ring_buf.p;
+  SR.ring_mask = uint32_t(rsize - 1);
+  SR.qhead = reinterpret_cast<unsigned*>(ctl.p + 8);
+  SR.qtail = reinterpret_cast<unsigned*>(ctl.p + 9);
+  SR.pending = ctl.p + 10;
+  SR.qerr = ctl.p + 11;
+  SR.n_sweeps = sweeps.p;
   BS_KERNEL(ctx, "k_link", (k_link<<<nb_(n0 * 6, 256), 256, 0, s>>>(S, int(n0))));
   int* lists[2] = {list_a.p, list_b.p};
   float* vals[2] = {val_a.p, val_b.p};
@@ -675,29 +811,39 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
     read_back(ctx, &n, S.n_slots, sizeof(int));
     BS_KERNEL(ctx, "k_sweep_init", (k_sweep_init<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, lists[0], cnt)));
     int pass = 0;
-    for (;;) {
+    {
+      const Sweep SD = [&] {
+        Sweep t = SR;
+        t.sx = S.sx;
+        t.sy = S.sy;
+        t.sz = S.sz;
+        t.in_val = S.in_val;
+        t.in_msk = S.in_msk;
+        t.out_val = S.out_val;
+        t.out_msk = S.out_msk;
+        return t;
+      }();
       for (;;) {
-        int queued = 0;
-        read_back(ctx, &queued, cnt + pass % 3, sizeof(int));
-        if (queued == 0) break;
-        if (pass >= (1 << 16)) fail(BS_ERR_TIMEOUT, "offset: sweep relaxation did not converge");
-        total_sweeps += uint64_t(queued);
-        const unsigned grid = nb_(uint64_t(queued), SW_WARPS);
-        BS_KERNEL(ctx, "k_relax", (k_relax<<<grid, 32 * SW_WARPS, 0, s>>>(S, lists[pass & 1], cnt + pass % 3, lists[(pass + 1) & 1],
-                                                                           cnt + (pass + 1) % 3, cnt + (pass + 2) % 3)));
+        // the queued leaves (lists[0], cnt[0]) into the ring, then one
+        // persistent relaxation until nothing is queued
+        BS_KERNEL(ctx, "k_ring_start", (k_ring_start<<<nb_(cap, 256), 256, 0, s>>>(SD, lists[0], cnt)));
+        BS_KERNEL(ctx, "k_relax_ring", (k_relax_ring<<<ring_grid, 32 * SW_WARPS, 0, s>>>(SD)));
         ++pass;
+        int qe = 0;
+        read_back(ctx, &qe, SR.qerr, sizeof(int));
+        if (qe) fail(BS_ERR_TIMEOUT, "offset: a wait of the persistent relaxation gave up");
+        read_back(ctx, &n, S.n_slots, sizeof(int));
+        if (uint64_t(n) > cap) return false;
+        BS_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int), s));
+        BS_CUDA(cudaMemsetAsync(S.changed, 0, sizeof(int), s));
+        BS_KERNEL(ctx, "k_spawn_clear", (k_spawn_clear<<<nb_(uint64_t(n), 256), 256, 0, s>>>(S, n)));
+        BS_KERNEL(ctx, "k_spawn_mark", (k_spawn_mark<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, lists[0], cnt)));
+        BS_KERNEL(ctx, "k_spawn_drop", (k_spawn_drop<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, lists[0], cnt)));
+        int ch = 0;
+        read_back(ctx, &ch, S.changed, sizeof(int));
+        if (!ch) break;
+        if (pass >= (1 << 16)) fail(BS_ERR_TIMEOUT, "offset: sweep relaxation did not converge");
       }
-      // the passes converged: check that the set of spawned leaves is the one
-      // the final outputs ask for
-      read_back(ctx, &n, S.n_slots, sizeof(int));
-      if (uint64_t(n) > cap) return false;
-      BS_CUDA(cudaMemsetAsync(S.changed, 0, sizeof(int), s));
-      BS_KERNEL(ctx, "k_spawn_clear", (k_spawn_clear<<<nb_(uint64_t(n), 256), 256, 0, s>>>(S, n)));
-      BS_KERNEL(ctx, "k_spawn_mark", (k_spawn_mark<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, lists[pass & 1], cnt + pass % 3)));
-      BS_KERNEL(ctx, "k_spawn_drop", (k_spawn_drop<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, lists[pass & 1], cnt + pass % 3)));
-      int ch = 0;
-      read_back(ctx, &ch, S.changed, sizeof(int));
-      if (!ch) break;
     }
     total_passes += uint64_t(pass);
     int of = 0;
@@ -707,6 +853,11 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   }
   int n = 0;
   read_back(ctx, &n, S.n_slots, sizeof(int));
+  {
+    unsigned long long sw = 0;
+    read_back(ctx, &sw, sweeps.p, sizeof sw);
+    total_sweeps = sw;
+  }
   ctx->last_stats[6] = total_passes;
   ctx->last_stats[7] = total_sweeps;
   ctx->last_stats[8] = BS_STATS_OFFSET;

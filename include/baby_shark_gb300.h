@@ -82,7 +82,8 @@ bs_status bs_ctx_stage_reset(bs_ctx* ctx);
  * winding-number pass, [7] warp-level far-field evaluations (low 32 bits) and
  * exact solid angles (high 32 bits).  A dual contouring call overwrites
  * [6] and [7] with its crossing and cell counts, an offset call with its
- * relaxation passes and leaf sweeps over the 8 sweep directions. */
+ * relaxation phases (persistent launches, one or more per sweep direction)
+ * and leaf sweeps over the 8 sweep directions. */
 bs_status bs_ctx_last_stats(const bs_ctx* ctx, uint64_t* out8);
 /* The same counters and more: [0..7] as above, [8] which call wrote them
  * (bs_stats_kind), [9] (voxel, sub-triangle) pairs whose exact distance a
