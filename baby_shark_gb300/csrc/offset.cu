@@ -95,21 +95,35 @@ __global__ void k_remove_far(const float* __restrict__ values, uint32_t* __restr
   if (b == n - 1 && lane == 0) keep[n] = 0u;
 }
 
-// Leaf copies: LEAVES_PER_BLOCK leaves per block of 128 threads each, one
-// float4 of a leaf's values per thread (one leaf per block measured fastest).
-constexpr int LEAVES_PER_BLOCK = 1;
+// Leaf copies: one warp per leaf, each lane moving four float4 of the leaf's
+// values with all four loads issued before the stores (2 KB in flight per
+// warp), streaming (evict-first) since nothing rereads them here.
+constexpr int COPY_WARPS = 8;
 
-__global__ void __launch_bounds__(128 * LEAVES_PER_BLOCK) k_gather_leaves(
+__device__ __forceinline__ void copy_leaf(uint64_t from, uint64_t to, const int4* __restrict__ oi,
+                                          const float* __restrict__ vi, const uint32_t* __restrict__ mi,
+                                          int4* __restrict__ oo, float* __restrict__ vo, uint32_t* __restrict__ mo) {
+  const int lane = threadIdx.x & 31;
+  const float4* src = reinterpret_cast<const float4*>(vi + from * 512);
+  float4* dst = reinterpret_cast<float4*>(vo + to * 512);
+  const float4 r0 = __ldcs(src + lane), r1 = __ldcs(src + lane + 32), r2 = __ldcs(src + lane + 64),
+               r3 = __ldcs(src + lane + 96);
+  const uint32_t m = lane < 16 ? __ldcs(mi + from * 16 + lane) : 0u;
+  __stcs(dst + lane, r0);
+  __stcs(dst + lane + 32, r1);
+  __stcs(dst + lane + 64, r2);
+  __stcs(dst + lane + 96, r3);
+  if (lane < 16) __stcs(mo + to * 16 + lane, m);
+  if (lane == 0) oo[to] = oi[from];
+}
+
+__global__ void __launch_bounds__(32 * COPY_WARPS) k_gather_leaves(
     const uint32_t* __restrict__ keep, const uint32_t* __restrict__ pos, uint64_t n, const int4* __restrict__ oi,
     const float* __restrict__ vi, const uint32_t* __restrict__ mi, int4* __restrict__ oo, float* __restrict__ vo,
     uint32_t* __restrict__ mo) {
-  const uint64_t b = blockIdx.x * uint64_t(LEAVES_PER_BLOCK) + (threadIdx.x >> 7);
-  const int t = threadIdx.x & 127;
+  const uint64_t b = blockIdx.x * uint64_t(COPY_WARPS) + (threadIdx.x >> 5);
   if (b >= n || !keep[b]) return;
-  const uint64_t d = pos[b];
-  reinterpret_cast<float4*>(vo + d * 512)[t] = reinterpret_cast<const float4*>(vi + b * 512)[t];
-  if (t < 16) mo[d * 16 + t] = mi[b * 16 + t];
-  if (t == 0) oo[d] = oi[b];
+  copy_leaf(b, pos[b], oi, vi, mi, oo, vo, mo);
 }
 
 // --------------------------------------------------------------- sweeps ----
@@ -557,17 +571,23 @@ __global__ void k_link(Sweep S, int n) {
   if (k == 0) S.linked[l] = 1;
 }
 
-// Start of a sweep: out = in, after-faces published from the input, the
-// input's before-layers stored, every live leaf queued.
+// Start of a sweep: after-faces published from the input, the input's
+// before-layers stored, every live leaf queued.  A live leaf's output is
+// written whole by its first sweep (every live leaf is queued, and a leaf
+// stops being live only through k_spawn_drop, which clears its output), so
+// only a slot that is not live gets its (empty) output here: its input is
+// empty too (a dropped leaf's output was cleared, spare slots start empty).
 __global__ void __launch_bounds__(128) k_sweep_init(Sweep S, int n, int* list, int* n_list) {
   const int lane = threadIdx.x & 31;
   const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (l >= n) return;
   const float* iv = S.in_val + uint64_t(l) * 512;
   const uint32_t* im = S.in_msk + uint64_t(l) * 16;
-  for (int k = lane; k < 128; k += 32)
-    reinterpret_cast<float4*>(S.out_val + uint64_t(l) * 512)[k] = reinterpret_cast<const float4*>(iv)[k];
-  if (lane < 16) S.out_msk[uint64_t(l) * 16 + lane] = im[lane];
+  if (!S.alive[l]) {
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k = lane; k < 128; k += 32) reinterpret_cast<float4*>(S.out_val + uint64_t(l) * 512)[k] = z;
+    if (lane < 16) S.out_msk[uint64_t(l) * 16 + lane] = 0u;
+  }
   const int sdir[3] = {S.sx, S.sy, S.sz};
   for (int ax = 0; ax < 3; ++ax) {
     for (int side = 0; side < 2; ++side) {
@@ -666,16 +686,12 @@ __global__ void k_leaf_keys(const int4* __restrict__ org, uint64_t n, unsigned l
   idx[i] = uint32_t(i);
 }
 
-__global__ void __launch_bounds__(128 * LEAVES_PER_BLOCK) k_permute_leaves(
+__global__ void __launch_bounds__(32 * COPY_WARPS) k_permute_leaves(
     const uint32_t* __restrict__ perm, uint64_t n, const int4* __restrict__ oi, const float* __restrict__ vi,
     const uint32_t* __restrict__ mi, int4* __restrict__ oo, float* __restrict__ vo, uint32_t* __restrict__ mo) {
-  const uint64_t d = blockIdx.x * uint64_t(LEAVES_PER_BLOCK) + (threadIdx.x >> 7);
-  const int t = threadIdx.x & 127;
+  const uint64_t d = blockIdx.x * uint64_t(COPY_WARPS) + (threadIdx.x >> 5);
   if (d >= n) return;
-  const uint64_t s = perm[d];
-  reinterpret_cast<float4*>(vo + d * 512)[t] = reinterpret_cast<const float4*>(vi + s * 512)[t];
-  if (t < 16) mo[d * 16 + t] = mi[s * 16 + t];
-  if (t == 0) oo[d] = oi[s];
+  copy_leaf(perm[d], d, oi, vi, mi, oo, vo, mo);
 }
 
 __global__ void k_count_bits(const uint32_t* __restrict__ m, uint64_t n_words, unsigned long long* out) {
@@ -699,7 +715,7 @@ static uint64_t compact_nonempty(bs_ctx* ctx, bs_volume* v, float remove_above) 
   int4* o2 = dalloc<int4>(ctx, m);
   float* v2 = dalloc<float>(ctx, uint64_t(m) * 512);
   uint32_t* m2 = dalloc<uint32_t>(ctx, uint64_t(m) * 16);
-  BS_KERNEL(ctx, "k_gather_leaves", (k_gather_leaves<<<nb_(n, LEAVES_PER_BLOCK), 128 * LEAVES_PER_BLOCK, 0, s>>>(keep.p, pos.p, n, v->d_origins, v->d_values, v->d_masks, o2, v2, m2)));
+  BS_KERNEL(ctx, "k_gather_leaves", (k_gather_leaves<<<nb_(n, COPY_WARPS), 32 * COPY_WARPS, 0, s>>>(keep.p, pos.p, n, v->d_origins, v->d_values, v->d_masks, o2, v2, m2)));
   dfree(ctx, v->d_origins);
   dfree(ctx, v->d_values);
   dfree(ctx, v->d_masks);
@@ -916,7 +932,7 @@ void volume_offset_impl(bs_ctx* ctx, bs_volume* v, float distance) {
     int4* o2 = dalloc<int4>(ctx, n);
     float* v2 = dalloc<float>(ctx, n * 512);
     uint32_t* m2 = dalloc<uint32_t>(ctx, n * 16);
-    BS_KERNEL(ctx, "k_permute_leaves", (k_permute_leaves<<<nb_(n, LEAVES_PER_BLOCK), 128 * LEAVES_PER_BLOCK, 0, s>>>(perm.p, n, v->d_origins, v->d_values, v->d_masks, o2, v2, m2)));
+    BS_KERNEL(ctx, "k_permute_leaves", (k_permute_leaves<<<nb_(n, COPY_WARPS), 32 * COPY_WARPS, 0, s>>>(perm.p, n, v->d_origins, v->d_values, v->d_masks, o2, v2, m2)));
     dfree(ctx, v->d_origins);
     dfree(ctx, v->d_values);
     dfree(ctx, v->d_masks);

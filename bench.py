@@ -26,8 +26,11 @@ parameters (`fast_tree`) and with the order-3 far field at accuracy scale 1.5
 (`order3_beta1.5`), each with its sign differences from the headline, the
 256-mesh uneven batch (`batched`), the learned far field against the plain
 traversal on 16 M points around the holed subdivision-9 icosphere, training
-time included (`learned`), and the launch shapes the autotuner picked during
-warm-up (`autotuned_launch_shape`).
+time included (`learned`), the launch shapes the autotuner picked during
+warm-up (`autotuned_launch_shape`), and the other single-GPU workloads
+(`other_configs`): the plain remesh of the subdivision-4 icosphere through
+dual contouring to a CornerTable, and the holed subdivision-9 icosphere's
+conversion on both trees.
 
 Other workloads (`--workload`): `open-icosphere` (4.7 M triangles with
 holes, voxel 0.001, signs of a sample checked against exact winding
@@ -422,12 +425,17 @@ def run_ours(args):
     fast3 = variant_secondary(ctx, params, dev, L, N, bs, C, args, order=3, beta=1.5) if args.order3 else None
     batch = batch_secondary(ctx, L, N, bs, C, args.batch_meshes) if args.batch_meshes else None
     learned = None
-    if args.learned_queries:
+    open_mesh = None
+    if args.learned_queries or args.configs:
         from baby_shark_gb300 import synthetic as syn
-        vl, fl = syn.open_icosphere()
+        open_mesh = syn.open_icosphere()
+    if args.learned_queries:
+        vl, fl = open_mesh
         learned = learned_secondary(ctx, vl, fl, args.learned_queries, steps=2, warmup=1, validation=100000)
         learned["workload"] = ("subdivision-9 icosphere with holes (%d triangles), %d points uniform in the box "
                                "padded by 10 %%" % (len(fl), args.learned_queries))
+
+    others = configs_secondary(ctx, L, N, bs, C, open_mesh) if args.configs else None
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -448,7 +456,8 @@ def run_ours(args):
             "autotuned_launch_shape": tuned,
             "fast_tree": fast_tree,
             "learned": learned,
-            "order3_beta1.5": fast3}
+            "order3_beta1.5": fast3,
+            "other_configs": others}
     if rank == 0:
         if world == 1:
             line["cpu_baseline"] = cpu_baseline()
@@ -854,6 +863,83 @@ def batch_secondary(ctx, L, N, bs, C, n_meshes, reps=3):
             "generation_s": t_gen}
 
 
+def configs_secondary(ctx, L, N, bs, C, open_mesh=None, reps=3):
+    """The other single-GPU workloads, timed beside the headline:
+
+    - the plain voxel remesh (icosphere subdivision 4, 5,120 triangles, noise
+      0.05, voxel 0.02, band 3): mesh -> SDF + sign -> dual contouring ->
+      CornerTable through the public API from host arrays, host clock around
+      the whole remesh, best of `reps` after a warm-up;
+    - the non-watertight conversion (subdivision-9 icosphere, 4-octave noise
+      0.1, 10 % of faces removed, 5,242,880 -> about 4.7 M triangles, voxel
+      0.001, band 3): mesh -> SDF + sign with the mesh resident in HBM, CUDA
+      events on the library stream, best of `reps`, on the reference's tree
+      (the bit-exact default) and on the library's fast tree."""
+    import torch
+    from baby_shark_gb300 import synthetic
+    out = {}
+    v1, f1 = synthetic.config1()
+
+    def remesh():
+        vol = bs.MeshToVolume(ctx).with_voxel_size(0.02).with_narrow_band_width(BAND).convert((v1, f1))
+        ct = bs.CornerTable.from_dual_contouring(vol, 0.02)
+        c = ct.counts()
+        return vol.counts()["active_voxels"], c["faces"], c["vertices"]
+
+    remesh()
+    ts = []
+    for _ in range(reps):
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        band, faces, verts = remesh()
+        ts.append(time.perf_counter() - t0)
+    t = min(ts)
+    out["remesh_icosphere_sub4"] = {
+        "workload": "icosphere subdivision 4 (%d triangles), radial noise 0.05, voxel 0.02, band 3: mesh -> SDF + "
+                    "sign -> dual contouring -> CornerTable from host arrays" % len(f1),
+        "ms": t * 1e3, "band_voxels": int(band), "band_voxels_per_s": band / t,
+        "corner_table_faces": int(faces), "corner_table_vertices": int(verts), "faces_per_s": faces / t}
+    if open_mesh is None:
+        open_mesh = synthetic.open_icosphere()
+    vo, fo = open_mesh
+    x = torch.from_numpy(vo).cuda()
+    tt = torch.from_numpy(fo.astype(np.int32)).cuda()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    res = {}
+    for tree in (0, 1):
+        P = N.M2VParams()
+        L.bs_m2v_params_default(C.byref(P))
+        P.voxel_size = 0.001
+        P.band_width = BAND
+        P.wn_tree = tree
+
+        def step():
+            o = C.c_void_p()
+            N.check(L.bs_mesh_to_volume_device(ctx.h, x.data_ptr(), x.shape[0], tt.data_ptr(), tt.shape[0],
+                                               C.byref(P), C.byref(o)), ctx.h)
+            return bs.Volume(o, ctx)
+
+        vol = step()
+        del vol
+        ms = []
+        band = 0
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            vol = step()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            band = vol.counts()["active_voxels"]
+            del vol
+        res["reference_tree" if tree == 0 else "fast_tree"] = {"ms": min(ms), "band_voxels": int(band),
+                                                               "band_voxels_per_s": band / (min(ms) / 1e3)}
+    out["open_icosphere_sub9"] = {
+        "workload": "subdivision-9 icosphere, 4-octave radial noise 0.1, 10 %% of faces removed (%d triangles), "
+                    "voxel 0.001, band 3: mesh -> SDF + sign, mesh resident in HBM" % len(fo), **res}
+    return out
+
+
 def pipeline_secondary(ctx, params, dev, L, N, bs, C):
     """The boolean workload's tail, once per boolean: A op B, then offset +0.01
     and -0.01 (each on its own copy), then dual contouring of each (and, as the
@@ -939,6 +1025,8 @@ def main():
                     help="skip the order-3 / accuracy-scale-1.5 sign-pass comparison")
     ap.add_argument("--batch-meshes", type=int, default=256,
                     help="meshes of the uneven-batch comparison (0 skips it)")
+    ap.add_argument("--configs", type=int, default=1,
+                    help="1: also time the plain remesh and the non-watertight conversion (other_configs)")
     ap.add_argument("--workload", default="tori", choices=["tori", "open-icosphere", "large-union", "learned"],
                     help="tori: the boolean workload's two tori (the headline line); open-icosphere: the "
                          "non-watertight subdivision-9 icosphere with an exact-sign check")
