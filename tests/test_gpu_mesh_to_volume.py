@@ -359,6 +359,46 @@ def test_distance_error_vs_float64_fine_voxel():
     assert err.max() < 2e-4
 
 
+def _f64_error_on_patch(v, f, centre, radius, h, n_pick, seed):
+    """Max and mean |float32 distance - float64 candidate minimum| / h over a
+    seeded sample of the band voxels of the faces within `radius` of `centre`."""
+    from tests.f64_distance import min_distance_f64
+    c = (v[f[:, 0]].astype(np.float64) + v[f[:, 1]] + v[f[:, 2]]) / 3
+    f2 = f[np.linalg.norm(c - centre, axis=1) < radius]
+    vol = bs.MeshToVolume(context()).with_voxel_size(h).with_narrow_band_width(3).convert((v, f2))
+    o, val, m = vol.export()
+    act = np.unpackbits(m.view(np.uint8), bitorder="little").reshape(len(o), 512).astype(bool)
+    li, vi = np.nonzero(act)
+    pick = np.random.default_rng(seed).choice(len(li), min(n_pick, len(li)), replace=False)
+    li, vi = li[pick], vi[pick]
+    vox = o[li].astype(np.int64) + np.stack([vi >> 6, (vi >> 3) & 7, vi & 7], 1)
+    sub, box = ob.subtriangles(v, f2, h, 3)
+    d64 = min_distance_f64(vox, h, sub, box)
+    assert np.all(np.isfinite(d64))
+    err = np.abs(np.abs(val[li, vi]).astype(np.float64) - d64) / h
+    return err.max(), err.mean(), len(f2), float(np.abs(v).max())
+
+
+def test_distance_error_vs_float64_open_icosphere():
+    """The holed subdivision-9 icosphere at its voxel size 0.001: the float32
+    vertices (ulp 1.2e-7 at |coordinates| up to 1.1 = 1.2e-4 voxel) bound the
+    error, which stays within 3e-4 voxel."""
+    v, f = synthetic.open_icosphere()
+    mx, mean, nf, vmax = _f64_error_on_patch(v, f, v[f[0, 0]].astype(np.float64), 0.025, 0.001, 600, 5)
+    print("open icosphere patch: %d faces, max %.3g voxel, mean %.3g voxel" % (nf, mx, mean))
+    assert nf > 300 and mx < 3e-4
+
+
+def test_distance_error_vs_float64_large_union_torus():
+    """The first torus of the 16-torus union at its voxel size 0.0005: the
+    float32 vertices (ulp 1.2e-7 to 2.4e-7 at |coordinates| up to ~2.2 =
+    up to 4.8e-4 voxel) bound the error, which stays within 1e-3 voxel."""
+    (v, f), = synthetic.large_union(n=1)
+    mx, mean, nf, vmax = _f64_error_on_patch(v, f, v[f[0, 0]].astype(np.float64), 0.07, 0.0005, 600, 6)
+    print("large-union torus patch: %d faces, |coord| <= %.2f, max %.3g voxel, mean %.3g voxel" % (nf, vmax, mx, mean))
+    assert nf > 300 and mx < 1e-3
+
+
 def test_launch_shapes_give_identical_volumes_and_autotune_picks_one():
     """Every launch shape and tile the autotuner chooses from gives the same
     volume, bit for bit, on both sign trees; the autotuner returns one of
