@@ -74,22 +74,28 @@ __device__ __forceinline__ float value_at(const McVol& V, const TileLookup& T, i
 
 __device__ __forceinline__ int t9(int x, int y, int z) { return (x * T9 + y) * T9 + z; }
 
-// Triangles of the cube at absolute voxel (x, y, z) with corner values
-// raw[8] (+inf = not active): returns the count; writes them when `out` is set.
-__device__ int cube_tris(const float* raw, int x, int y, int z, float h, float* out) {
-  float v[8];
+// Triangles of the cube at absolute voxel (x, y, z) whose corner i has the
+// value corner(i) (+inf = not active): returns the count; writes them when
+// `out` is set.  No per-cube arrays: corner values are read through the
+// accessor when needed (shared memory for leaf cubes), the segment table
+// `next` (edge -> next edge of its cycle) lives in 12 nibbles of a register,
+// and each cycle is fanned while it is walked (triangles p0 p_i p_i+1 in
+// the walk's order).
+template <class Corner>
+__device__ int cube_tris(Corner corner, int x, int y, int z, float h, float* out) {
+  auto clamp = [](float r) { return fabsf(r) < 1e-6f ? copysignf(1e-6f, r) : r; };
   uint32_t in = 0;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    const float r = raw[i];
+    const float r = corner(i);
     if (r == INFINITY) return 0;  // a corner is not active: no cube (Cube::from_voxel)
-    v[i] = fabsf(r) < 1e-6f ? copysignf(1e-6f, r) : r;
-    if (v[i] < 0.0f) in |= 1u << i;
+    if (clamp(r) < 0.0f) in |= 1u << i;
   }
   if (in == 0u || in == 0xffu) return 0;
-  int8_t next[12];
+  uint64_t nxt = ~0ull;  // nibble e: the edge after e, 0xf = none
+  auto set_next = [&](int e, int to) { nxt = (nxt & ~(0xfull << (4 * e))) | (uint64_t(to) << (4 * e)); };
+  auto get_next = [&](int e) { return int((nxt >> (4 * e)) & 0xfull); };
 #pragma unroll
-  for (int e = 0; e < 12; ++e) next[e] = -1;
   for (int f = 0; f < 6; ++f) {
     int c[4];
 #pragma unroll
@@ -106,63 +112,70 @@ __device__ int cube_tris(const float* raw, int x, int y, int z, float h, float* 
         if (!ia && ib) entry = c_edge_of[a][b];
         if (ia && !ib) exit = c_edge_of[a][b];
       }
-      next[entry] = int8_t(exit);
+      set_next(entry, exit);
     } else if (k == 4) {
       const int p = ((in >> c[0]) & 1u) ? 0 : 1;  // corners p and p + 2 are inside
-      const float prod_in = fmul(v[c[p]], v[c[p + 2]]), prod_out = fmul(v[c[(p + 1) & 3]], v[c[(p + 3) & 3]]);
+      const float prod_in = fmul(clamp(corner(c[p])), clamp(corner(c[p + 2])));
+      const float prod_out = fmul(clamp(corner(c[(p + 1) & 3])), clamp(corner(c[(p + 3) & 3])));
       if (prod_in > prod_out) {
         for (int q = (p + 1) & 3, t = 0; t < 2; ++t, q = (q + 2) & 3)
-          next[c_edge_of[c[q]][c[(q + 1) & 3]]] = c_edge_of[c[(q + 3) & 3]][c[q]];
+          set_next(c_edge_of[c[q]][c[(q + 1) & 3]], c_edge_of[c[(q + 3) & 3]][c[q]]);
       } else {
         for (int r = p, t = 0; t < 2; ++t, r = (r + 2) & 3)
-          next[c_edge_of[c[(r + 3) & 3]][c[r]]] = c_edge_of[c[r]][c[(r + 1) & 3]];
+          set_next(c_edge_of[c[(r + 3) & 3]][c[r]], c_edge_of[c[r]][c[(r + 1) & 3]]);
       }
     }
   }
+  // the crossing on edge e, scaled by the voxel size
+  auto point = [&](int e) {
+    const int a = c_edge[e][0], b = c_edge[e][1];
+    const float va = fmaxf(fabsf(corner(a)), 1e-6f), vb = fmaxf(fabsf(corner(b)), 1e-6f);
+    const float t = fdiv(va, fadd(va, vb));
+    float qx = float(x + c_corner[a][0]), qy = float(y + c_corner[a][1]), qz = float(z + c_corner[a][2]);
+    const int ax = c_edge_axis[e];
+    if (ax == 0) qx = fadd(qx, t);
+    else if (ax == 1) qy = fadd(qy, t);
+    else qz = fadd(qz, t);
+    return f3(fmul(qx, h), fmul(qy, h), fmul(qz, h));
+  };
   int count = 0;
   uint32_t seen = 0;
   for (int e0 = 0; e0 < 12; ++e0) {
-    if (next[e0] < 0 || ((seen >> e0) & 1u)) continue;
-    int poly[12], n = 0;
-    for (int e = e0; !((seen >> e) & 1u) && n < 12; e = next[e]) {
+    if (get_next(e0) == 0xf || ((seen >> e0) & 1u)) continue;
+    seen |= 1u << e0;
+    const F3 a = point(e0);
+    int e = get_next(e0);
+    if ((seen >> e) & 1u) continue;
+    seen |= 1u << e;
+    F3 b = point(e);
+    int n = 2;
+    for (e = get_next(e); e != 0xf && !((seen >> e) & 1u) && n < 12; e = get_next(e)) {
       seen |= 1u << e;
-      poly[n++] = e;
-    }
-    F3 p[12];
-    for (int i = 0; i < n; ++i) {
-      const int e = poly[i], a = c_edge[e][0], b = c_edge[e][1];
-      const float va = fmaxf(fabsf(raw[a]), 1e-6f), vb = fmaxf(fabsf(raw[b]), 1e-6f);
-      const float t = fdiv(va, fadd(va, vb));
-      float q[3] = {float(x + c_corner[a][0]), float(y + c_corner[a][1]), float(z + c_corner[a][2])};
-      const int ax = c_edge_axis[e];
-      q[ax] = fadd(q[ax], t);
-      p[i] = f3(fmul(q[0], h), fmul(q[1], h), fmul(q[2], h));
-    }
-    for (int i = 1; i + 1 < n; ++i) {
-      const F3 a = p[0], b = p[i], c = p[i + 1];
+      ++n;
+      const F3 c = point(e);
       const F3 u = f3(fsub(b.x, a.x), fsub(b.y, a.y), fsub(b.z, a.z));
       const F3 w = f3(fsub(c.x, a.x), fsub(c.y, a.y), fsub(c.z, a.z));
       const float cx = fsub(fmul(u.y, w.z), fmul(u.z, w.y));
       const float cy = fsub(fmul(u.z, w.x), fmul(u.x, w.z));
       const float cz = fsub(fmul(u.x, w.y), fmul(u.y, w.x));
-      if (fadd(fadd(fmul(cx, cx), fmul(cy, cy)), fmul(cz, cz)) == 0.0f) continue;  // Triangle3::is_degenerate
-      if (out) {
-        float* o = out + 9 * count;
-        o[0] = a.x; o[1] = a.y; o[2] = a.z;
-        o[3] = b.x; o[4] = b.y; o[5] = b.z;
-        o[6] = c.x; o[7] = c.y; o[8] = c.z;
+      if (fadd(fadd(fmul(cx, cx), fmul(cy, cy)), fmul(cz, cz)) != 0.0f) {  // Triangle3::is_degenerate
+        if (out) {
+          float* o = out + 9 * count;
+          o[0] = a.x; o[1] = a.y; o[2] = a.z;
+          o[3] = b.x; o[4] = b.y; o[5] = b.z;
+          o[6] = c.x; o[7] = c.y; o[8] = c.z;
+        }
+        ++count;
       }
-      ++count;
+      b = c;
     }
   }
   return count;
 }
 
 __device__ __forceinline__ int leaf_cube(const float* W, int x, int y, int z, int4 org, float h, float* out) {
-  float raw[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) raw[i] = W[t9(x + c_corner[i][0], y + c_corner[i][1], z + c_corner[i][2])];
-  return cube_tris(raw, org.x + x, org.y + y, org.z + z, h, out);
+  return cube_tris([&](int i) { return W[t9(x + c_corner[i][0], y + c_corner[i][1], z + c_corner[i][2])]; },
+                   org.x + x, org.y + y, org.z + z, h, out);
 }
 
 // One warp per leaf.  Pass 1 (tris == nullptr) stores each leaf's triangle
@@ -267,10 +280,11 @@ __global__ void k_mc_tiles(McVol V, TileLookup T, const int4* __restrict__ tiles
   float raw[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) raw[k] = value_at(V, T, x + c_corner[k][0], y + c_corner[k][1], z + c_corner[k][2]);
+  auto corner = [&](int k) { return raw[k]; };
   if (!tris) {
-    count[c] = uint32_t(cube_tris(raw, x, y, z, h, nullptr));
+    count[c] = uint32_t(cube_tris(corner, x, y, z, h, nullptr));
   } else if (off[c + 1] > off[c]) {
-    cube_tris(raw, x, y, z, h, tris + 9 * off[c]);
+    cube_tris(corner, x, y, z, h, tris + 9 * off[c]);
   }
 }
 

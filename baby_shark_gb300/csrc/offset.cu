@@ -578,27 +578,37 @@ __global__ void k_link(Sweep S, int n) {
 // only a slot that is not live gets its (empty) output here: its input is
 // empty too (a dropped leaf's output was cleared, spare slots start empty).
 __global__ void __launch_bounds__(128) k_sweep_init(Sweep S, int n, int* list, int* n_list) {
-  const int lane = threadIdx.x & 31;
+  __shared__ __align__(16) float tile[4][512];
+  __shared__ uint32_t tmask[4][16];
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
   const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (l >= n) return;
-  const float* iv = S.in_val + uint64_t(l) * 512;
-  const uint32_t* im = S.in_msk + uint64_t(l) * 16;
-  if (!S.alive[l]) {
+  const bool live = S.alive[l] != 0;
+  if (!live) {
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int k = lane; k < 128; k += 32) reinterpret_cast<float4*>(S.out_val + uint64_t(l) * 512)[k] = z;
     if (lane < 16) S.out_msk[uint64_t(l) * 16 + lane] = 0u;
+  } else {  // the input, staged with coalesced loads (faces are strided)
+    const float4* iv4 = reinterpret_cast<const float4*>(S.in_val + uint64_t(l) * 512);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) reinterpret_cast<float4*>(tile[wi])[lane + 32 * j] = iv4[lane + 32 * j];
+    if (lane < 16) tmask[wi][lane] = S.in_msk[uint64_t(l) * 16 + lane];
+    __syncwarp();
   }
+  const float* iv = tile[wi];
+  const uint32_t* im = tmask[wi];
   const int sdir[3] = {S.sx, S.sy, S.sz};
   for (int ax = 0; ax < 3; ++ax) {
     for (int side = 0; side < 2; ++side) {
-      // side 0: the after-face (published output), side 1: the before-layer
+      // side 0: the after-face (published output), side 1: the before-layer;
+      // a slot that is not live has an empty input, so empty faces
       const int fl = (sdir[ax] > 0) == (side == 0) ? 7 : 0;
       float* fv = side == 0 ? S.pub_val : S.inf_val;
       uint32_t* fm = side == 0 ? S.pub_msk : S.inf_msk;
       for (int r = 0; r < 2; ++r) {
         const int i = lane + 32 * r;
         const int o = face_off(ax, fl, i);
-        const bool on = bit(im, o);
+        const bool on = live && bit(im, o);
         fv[(uint64_t(l) * 3 + ax) * 64 + i] = on ? iv[o] : 0.f;
         const uint32_t mw = __ballot_sync(0xffffffffu, on);
         if (lane == 0) fm[(uint64_t(l) * 3 + ax) * 2 + r] = mw;
@@ -608,7 +618,7 @@ __global__ void __launch_bounds__(128) k_sweep_init(Sweep S, int n, int* list, i
   if (lane == 0) {
     S.spawned[l] = 0;
     S.dirty[l] = 0;
-    if (S.alive[l]) {
+    if (live) {
       S.dirty[l] = 1;
       list[atomicAdd(n_list, 1)] = l;
     }

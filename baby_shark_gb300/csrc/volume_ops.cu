@@ -173,23 +173,26 @@ namespace bs {
 __device__ __forceinline__ bool mask_on(const uint32_t* m, int i) { return (m[i >> 5] >> (i & 31)) & 1u; }
 __device__ __forceinline__ float signed_far(bool neg) { return neg ? -FAR_F : FAR_F; }
 
-// leaf_node/flood_fill.rs:12-50.  One warp per leaf: the leaf is staged in
-// shared memory with coalesced float4 loads, lane l scans the z-lines
-// (x, y) = (l >> 3, l & 7) and (4 + (l >> 3), l & 7), and the leaf is written
-// back whole.  Full and empty leaves are left as they are.
+// leaf_node/flood_fill.rs:12-50.  One warp per leaf.  Scanning a z-line
+// (x, y), the reference carries the sign of the last active voxel it has met:
+// starting from the leaf's first active voxel, then the active voxels
+// (xx, 0, 0) for xx <= x, then (x, yy, 0) for yy <= y, then along the line,
+// and an inactive voxel takes the carried sign (+-far).  Here the leaf's
+// values stay in registers (four float4 per lane, coalesced), the active and
+// sign bits of its 512 voxels go to shared memory as two 16-word masks, and
+// lane l carries the sign along lines l and l + 32 with bit operations on
+// those masks only; the fill bits of each line go back through shared memory
+// and the leaf is written whole.  Full and empty leaves are left as they are.
 constexpr int FF_WARPS = 8;
 __global__ void __launch_bounds__(32 * FF_WARPS) k_ff_leaf(float* __restrict__ values, const uint32_t* __restrict__ masks,
                                                            uint64_t n, uint8_t* __restrict__ first_neg,
                                                            uint8_t* __restrict__ last_neg) {
-  __shared__ float4 sv4[FF_WARPS][128];
-  __shared__ uint32_t smk[FF_WARPS][16];
+  __shared__ uint32_t sact[FF_WARPS][16], sneg[FF_WARPS][16];
+  __shared__ uint8_t sfill[FF_WARPS][64];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint64_t b = blockIdx.x * uint64_t(FF_WARPS) + w;
   if (b >= n) return;
-  float* V = reinterpret_cast<float*>(sv4[w]);
-  uint32_t* M = smk[w];
   const uint32_t mw = lane < 16 ? masks[b * 16 + lane] : 0u;
-  if (lane < 16) M[lane] = mw;
   const bool full = __all_sync(0xffffffffu, lane >= 16 || mw == 0xffffffffu);
   const uint32_t nonzero = __ballot_sync(0xffffffffu, mw != 0u);
   float4* g4 = reinterpret_cast<float4*>(values + b * 512);
@@ -200,33 +203,63 @@ __global__ void __launch_bounds__(32 * FF_WARPS) k_ff_leaf(float* __restrict__ v
     }
     return;
   }
+  // float4 k = lane + 32 j holds voxels 4k .. 4k + 3: word k >> 3, bits 4 (k & 7) + i
+  float4 r[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) r[j] = g4[lane + 32 * j];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    uint32_t nib = (signbit(r[j].x) ? 1u : 0u) | (signbit(r[j].y) ? 2u : 0u) | (signbit(r[j].z) ? 4u : 0u) |
+                   (signbit(r[j].w) ? 8u : 0u);
+    nib <<= 4 * (lane & 7);
+    nib |= __shfl_xor_sync(0xffffffffu, nib, 1);
+    nib |= __shfl_xor_sync(0xffffffffu, nib, 2);
+    nib |= __shfl_xor_sync(0xffffffffu, nib, 4);
+    if ((lane & 7) == 0) sneg[w][(lane >> 3) + 4 * j] = nib;
+  }
+  if (lane < 16) sact[w][lane] = mw;
+  __syncwarp();
+  const uint32_t* A = sact[w];
+  const uint32_t* Ng = sneg[w];
   const int fw = __ffs(nonzero) - 1;
   const int first = fw * 32 + __ffs(__shfl_sync(0xffffffffu, mw, fw)) - 1;
+  const uint32_t s0 = (Ng[first >> 5] >> (first & 31)) & 1u;
 #pragma unroll
-  for (int j = 0; j < 4; ++j) sv4[w][lane + 32 * j] = g4[lane + 32 * j];
-  __syncwarp();
-  const bool s0 = signbit(V[first]);
-  for (int line = lane; line < 64; line += 32) {
-    const int x = line >> 3, y = line & 7;
-    bool c = s0;
-    for (int xx = 0; xx <= x; ++xx)
-      if (mask_on(M, xx << 6)) c = signbit(V[xx << 6]);
-    for (int yy = 0; yy <= y; ++yy)
-      if (mask_on(M, (x << 6) | (yy << 3))) c = signbit(V[(x << 6) | (yy << 3)]);
-    for (int z = 0; z < 8; ++z) {
-      const int o = (x << 6) | (y << 3) | z;
-      if (mask_on(M, o))
-        c = signbit(V[o]);
-      else
-        V[o] = signed_far(c);
+  for (int h = 0; h < 2; ++h) {
+    const int line = lane + 32 * h, x = line >> 3, y = line & 7;
+    uint32_t c = s0;
+    for (int xx = 0; xx <= x; ++xx)  // voxel (xx, 0, 0): word 2 xx, bit 0
+      if (A[2 * xx] & 1u) c = Ng[2 * xx] & 1u;
+    for (int yy = 0; yy <= y; ++yy) {  // voxel (x, yy, 0): word 2 x + yy / 4, bit 8 (yy % 4)
+      const int wd = 2 * x + (yy >> 2), bt = 8 * (yy & 3);
+      if ((A[wd] >> bt) & 1u) c = (Ng[wd] >> bt) & 1u;
     }
+    const int sh = 8 * (line & 3);
+    const uint32_t a8 = (A[line >> 2] >> sh) & 0xffu, n8 = (Ng[line >> 2] >> sh) & 0xffu;
+    uint32_t fill = 0;
+#pragma unroll
+    for (int z = 0; z < 8; ++z) {
+      if ((a8 >> z) & 1u)
+        c = (n8 >> z) & 1u;
+      else
+        fill |= c << z;
+    }
+    sfill[w][line] = uint8_t(fill);
   }
   __syncwarp();
 #pragma unroll
-  for (int j = 0; j < 4; ++j) g4[lane + 32 * j] = sv4[w][lane + 32 * j];
-  if (lane == 0) {
-    first_neg[b] = signbit(V[0]) ? 1 : 0;
-    last_neg[b] = signbit(V[511]) ? 1 : 0;
+  for (int j = 0; j < 4; ++j) {
+    const int k = lane + 32 * j;
+    const uint32_t act4 = (A[k >> 3] >> (4 * (k & 7))) & 0xfu;
+    const uint32_t fill4 = (uint32_t(sfill[w][k >> 1]) >> (4 * (k & 1))) & 0xfu;  // voxels 4k.. of line k / 2
+    float4 t = r[j];
+    if (!(act4 & 1u)) t.x = signed_far(fill4 & 1u);
+    if (!(act4 & 2u)) t.y = signed_far(fill4 & 2u);
+    if (!(act4 & 4u)) t.z = signed_far(fill4 & 4u);
+    if (!(act4 & 8u)) t.w = signed_far(fill4 & 8u);
+    g4[k] = t;
+    if (k == 0) first_neg[b] = signbit(t.x) ? 1 : 0;
+    if (k == 127) last_neg[b] = signbit(t.w) ? 1 : 0;
   }
 }
 
