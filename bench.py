@@ -72,6 +72,12 @@ WN_FLOP_PER_VOXEL = int(round(WN_FAR_PER_VOXEL * WN_FLOP_FAR + WN_EXACT_PER_VOXE
 # torus by the units processed (35,669,277 voxels; 6,848,421,294 pairs);
 # k_rt_sign captured on one full torus (582.8 MB read + 272.0 MB written)
 TRAFFIC_PER_LAUNCH = {"k_wn_sign": 642e6, "k_brick_distance": 1436e6, "k_rt_sign": 854.8e6}
+# smsp__inst_executed.sum per launch of the same capture of k_rt_sign (one
+# full torus, 35,669,277 band voxels): warp instructions, the kernel's real
+# bound (it issues on 86 % of the cycles); scaled by the voxels of a launch
+RT_SIGN_WARP_INST_PER_VOXEL = 67.74e9 / 35669277
+SM_COUNT_GB300 = 152
+SCHEDULERS_PER_SM = 4
 METRIC = "band voxels/s mesh→SDF+sign: learned/batched vs plain GPU, 0 sign flips"
 UNIT = "band_voxels/s"
 WORKLOAD = ("two displaced tori, 1,048,576 triangles each, voxel 0.002, band 3: mesh->SDF+sign (plain GPU path; "
@@ -393,6 +399,16 @@ def run_ours(args):
                 "%.0f exact triangles x %d FLOP, counted by the oracle) x %d voxels per launch"
                 % (WN_FLOP_PER_VOXEL, WN_FAR_PER_VOXEL, WN_FLOP_FAR, WN_EXACT_PER_VOXEL, WN_FLOP_EXACT,
                    stats["active_voxels"]))
+        # the bound that holds it: warp-instruction issue (one per scheduler
+        # per cycle) at the SM clock sampled during the timed region
+        if clk.get("sm_mhz"):
+            inst = RT_SIGN_WARP_INST_PER_VOXEL * stats["active_voxels"]
+            issue_peak = SM_COUNT_GB300 * SCHEDULERS_PER_SM * clk["sm_mhz"] * 1e6
+            extra["issue_bound"] = {
+                "warp_instructions_per_launch": inst, "achieved_per_s": inst / per_launch_s,
+                "peak_per_s": issue_peak, "frac": inst / per_launch_s / issue_peak,
+                "source": "smsp__inst_executed.sum of one ncu capture (profiles/k_rt_sign_one_torus.md), per band "
+                          "voxel; peak = 152 SMs x 4 schedulers x the sampled SM clock"}
     elif name == "k_wn_sign":
         flops = WN_FLOP_PER_VOXEL * stats["active_voxels"]
         # what the warp-coherent traversal executes: every lane of a warp evaluates
