@@ -481,7 +481,7 @@ struct __align__(16) BatchTri {
   float4 dxb;  //   ... x = 4..7
   float4 yz;   // bounding box lo.y lo.z hi.y hi.z
   int4 box;    // x0 y0 z0 nx: first voxel of (widened box) x (brick) and its x extent
-  int4 box1;   // nz, mask of the brick x covered by the widened box, bits of E0, -
+  int4 box1;   // nz, mask of the brick x covered by the widened box, bits of E0, bits of max dx
 };
 
 constexpr float CULL_SCALE = 1.0f - 0x1p-20f;
@@ -544,11 +544,12 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_brick_distance(
         BatchTri& q = W[lane];
         const F3 ab = sub3(bb, a), ac = sub3(c, a), cb = sub3(c, bb);
         const float lox = fminf(fminf(a.x, bb.x), c.x), hix = fmaxf(fmaxf(a.x, bb.x), c.x);
-        float dx[8];
+        float dx[8], dxmax = 0.0f;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {  // squared box distance in x of the brick's voxel columns x = org.x + i
           const float d = box_d(lox, hix, gtab[0][i]);
           dx[i] = fmul(fmul(d, d), CULL_SCALE);
+          dxmax = fmaxf(dxmax, dx[i]);
         }
         q.v0 = make_float4(a.x, a.y, a.z, ab.x);
         q.v1 = make_float4(ab.y, ab.z, ac.x, ac.y);
@@ -561,7 +562,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_brick_distance(
         q.yz = make_float4(fminf(fminf(a.y, bb.y), c.y), fminf(fminf(a.z, bb.z), c.z),
                            fmaxf(fmaxf(a.y, bb.y), c.y), fmaxf(fmaxf(a.z, bb.z), c.z));
         q.box = make_int4(x0, y0, z0, nx);
-        q.box1 = make_int4(nz, int(((1u << nx) - 1u) << (x0 - org.x)), __float_as_int(e0), 0);
+        q.box1 = make_int4(nz, int(((1u << nx) - 1u) << (x0 - org.x)), __float_as_int(e0), __float_as_int(dxmax));
         cols = ny * nz;
       }
     }
@@ -602,11 +603,16 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_brick_distance(
         const float4 cc = *reinterpret_cast<const float4*>(&dmin[colb + 4]);
         const float dxs[8] = {dxa.x, dxa.y, dxa.z, dxa.w, dxb.x, dxb.y, dxb.z, dxb.w};
         const float cur[8] = {ca.x, ca.y, ca.z, ca.w, cc.x, cc.y, cc.z, cc.w};
+        // the margin 33 t^2 with t = c2 lb + E0 grows with lb (c2, E0 >= 0 and
+        // each float step is monotone), so the column's largest lb gives a
+        // margin no smaller than any of its voxels' own: the test below culls
+        // a subset of what the per-voxel margin would, and stays exact
+        const float tcol = fmaf(c2, fadd(__int_as_float(b1.w), dyz), e0);
+        const float margin = 33.0f * (tcol * tcol);
 #pragma unroll
         for (int ix = 0; ix < 8; ++ix) {
           const float lb = fadd(dxs[ix], dyz);
-          const float tt = fmaf(c2, lb, e0);
-          bits |= (lb > fmaf(cur[ix], 1.03125f, 33.0f * (tt * tt))) ? 0u : (1u << ix);
+          bits |= (lb > fmaf(cur[ix], 1.03125f, margin)) ? 0u : (1u << ix);
         }
         bits &= uint32_t(b1.y);  // the voxels of (widened box) x (brick) in this column
       }
