@@ -44,7 +44,7 @@ struct bs_ctx {
   // the distance pass (64, 128, 256) and warps per block of the sign pass
   // (2, 4, 8)
   int tune_dist_threads = 128;
-  int tune_dist_batch = 16;  // sub-triangles per warp tile of the distance pass (8, 16, 32)
+  int tune_dist_batch = 32;  // sub-triangles per warp tile of the distance pass (8, 16, 32)
   int tune_wn_warps = 4;
   // counters of the last mesh -> volume, offset or dual contouring call
   // (see bs_ctx_last_counters); [8] names the call that wrote them

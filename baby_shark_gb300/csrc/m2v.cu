@@ -2458,7 +2458,8 @@ bs_status bs_ctx_set_launch_shape(bs_ctx* ctx, int32_t dist_threads, int32_t wn_
   if (wn_warps && wn_warps != 2 && wn_warps != 4 && wn_warps != 8) return BS_ERR_INVALID_ARG;
   if (dist_tile && dist_tile != 8 && dist_tile != 16 && dist_tile != 32) return BS_ERR_INVALID_ARG;
   const int th = dist_threads ? dist_threads : ctx->tune_dist_threads;
-  const int ti = dist_tile ? dist_tile : ctx->tune_dist_batch;
+  // a tile left unset follows the threads: 256 threads take at most 16
+  const int ti = dist_tile ? dist_tile : (th == 256 && ctx->tune_dist_batch == 32 ? 16 : ctx->tune_dist_batch);
   if (th == 256 && ti == 32) return BS_ERR_INVALID_ARG;
   ctx->tune_dist_threads = th;
   ctx->tune_dist_batch = ti;

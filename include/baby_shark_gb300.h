@@ -186,7 +186,9 @@ bs_status bs_mesh_to_volume_batch_device(bs_ctx* ctx, uint64_t n_meshes, const f
  * unit of every later boolean, offset and mesher. */
 bs_status bs_autotune_mesh_to_volume(bs_ctx* ctx, const float* d_xyz, uint64_t nv, const uint32_t* d_tri, uint64_t nt,
                                      const bs_m2v_params* p, int32_t* h_choice, float* h_ms);
-/* Sets the launch shapes directly (0 keeps the current value). */
+/* Sets the launch shapes directly (0 keeps the current value; a context
+ * starts at 128 threads per brick, tiles of 32 sub-triangles and 4 sign
+ * warps, and a tile left at 0 with 256 threads becomes 16). */
 bs_status bs_ctx_set_launch_shape(bs_ctx* ctx, int32_t dist_threads, int32_t wn_warps, int32_t dist_tile);
 /* ------------------------------------------------------------- volumes --- */
 /* Volume::with_voxel_size (volume/mod.rs:17-24): an empty volume (no leaves,
