@@ -461,7 +461,8 @@ def run_ours(args):
                        "triangles_per_step": int(len(fa) + len(fb)),
                        "band_voxels_per_step": int(band), "l2": "flushed between steps (256 MiB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "ms_per_step": e2e_ms, "steps_ms": [round(t * 1e3, 2) for t in t_e2e]},
             "gpu_launches": int(launches),
             "roofline": roof,
             "clocks": clk,
