@@ -359,7 +359,7 @@ def run_ours(args):
     value = band_all / (ms / 1000.0)
 
     # ---- e2e: host buffers through the C ABI, upload + export inside each step ----
-    for _ in range(max(1, args.warmup // 2)):
+    for _ in range(max(1, args.warmup)):
         step_e2e()
     t_e2e = []
     for _ in range(args.steps):
