@@ -183,7 +183,7 @@ struct Sweep {
   int* changed;
   int sx, sy, sz, neg;
   float lim, h;
-  // work queue of the persistent relaxation (null: queue into lists)
+  // work queue of the persistent relaxation (null: queue into a list)
   unsigned long long* ring;  // entry: position << 32 | slot; RING_EMPTY when free
   uint32_t ring_mask;
   unsigned* qhead;           // next position to take
@@ -745,7 +745,7 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   DBuf<float> val_a(ctx, cap * 512), val_b(ctx, cap * 512), pub_val(ctx, cap * 192), inf_val(ctx, cap * 192);
   DBuf<uint32_t> msk_a(ctx, cap * 16), msk_b(ctx, cap * 16), frz(ctx, cap * 16), pub_msk(ctx, cap * 6),
       inf_msk(ctx, cap * 6);
-  DBuf<int> flags(ctx, cap * 6), list_a(ctx, cap), list_b(ctx, cap), ctl(ctx, 16), nbr(ctx, cap * 6);
+  DBuf<int> flags(ctx, cap * 6), list(ctx, cap), ctl(ctx, 16), nbr(ctx, cap * 6);
   // every spare slot is an empty leaf: zero inputs, outputs, faces and flags
   BS_CUDA(cudaMemsetAsync(val_a.p, 0, cap * 512 * sizeof(float), s));
   BS_CUDA(cudaMemsetAsync(val_b.p, 0, cap * 512 * sizeof(float), s));
@@ -772,7 +772,8 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   }
   LeafHashBuf hb;
   hb.build(ctx, org.p, n0, cap);
-  // ctl: [0..2] rotating list counters, [3] used slots, [4] overflow, [5] changed
+  // ctl: [0] length of `list` (leaves to queue), [3] used slots, [4] overflow, [5] changed,
+  //      [8] ring head, [9] ring tail, [10] pending, [11] a wait gave up
   int* cnt = ctl.p;
   Sweep S;
   S.org = org.p;
@@ -817,7 +818,6 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
   SR.qerr = ctl.p + 11;
   SR.n_sweeps = sweeps.p;
   BS_KERNEL(ctx, "k_link", (k_link<<<nb_(n0 * 6, 256), 256, 0, s>>>(S, int(n0))));
-  int* lists[2] = {list_a.p, list_b.p};
   float* vals[2] = {val_a.p, val_b.p};
   uint32_t* msks[2] = {msk_a.p, msk_b.p};
   int cur = 0;
@@ -833,9 +833,9 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
     S.out_val = vals[cur ^ 1];
     S.out_msk = msks[cur ^ 1];
     int n = 0;
-    BS_CUDA(cudaMemsetAsync(cnt, 0, 3 * sizeof(int), s));
+    BS_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int), s));
     read_back(ctx, &n, S.n_slots, sizeof(int));
-    BS_KERNEL(ctx, "k_sweep_init", (k_sweep_init<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, lists[0], cnt)));
+    BS_KERNEL(ctx, "k_sweep_init", (k_sweep_init<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, list.p, cnt)));
     int pass = 0;
     {
       const Sweep SD = [&] {
@@ -850,9 +850,9 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
         return t;
       }();
       for (;;) {
-        // the queued leaves (lists[0], cnt[0]) into the ring, then one
+        // the queued leaves (list, cnt[0]) into the ring, then one
         // persistent relaxation until nothing is queued
-        BS_KERNEL(ctx, "k_ring_start", (k_ring_start<<<nb_(cap, 256), 256, 0, s>>>(SD, lists[0], cnt)));
+        BS_KERNEL(ctx, "k_ring_start", (k_ring_start<<<nb_(cap, 256), 256, 0, s>>>(SD, list.p, cnt)));
         BS_KERNEL(ctx, "k_relax_ring", (k_relax_ring<<<ring_grid, 32 * SW_WARPS, 0, s>>>(SD)));
         ++pass;
         int qe = 0;
@@ -863,8 +863,8 @@ static bool run_sweeps(bs_ctx* ctx, bs_volume* v, uint64_t cap, float h, float l
         BS_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int), s));
         BS_CUDA(cudaMemsetAsync(S.changed, 0, sizeof(int), s));
         BS_KERNEL(ctx, "k_spawn_clear", (k_spawn_clear<<<nb_(uint64_t(n), 256), 256, 0, s>>>(S, n)));
-        BS_KERNEL(ctx, "k_spawn_mark", (k_spawn_mark<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, lists[0], cnt)));
-        BS_KERNEL(ctx, "k_spawn_drop", (k_spawn_drop<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, lists[0], cnt)));
+        BS_KERNEL(ctx, "k_spawn_mark", (k_spawn_mark<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, list.p, cnt)));
+        BS_KERNEL(ctx, "k_spawn_drop", (k_spawn_drop<<<nb_(uint64_t(n) * 32, 128), 128, 0, s>>>(S, n, list.p, cnt)));
         int ch = 0;
         read_back(ctx, &ch, S.changed, sizeof(int));
         if (!ch) break;
