@@ -42,6 +42,7 @@ learned far field against the traversal on points in the padded box).
 oracle port; the Rust crate cannot be built here) on the same metric.
 """
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -336,6 +337,10 @@ def run_ours(args):
     torch.cuda.synchronize()
     ctx.synchronize()
     per_step, band = [], 0
+    # the interpreter's collector stays off while steps are timed (a
+    # collection pause would be host time between the library's launches)
+    gc.collect()
+    gc.disable()
     with torch.cuda.stream(stream):
         for _ in range(args.steps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -348,6 +353,7 @@ def run_ours(args):
             per_step.append(e0.elapsed_time(e1))
     ctx.synchronize()
     torch.cuda.synchronize()
+    gc.enable()
     barrier()
     clk = clocks.stop()
     launches = ctx.kernel_launches - launches0
@@ -362,12 +368,15 @@ def run_ours(args):
     for _ in range(max(1, args.warmup)):
         step_e2e()
     t_e2e = []
+    gc.collect()
+    gc.disable()
     for _ in range(args.steps):
         ctx.synchronize()
         t0 = time.perf_counter()
         b_e2e, h2d, d2h = step_e2e()
         ctx.synchronize()
         t_e2e.append(time.perf_counter() - t0)
+    gc.enable()
     e2e_ms, e2e_band = combine_ranks(1000.0 * sum(t_e2e) / len(t_e2e), b_e2e, world, "cuda")
     e2e_value = e2e_band / (e2e_ms / 1000.0)
 
