@@ -370,6 +370,8 @@ def run_ours(args):
     t_e2e = []
     gc.collect()
     gc.disable()
+    clocks_e2e = ClockSampler(local)
+    clocks_e2e.start()
     for _ in range(args.steps):
         ctx.synchronize()
         t0 = time.perf_counter()
@@ -377,6 +379,7 @@ def run_ours(args):
         ctx.synchronize()
         t_e2e.append(time.perf_counter() - t0)
     gc.enable()
+    clk_e2e = clocks_e2e.stop()
     e2e_ms, e2e_band = combine_ranks(1000.0 * sum(t_e2e) / len(t_e2e), b_e2e, world, "cuda")
     e2e_value = e2e_band / (e2e_ms / 1000.0)
 
@@ -471,7 +474,7 @@ def run_ours(args):
                        "band_voxels_per_step": int(band), "l2": "flushed between steps (256 MiB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "ms_per_step": e2e_ms, "steps_ms": [round(t * 1e3, 2) for t in t_e2e]},
+                    "ms_per_step": e2e_ms, "steps_ms": [round(t * 1e3, 2) for t in t_e2e], "clocks": clk_e2e},
             "gpu_launches": int(launches),
             "roofline": roof,
             "clocks": clk,
