@@ -296,17 +296,23 @@ def run_ours(args):
         N.check(L.bs_volume_export(ctx.h, vol.h, o.data_ptr(), val.data_ptr(), m.data_ptr()), ctx.h)
         return n * (12 + 2048 + 64)
 
+    export_s = []  # host time of the exports of each step (the rest is upload + conversion)
+
     def step_e2e():
         band, h2d, d2h = 0, 0, 0
+        te = 0.0
         for k, (x, t) in enumerate(host_in):
             out = C.c_void_p()
             N.check(L.bs_mesh_to_volume(ctx.h, x.data_ptr(), x.shape[0], t.data_ptr(), t.shape[0], C.byref(params),
                                         C.byref(out)), ctx.h)
             vol = bs.Volume(out, ctx)
+            t0 = time.perf_counter()
             d2h += export_pinned(vol, k)
+            te += time.perf_counter() - t0
             band += vol.counts()["active_voxels"]
             h2d += x.numel() * 4 + t.numel() * 4
             del vol
+        export_s.append(te)
         return band, h2d, d2h
 
     def barrier():
@@ -368,6 +374,7 @@ def run_ours(args):
     for _ in range(max(1, args.warmup)):
         step_e2e()
     t_e2e = []
+    del export_s[:]
     gc.collect()
     gc.disable()
     clocks_e2e = ClockSampler(local)
@@ -474,7 +481,8 @@ def run_ours(args):
                        "band_voxels_per_step": int(band), "l2": "flushed between steps (256 MiB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "ms_per_step": e2e_ms, "steps_ms": [round(t * 1e3, 2) for t in t_e2e], "clocks": clk_e2e},
+                    "ms_per_step": e2e_ms, "steps_ms": [round(t * 1e3, 2) for t in t_e2e],
+                    "export_ms": [round(t * 1e3, 2) for t in export_s], "clocks": clk_e2e},
             "gpu_launches": int(launches),
             "roofline": roof,
             "clocks": clk,
