@@ -112,7 +112,7 @@ __device__ int cube_tris(Corner corner, int x, int y, int z, float h, float* out
         if (!ia && ib) entry = c_edge_of[a][b];
         if (ia && !ib) exit = c_edge_of[a][b];
       }
-      set_next(entry, exit);
+      if (entry >= 0 && exit >= 0) set_next(entry, exit);  // always both on a face with two crossings
     } else if (k == 4) {
       const int p = ((in >> c[0]) & 1u) ? 0 : 1;  // corners p and p + 2 are inside
       const float prod_in = fmul(clamp(corner(c[p])), clamp(corner(c[p + 2])));
