@@ -71,6 +71,18 @@ def test_rotated_shifted_torus_negative_coords():
     assert_parity(vol, ov)
 
 
+def test_far_from_origin_matches_oracle():
+    """A mesh two thousand units from the origin at voxel 0.05: the float32
+    coordinates keep only about 1e-4 of absolute precision there (ulp 1.2e-4
+    at 2000), so the grid points, sub-triangles, distances and the tree's
+    far-field terms all round coarsely; the volume is still the oracle's bit
+    for bit."""
+    v, f = synthetic.icosphere(3, 0.5, 0.02, seed=21)
+    v = (v.astype(np.float64) + np.array([1000.25, -2000.5, 333.0])).astype(np.float32)
+    vol, ov, _ = run_both(v, f, 0.05, 2)
+    assert_parity(vol, ov)
+
+
 ATAN2_RESIDUE = 1e-6  # |wn - 0.2| below which last-place atan2f differences may flip a sign
 
 
