@@ -390,15 +390,31 @@ __device__ void relax_leaf(const Sweep& S, int leaf, RelaxSmem& sm, int* __restr
       if (nb >= 0) S.nbr[uint64_t(nb) * 6 + (lane ^ 1)] = leaf;
     }
   }
-  const float* iv = S.in_val + uint64_t(leaf) * 512;
+  // the leaf's input: each lane's four float4 (voxels 4 k4 .. 4 k4 + 3 of
+  // z-line k4 / 2, k4 = lane + 32 j) and the mask words, all loads issued
+  // before any store, so the leaf costs one memory latency, not sixteen
+  const float4* iv4 = reinterpret_cast<const float4*>(S.in_val + uint64_t(leaf) * 512);
   const uint32_t* im = S.in_msk + uint64_t(leaf) * 16;
-  for (int k = lane; k < 512; k += 32) {
-    const uint32_t m = im[k >> 5];
-    const float v = iv[k];
-    W[pad_idx(k >> 6, (k >> 3) & 7, k & 7)] = ((m >> lane) & 1u) ? v : INFINITY;
+  {
+    float4 in4[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) in4[j] = iv4[lane + 32 * j];
+    const uint32_t mw_in = lane < 16 ? im[lane] : 0u;
+    const uint32_t fz = lane < 16 ? S.frz[uint64_t(leaf) * 16 + lane] : 0u;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int k4 = lane + 32 * j, k = 4 * k4;
+      const uint32_t m = __shfl_sync(0xffffffffu, mw_in, k4 >> 3) >> (4 * (k4 & 7));
+      const int base = pad_idx(k >> 6, (k >> 3) & 7, k & 7);  // z, z + 1, z + 2, z + 3 follow
+      W[base] = (m & 1u) ? in4[j].x : INFINITY;
+      W[base + 1] = (m & 2u) ? in4[j].y : INFINITY;
+      W[base + 2] = (m & 4u) ? in4[j].z : INFINITY;
+      W[base + 3] = (m & 8u) ? in4[j].w : INFINITY;
+    }
+    if (lane < 16) F[lane] = fz;
   }
-  if (lane < 16) F[lane] = S.frz[uint64_t(leaf) * 16 + lane];
   // this leaf's faces as published before: only this warp writes them in this pass
+#pragma unroll
   for (int k = lane; k < 3 * 64; k += 32) oldf[w][k] = __ldcg(&S.pub_val[uint64_t(leaf) * 192 + k]);
   if (lane < 6) oldm[w][lane] = __ldcg(&S.pub_msk[uint64_t(leaf) * 6 + lane]);
   // halo: all twelve loads of this lane first, then the tile writes
@@ -441,13 +457,27 @@ __device__ void relax_leaf(const Sweep& S, int leaf, RelaxSmem& sm, int* __restr
     }
     __syncwarp();
   }
-  float* ov = S.out_val + uint64_t(leaf) * 512;
-  for (int k = lane; k < 512; k += 32) {
-    const float t = W[pad_idx(k >> 6, (k >> 3) & 7, k & 7)];
-    const bool on = t != INFINITY;
-    ov[k] = on ? t : iv[k];
-    const uint32_t mw = __ballot_sync(0xffffffffu, on);
-    if (lane == 0) S.out_msk[uint64_t(leaf) * 16 + (k >> 5)] = mw;
+  // outputs: the swept values where active, the input elsewhere (read again,
+  // batched, from L2), and the active masks assembled from each lane's four
+  {
+    float4 in4[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) in4[j] = iv4[lane + 32 * j];
+    float4* ov4 = reinterpret_cast<float4*>(S.out_val + uint64_t(leaf) * 512);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int k4 = lane + 32 * j, k = 4 * k4;
+      const int base = pad_idx(k >> 6, (k >> 3) & 7, k & 7);
+      const float t0 = W[base], t1 = W[base + 1], t2 = W[base + 2], t3 = W[base + 3];
+      const bool a0 = t0 != INFINITY, a1 = t1 != INFINITY, a2 = t2 != INFINITY, a3 = t3 != INFINITY;
+      ov4[k4] = make_float4(a0 ? t0 : in4[j].x, a1 ? t1 : in4[j].y, a2 ? t2 : in4[j].z, a3 ? t3 : in4[j].w);
+      uint32_t nib = (a0 ? 1u : 0u) | (a1 ? 2u : 0u) | (a2 ? 4u : 0u) | (a3 ? 8u : 0u);
+      nib <<= 4 * (lane & 7);
+      nib |= __shfl_xor_sync(0xffffffffu, nib, 1);
+      nib |= __shfl_xor_sync(0xffffffffu, nib, 2);
+      nib |= __shfl_xor_sync(0xffffffffu, nib, 4);
+      if ((lane & 7) == 0) S.out_msk[uint64_t(leaf) * 16 + (k4 >> 3)] = nib;
+    }
   }
   uint32_t flags = 0;  // bit ax: face changed, bit 3 + ax: face asks for the next leaf
 #pragma unroll
