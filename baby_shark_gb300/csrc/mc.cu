@@ -190,17 +190,35 @@ __global__ void __launch_bounds__(32 * MC_WARPS) k_mc(McVol V, TileLookup T, uin
   if (leaf >= n) return;
   float* W = tile[w];
   const int4 org = V.org[leaf];
-  const float* lv = V.val + leaf * 512;
-  const uint32_t* lm = V.msk + leaf * 16;
-  for (int k = lane; k < 512; k += 32)
-    W[t9(k >> 6, (k >> 3) & 7, k & 7)] = ((lm[k >> 5] >> (k & 31)) & 1u) ? lv[k] : INFINITY;
+  // the leaf: four float4 per lane (voxels 4 k4 .. 4 k4 + 3, k4 = lane + 32 j)
+  // and its mask words, every load issued before the first store
+  {
+    const float4* lv4 = reinterpret_cast<const float4*>(V.val + leaf * 512);
+    float4 in4[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) in4[j] = lv4[lane + 32 * j];
+    const uint32_t mw = lane < 16 ? V.msk[leaf * 16 + lane] : 0u;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int k4 = lane + 32 * j, k = 4 * k4;
+      const uint32_t m = __shfl_sync(0xffffffffu, mw, k4 >> 3) >> (4 * (k4 & 7));
+      const int base = t9(k >> 6, (k >> 3) & 7, k & 7);  // z, z + 1, z + 2, z + 3 follow
+      W[base] = (m & 1u) ? in4[j].x : INFINITY;
+      W[base + 1] = (m & 2u) ? in4[j].y : INFINITY;
+      W[base + 2] = (m & 4u) ? in4[j].z : INFINITY;
+      W[base + 3] = (m & 8u) ? in4[j].w : INFINITY;
+    }
+  }
   // neighbours +x, +y, +z, +x+y, +x+z, +y+z, +x+y+z
   if (lane < 7) {
     const int d = lane + 1;  // bit 0: x, bit 1: y, bit 2: z
     snb[w][lane] = V.hash.find(org.x + ((d & 1) ? 8 : 0), org.y + ((d & 2) ? 8 : 0), org.z + ((d & 4) ? 8 : 0));
   }
   __syncwarp();
-  // the 217 halo cells: x = 8 or y = 8 or z = 8
+  // the 217 halo cells: x = 8 or y = 8 or z = 8 (loop unrolled so that the
+  // seven rounds' loads overlap; a neighbour's value is loaded with its mask
+  // word rather than after it)
+#pragma unroll
   for (int k = lane; k < 217; k += 32) {
     int x, y, z;
     if (k < 64) { x = 8; y = k >> 3; z = k & 7; }
@@ -215,7 +233,9 @@ __global__ void __launch_bounds__(32 * MC_WARPS) k_mc(McVol V, TileLookup T, uin
     float val = INFINITY;
     if (n_leaf >= 0) {
       const int o = ((x & 7) << 6) | ((y & 7) << 3) | (z & 7);
-      if ((V.msk[uint64_t(n_leaf) * 16 + (o >> 5)] >> (o & 31)) & 1u) val = V.val[uint64_t(n_leaf) * 512 + o];
+      const uint32_t mword = V.msk[uint64_t(n_leaf) * 16 + (o >> 5)];
+      const float vv = V.val[uint64_t(n_leaf) * 512 + o];
+      if ((mword >> (o & 31)) & 1u) val = vv;
     } else {
       float tv;
       if (tile_value(T, org.x + x, org.y + y, org.z + z, tv)) val = tv;
